@@ -1,0 +1,163 @@
+"""Python host API over the C ABI: contexts, device collections, joins.
+
+    ctx = Context()                      # one CUDA stream on one GB300
+    coll = ctx.upload(tokens, sizes)     # device_collection (collection.hpp:54-71)
+    res = ctx.self_join(coll, threshold=0.8)            # R join R
+    res = ctx.rs_join(indexed, probe, threshold=0.8)    # R join S
+    res.pairs  # (count, 2) uint32 (probe id, indexed id); res.count
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import _lib
+from ._lib import SIM, TECH, TECH_NAMES, JoinDesc, JoinOpts, U32P, check, load
+
+
+@dataclass
+class JoinResult:
+    count: int
+    pairs: Optional[np.ndarray]  # None when count_only or device_pairs
+    technique: str
+    device_ms: float
+    kernel_ms: float = 0.0
+    stats: Optional[list] = None
+    device_pairs: int = 0  # device address when device_pairs was requested
+
+
+def make_opts(threshold: float = 0.8, sim: str = "jaccard", technique: str = "auto", bitmap: int = 0,
+              count_only: bool = False, verify_mode: int = 0, sort_pairs: bool = False,
+              pair_capacity: int = 0, device_pairs: bool = False, collect_stats: bool = False) -> JoinOpts:
+    if sim not in SIM:
+        raise ValueError(f"unknown similarity {sim!r}")
+    if technique not in TECH:
+        raise ValueError(f"unknown technique {technique!r}")
+    return JoinOpts(SIM[sim], float(threshold), TECH[technique], int(bitmap), int(bool(count_only)),
+                    int(verify_mode), int(bool(sort_pairs)), int(pair_capacity), int(bool(device_pairs)),
+                    int(bool(collect_stats)))
+
+
+def _take_result(lib, r) -> JoinResult:
+    try:
+        n = lib.hyset_result_count(r)
+        ptr = lib.hyset_result_pairs(r)
+        pairs = None
+        if ptr:
+            pairs = (np.ctypeslib.as_array(C.cast(ptr, U32P), (2 * n,)).reshape(n, 2).copy() if n
+                     else np.zeros((0, 2), np.uint32))
+        st = (C.c_uint64 * 8)()
+        k = lib.hyset_result_stats(r, st, 8)
+        return JoinResult(int(n), pairs, TECH_NAMES.get(lib.hyset_result_technique(r), "?"),
+                          float(lib.hyset_result_device_ms(r)), float(lib.hyset_result_kernel_ms(r)),
+                          [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0))
+    finally:
+        lib.hyset_result_free(r)
+
+
+class DeviceCollection:
+    """A size-sorted collection resident in HBM (the reference's device_collection)."""
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p, n: int, keep=None):
+        self._ctx = ctx
+        self.handle = handle
+        self.n = n
+        self._keep = keep  # host/device arrays that must outlive the handle
+
+    def free(self):
+        if self.handle:
+            load().hyset_collection_free(self._ctx.handle, self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self._ctx.handle:
+                self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        self._lib = load()
+        h = C.c_void_p()
+        check(self._lib.hyset_create(device, C.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self._lib.hyset_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def last_error(self) -> str:
+        return self._lib.hyset_last_error(self.handle).decode()
+
+    # ---- collections
+    def upload(self, tokens, sizes, starts=None) -> DeviceCollection:
+        tok = np.ascontiguousarray(tokens, dtype=np.uint32)
+        sz = np.ascontiguousarray(sizes, dtype=np.uint32)
+        st = None if starts is None else np.ascontiguousarray(starts, dtype=np.uint32)
+        h = C.c_void_p()
+        check(self._lib.hyset_collection_upload(
+            self.handle, tok.ctypes.data_as(U32P), tok.size, None if st is None else st.ctypes.data_as(U32P),
+            sz.ctypes.data_as(U32P), sz.size, C.byref(h)), self.handle)
+        return DeviceCollection(self, h, int(sz.size))
+
+    def from_device(self, d_tokens: int, n_tokens: int, d_starts: int, d_sizes: int, n_sets: int,
+                    keep=None) -> DeviceCollection:
+        """Wraps CSR arrays already in device memory (raw device pointers)."""
+        h = C.c_void_p()
+        check(self._lib.hyset_collection_from_device(self.handle, C.c_void_p(d_tokens), n_tokens,
+                                                     C.c_void_p(d_starts), C.c_void_p(d_sizes), n_sets,
+                                                     C.byref(h)), self.handle)
+        return DeviceCollection(self, h, n_sets, keep)
+
+    # ---- joins
+    def self_join(self, coll: DeviceCollection, threshold: float = 0.8, **kw) -> JoinResult:
+        o = make_opts(threshold, **kw)
+        r = C.c_void_p()
+        check(self._lib.hyset_self_join(self.handle, coll.handle, C.byref(o), C.byref(r)), self.handle)
+        return _take_result(self._lib, r)
+
+    def rs_join(self, indexed: DeviceCollection, probe: DeviceCollection, threshold: float = 0.8,
+                **kw) -> JoinResult:
+        o = make_opts(threshold, **kw)
+        r = C.c_void_p()
+        check(self._lib.hyset_rs_join(self.handle, indexed.handle, probe.handle, C.byref(o), C.byref(r)),
+              self.handle)
+        return _take_result(self._lib, r)
+
+    def batch_join(self, joins: Sequence[tuple]) -> list:
+        """joins: (indexed, probe_or_None, opts_kwargs) triples."""
+        n = len(joins)
+        descs = (JoinDesc * max(n, 1))()
+        for i, (R, S, kw) in enumerate(joins):
+            descs[i].indexed = R.handle
+            descs[i].probe = S.handle if S is not None else None
+            descs[i].opts = make_opts(**kw)
+        res = (C.c_void_p * max(n, 1))()
+        check(self._lib.hyset_batch_join(self.handle, descs, n, res), self.handle)
+        return [_take_result(self._lib, C.c_void_p(res[i])) for i in range(n)]
+
+
+def sorted_pairs(pairs: np.ndarray) -> np.ndarray:
+    p = np.asarray(pairs, dtype=np.uint32).reshape(-1, 2)
+    if p.shape[0] == 0:
+        return p
+    key = (p[:, 0].astype(np.uint64) << np.uint64(32)) | p[:, 1].astype(np.uint64)
+    return p[np.argsort(key, kind="stable")]

@@ -1,0 +1,917 @@
+// capi.cu — the C ABI (include/hyset_gb300.h): contexts, collections, bound
+// tables, index builds, joins, the reference-shaped handlers and the candidate
+// verifier.  Host code; every device step runs on the context's stream.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "internal.h"
+
+using namespace hs;
+
+namespace {
+
+// ---------------------------------------------------------------- errors
+hyset_status fail(hyset_ctx* ctx, hyset_status st, const char* what, cudaError_t e = cudaSuccess) {
+    if (ctx) {
+        char buf[512];
+        if (e != cudaSuccess)
+            std::snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+        else
+            std::snprintf(buf, sizeof buf, "%s", what);
+        ctx->err = buf;
+    }
+    return st;
+}
+
+#define CK(call)                                                                        \
+    do {                                                                                \
+        cudaError_t _e = (call);                                                        \
+        if (_e != cudaSuccess)                                                          \
+            return fail(ctx, _e == cudaErrorMemoryAllocation ? HYSET_E_NOMEM : HYSET_E_CUDA, #call, _e); \
+    } while (0)
+
+#define ST(call)                                \
+    do {                                        \
+        hyset_status _s = (call);               \
+        if (_s != HYSET_OK) return _s;          \
+    } while (0)
+
+// ---------------------------------------------------------------- bounds
+// The reference's similarity bounds (include/hyset/similarity.hpp:11-54) in the
+// same double expressions; this translation unit is compiled without
+// multiply-add contraction so the doubles match the reference bit for bit.
+// Cosine and dice have no reference code and follow the same style.
+int imin(int a, int b) { return (a > b) ? b : a; }
+
+uint32_t sim_minoverlap(int sim, uint32_t l1, uint32_t l2, double t) {
+    switch (sim) {
+    case SIM_COSINE: return (uint32_t)(std::ceil(t * std::sqrt((double)l1 * (double)l2)));
+    case SIM_DICE: return (uint32_t)(std::ceil(t * (double)(l1 + l2) / 2.0));
+    default: return (uint32_t)(std::ceil((double)(l1 + l2) * t / (1 + t)));
+    }
+}
+uint32_t minsize_of(int sim, uint32_t len, double t) {
+    switch (sim) {
+    case SIM_COSINE: return (uint32_t)(std::ceil(t * t * (double)len));
+    case SIM_DICE: return (uint32_t)(std::ceil(t * (double)len / (2.0 - t)));
+    default: return (uint32_t)(std::ceil(t * (double)len));
+    }
+}
+uint32_t minoverlap_of(int sim, uint32_t l1, uint32_t l2, double t) {
+    return (uint32_t)imin((int)l2, imin((int)l1, (int)sim_minoverlap(sim, l1, l2, t)));
+}
+uint32_t maxprefix_of(int sim, uint32_t len, double t) {
+    return (uint32_t)imin((int)len, (int)(len - minsize_of(sim, len, t) + 1));
+}
+uint32_t midprefix_of(int sim, uint32_t len, double t) {
+    return (uint32_t)imin((int)len, (int)(len - minoverlap_of(sim, len, len, t) + 1));
+}
+
+constexpr uint64_t MAX_COSINE_TABLE = 64ull << 20;  // entries
+
+hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int index_maxprefix, Bounds** out) {
+    auto key = std::make_tuple(sim, tau, L, index_maxprefix);
+    auto it = ctx->bounds.find(key);
+    if (it != ctx->bounds.end()) {
+        *out = it->second.get();
+        return HYSET_OK;
+    }
+    auto b = std::make_unique<Bounds>();
+    b->sim = sim;
+    b->tau = tau;
+    b->L = L;
+    b->index_maxprefix = index_maxprefix;
+    b->minsize.resize(L + 1);
+    b->probe_prefix.resize(L + 1);
+    b->index_prefix.resize(L + 1);
+    b->max_partner.resize(L + 1);
+    for (uint32_t l = 0; l <= L; ++l) {
+        b->minsize[l] = minsize_of(sim, l, tau);
+        b->probe_prefix[l] = l ? maxprefix_of(sim, l, tau) : 0;
+        b->index_prefix[l] = l ? (index_maxprefix ? maxprefix_of(sim, l, tau) : midprefix_of(sim, l, tau)) : 0;
+        if (b->minsize[l] > l) return fail(ctx, HYSET_E_INVALID, "threshold yields minsize > set size");
+    }
+    uint32_t q = 0;
+    for (uint32_t l = 0; l <= L; ++l) {
+        while (q + 1 <= L && b->minsize[q + 1] <= l) ++q;
+        b->max_partner[l] = q;
+    }
+    if (sim == SIM_COSINE) {
+        b->mo_row.resize((size_t)L + 2);
+        uint64_t run = 0;
+        for (uint32_t big = 0; big <= L; ++big) {
+            b->mo_row[big] = run;
+            run += (uint64_t)(big - b->minsize[big] + 1);
+        }
+        b->mo_row[L + 1] = run;
+        if (run > MAX_COSINE_TABLE)
+            return fail(ctx, HYSET_E_UNSUPPORTED, "cosine bound table too large for the longest set");
+        b->mo_tab.resize(run);
+        for (uint32_t big = 0; big <= L; ++big)
+            for (uint32_t small = b->minsize[big]; small <= big; ++small)
+                b->mo_tab[b->mo_row[big] + (small - b->minsize[big])] = sim_minoverlap(sim, big, small, tau);
+        b->mo_sum.assign(1, 0);
+    } else {
+        b->mo_sum.resize(2 * (size_t)L + 1);
+        for (uint32_t s = 0; s <= 2 * L; ++s) b->mo_sum[s] = sim_minoverlap(sim, s, 0, tau);
+        b->mo_row.assign(1, 0);
+        b->mo_tab.assign(1, 0);
+    }
+    // one device allocation holding all tables
+    size_t n32 = 4 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size();
+    size_t bytes = b->mo_row.size() * 8 + n32 * 4;
+    CK(b->dev.ensure(bytes, ctx->stream));
+    uint8_t* base = b->dev.as<uint8_t>();
+    uint64_t* d_row = (uint64_t*)base;
+    uint32_t* p = (uint32_t*)(base + b->mo_row.size() * 8);
+    auto put = [&](const std::vector<uint32_t>& v, uint32_t*& dst) -> cudaError_t {
+        uint32_t* d = p;
+        p += v.size();
+        dst = d;
+        return cudaMemcpyAsync(d, v.data(), v.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
+    };
+    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_sum, *d_tab;
+    CK(cudaMemcpyAsync(d_row, b->mo_row.data(), b->mo_row.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(put(b->minsize, d_minsize));
+    CK(put(b->probe_prefix, d_pp));
+    CK(put(b->index_prefix, d_ip));
+    CK(put(b->max_partner, d_mp));
+    CK(put(b->mo_sum, d_sum));
+    CK(put(b->mo_tab, d_tab));
+    CK(cudaStreamSynchronize(ctx->stream));
+    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_sum, d_row, d_tab, L, sim};
+    *out = b.get();
+    ctx->bounds.emplace(key, std::move(b));
+    return HYSET_OK;
+}
+
+// first_ge[l] = first id of the collection with size >= l, l in [0, L+1].
+hyset_status upload_first_ge(hyset_ctx* ctx, const hyset_coll* c, uint32_t L, DevBuf& buf) {
+    std::vector<uint32_t> f((size_t)L + 2);
+    for (uint32_t l = 0; l <= L + 1; ++l)
+        f[l] = (uint32_t)(std::lower_bound(c->h_sizes.begin(), c->h_sizes.end(), l) - c->h_sizes.begin());
+    CK(buf.ensure(f.size() * 4, ctx->stream));
+    CK(cudaMemcpyAsync(buf.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // f goes out of scope
+    return HYSET_OK;
+}
+
+int key_bits_for(uint32_t universe) {
+    int bits = 1;
+    while (bits < 32 && (universe - 1) >> bits) ++bits;
+    return bits;
+}
+
+// Global inverted index over the prefix entries of every set, lists ordered by
+// set id: histogram + scan give the list offsets, a stable radix sort by token
+// of the entries (emitted in set order) gives the order inside each list.
+hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, int kind) {
+    // Rebuilt on every join (buffers are reused): a join's timed device work
+    // always includes its own index build.
+    Index& ix = c->index;
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = c->n, U = c->universe;
+    uint64_t E = 0;
+    const std::vector<uint32_t>& pre = b->index_prefix;
+    for (uint32_t i = 0; i < n; ++i) E += pre[c->h_sizes[i]];
+    if (E >= (1ull << 32)) return fail(ctx, HYSET_E_UNSUPPORTED, "more than 2^32 prefix entries");
+    const uint64_t E1 = E ? E : 1;
+    CK(ctx->s_len.ensure((size_t)n * 4 + 4, s));
+    CK(ctx->s_off.ensure((size_t)n * 4 + 4, s));
+    CK(ctx->s_tok.ensure(E1 * 4, s));
+    CK(ctx->s_set.ensure(E1 * 4, s));
+    CK(ctx->s_pos.ensure(E1 * 4, s));
+    CK(ctx->s_order.ensure(E1 * 4, s));
+    CK(ctx->s_altk.ensure(E1 * 4, s));
+    CK(ctx->s_altv.ensure(E1 * 4, s));
+    CK(ctx->s_counts.ensure(((size_t)U + 1) * 4, s));
+    size_t scan_words = std::max(std::max(scan_scratch_words(n), scan_scratch_words((uint64_t)U + 1)),
+                                 radix_scratch_words(E1));
+    CK(ctx->s_scan.ensure(scan_words * 4, s));
+    CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
+    CK(ix.set.ensure(E1 * 4, s));
+    CK(ix.pos.ensure(E1 * 4, s));
+    CollView v = c->view();
+    uint32_t* len = ctx->s_len.as<uint32_t>();
+    uint32_t* off = ctx->s_off.as<uint32_t>();
+    uint32_t* scr = ctx->s_scan.as<uint32_t>();
+    CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
+    CK(scan_exclusive(len, off, n, scr, s));
+    CK(emit_prefix_entries(v, 0, n, off, len, ctx->s_tok.as<uint32_t>(), ctx->s_set.as<uint32_t>(),
+                           ctx->s_pos.as<uint32_t>(), s));
+    uint32_t* counts = ctx->s_counts.as<uint32_t>();
+    CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+    CK(token_histogram(ctx->s_tok.as<uint32_t>(), E, counts, s));
+    CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
+    CK(iota_u32(ctx->s_order.as<uint32_t>(), E, s));
+    CK(radix_sort_pairs(ctx->s_tok.as<uint32_t>(), ctx->s_order.as<uint32_t>(), ctx->s_altk.as<uint32_t>(),
+                        ctx->s_altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
+    CK(gather_entries(ctx->s_order.as<uint32_t>(), E, ctx->s_set.as<uint32_t>(), ctx->s_pos.as<uint32_t>(),
+                      ix.set.as<uint32_t>(), ix.pos.as<uint32_t>(), s));
+    ix.sim = b->sim;
+    ix.tau = b->tau;
+    ix.kind = kind;
+    ix.universe = U;
+    ix.entries = E;
+    return HYSET_OK;
+}
+
+// Signatures are regenerated on every join (the buffer is reused).
+hyset_status get_bitmaps(hyset_ctx* ctx, hyset_coll* c, int words, const uint64_t** out) {
+    DevBuf& d = c->bitmaps[words];
+    CK(d.ensure((size_t)c->n * words * 8 + 8, ctx->stream));
+    CK(generate_bitmaps(c->view(), words, d.as<uint64_t>(), ctx->stream));
+    *out = d.as<uint64_t>();
+    return HYSET_OK;
+}
+
+hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
+    if (!o) return fail(ctx, HYSET_E_INVALID, "null options");
+    if (!(o->threshold > 0.0 && o->threshold <= 1.0)) return fail(ctx, HYSET_E_INVALID, "threshold must be in (0, 1]");
+    if (o->sim < HYSET_JACCARD || o->sim > HYSET_DICE) return fail(ctx, HYSET_E_INVALID, "unknown similarity");
+    if (o->technique < HYSET_TECH_AUTO || o->technique > HYSET_TECH_DIRECT)
+        return fail(ctx, HYSET_E_INVALID, "unknown technique");
+    if (o->bitmap_bits != 0 && o->bitmap_bits != 64 && o->bitmap_bits != 128 && o->bitmap_bits != 256 &&
+        o->bitmap_bits != 512)
+        return fail(ctx, HYSET_E_INVALID, "bitmap_bits must be 0, 64, 128, 256 or 512");
+    if (o->verify_mode > 2) return fail(ctx, HYSET_E_INVALID, "verify_mode must be 0, 1 or 2");
+    return HYSET_OK;
+}
+
+// Heuristic technique choice used until the learned selector is loaded: short
+// sets favour enumerating the length window with signatures, long sets the
+// prefix index.
+hyset_technique choose_technique(const hyset_coll* R, const hyset_join_opts* o) {
+    double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
+    if (R->n <= 20000 && avg <= 64) return HYSET_TECH_BITMAP;
+    (void)o;
+    return HYSET_TECH_FGSS;
+}
+
+int choose_vmode(const hyset_coll* R, const hyset_join_opts* o) {
+    if (o->verify_mode) return (int)o->verify_mode;
+    double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
+    return avg <= 48 ? 1 : 2;
+}
+
+// Runs one configured join launch into the context's pair buffer, growing the
+// buffer and re-running when the first pass overflowed.
+hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const hyset_join_opts* o,
+                      hyset_result* res, bool timed_from_ev0) {
+    cudaStream_t s = ctx->stream;
+    const int count_only = o->count_only ? 1 : 0;
+    uint64_t cap = o->pair_capacity ? o->pair_capacity : std::max<uint64_t>(1u << 20, 4ull * P.S.n);
+    if (count_only) cap = 0;
+    CK(ctx->s_count.ensure(16, s));
+    CK(ctx->s_work.ensure(16, s));
+    CK(ctx->s_stats.ensure(64, s));
+    P.stats = o->collect_stats ? ctx->s_stats.as<unsigned long long>() : nullptr;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (!count_only) CK(ctx->s_pairs.ensure(std::max<uint64_t>(cap, 1) * sizeof(uint2), s));
+        P.out.pairs = count_only ? nullptr : ctx->s_pairs.as<uint2>();
+        P.out.count = ctx->s_count.as<unsigned long long>();
+        P.out.cap = cap;
+        P.out.count_only = count_only;
+        P.work = ctx->s_work.as<unsigned int>();
+        if (!timed_from_ev0 || attempt > 0) CK(cudaEventRecord(ctx->ev0, s));
+        CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+        CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
+        if (P.stats) CK(cudaMemsetAsync(P.stats, 0, 64, s));
+        CK(cudaEventRecord(ctx->ek0, s));
+        CK(launch_join(P, tech, vmode, ctx->sm_count, s));
+        CK(cudaEventRecord(ctx->ek1, s));
+        CK(cudaEventRecord(ctx->ev1, s));
+        unsigned long long count = 0;
+        CK(cudaMemcpyAsync(&count, ctx->s_count.p, 8, cudaMemcpyDeviceToHost, s));
+        if (P.stats) CK(cudaMemcpyAsync(res->stats, P.stats, 64, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float ms = 0, kms = 0;
+        CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        CK(cudaEventElapsedTime(&kms, ctx->ek0, ctx->ek1));
+        res->device_ms = ms;
+        res->kernel_ms = kms;
+        res->count = count;
+        if (count_only || count <= cap) break;
+        cap = count + count / 8 + 1024;  // overflow: retry once with room for everything
+        if (attempt == 1) return fail(ctx, HYSET_E_OVERFLOW, "pair buffer overflow after resize");
+    }
+    if (!count_only && o->device_pairs) {
+        res->device_pairs = ctx->s_pairs.p;
+    } else if (!count_only) {
+        res->pairs.resize(res->count);
+        if (res->count)
+            CK(cudaMemcpyAsync(res->pairs.data(), ctx->s_pairs.p, res->count * sizeof(hyset_pair),
+                               cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        res->has_pairs = 1;
+    }
+    return HYSET_OK;
+}
+
+hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, hyset_result* res) {
+    ST(check_opts(ctx, o));
+    const bool self = (S == R);
+    const uint32_t L = std::max(R->max_size, S->max_size);
+    Bounds* b = nullptr;
+    ST(get_bounds(ctx, o->sim, o->threshold, L, self ? 0 : 1, &b));
+    hyset_technique tech = o->technique == HYSET_TECH_AUTO ? choose_technique(R, o) : o->technique;
+    int vmode = choose_vmode(R, o);
+    res->technique = tech;
+    CK(cudaEventRecord(ctx->ev0, ctx->stream));
+    ST(upload_first_ge(ctx, R, L, ctx->s_firstge));
+    JoinParams P{};
+    P.R = R->view();
+    P.S = S->view();
+    P.B = b->view;
+    P.first_ge = ctx->s_firstge.as<uint32_t>();
+    P.self = self ? 1 : 0;
+    P.p_lo = 0;
+    P.p_hi = S->n;
+    P.r_lo = 0;
+    P.r_hi = R->n;
+    if (tech == HYSET_TECH_FGSS) {
+        ST(build_sorted_index(ctx, R, b, self ? 0 : 1));
+        P.X = R->index.view();
+    }
+    int words = (int)(o->bitmap_bits / 64);
+    if (tech == HYSET_TECH_BITMAP && words == 0) words = 1;  // the bitmap technique needs signatures
+    if (tech == HYSET_TECH_DIRECT) words = 0;
+    if (words) {
+        const uint64_t *br = nullptr, *bs = nullptr;
+        ST(get_bitmaps(ctx, R, words, &br));
+        if (self) bs = br;
+        else ST(get_bitmaps(ctx, S, words, &bs));
+        P.bits_R = br;
+        P.bits_S = bs;
+        P.words = words;
+    }
+    int ktech = tech == HYSET_TECH_FGSS ? TECH_FGSS : (tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
+    ST(run_join(ctx, P, ktech, vmode, o, res, true));
+    if (P.X.set && o->collect_stats) {
+        res->stats[3] = R->index.entries;
+    }
+    res->stats[4] = S->n_tokens;
+    if (o->sort_pairs && res->has_pairs)
+        std::sort(res->pairs.begin(), res->pairs.end(), [](const hyset_pair& x, const hyset_pair& y) {
+            return x.first != y.first ? x.first < y.first : x.second < y.second;
+        });
+    return HYSET_OK;
+}
+
+hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
+    cudaStream_t s = ctx->stream;
+    c->h_sizes.resize(c->n);
+    if (c->n) {
+        if (h_sizes_or_null) std::memcpy(c->h_sizes.data(), h_sizes_or_null, (size_t)c->n * 4);
+        else CK(cudaMemcpyAsync(c->h_sizes.data(), c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
+    }
+    DevBuf flags;
+    CK(flags.ensure(16, s));
+    CK(cudaMemsetAsync(flags.p, 0, 16, s));
+    CK(validate_collection(c->view(), c->n_tokens, flags.as<uint32_t>(), s));
+    uint32_t f[2] = {0, 0};
+    CK(cudaMemcpyAsync(f, flags.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    flags.release(s);
+    if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
+    if (f[0] & 1) return fail(ctx, HYSET_E_INVALID, "empty set in collection");
+    if (f[0] & 2) return fail(ctx, HYSET_E_INVALID, "set tokens must be strictly ascending");
+    if (f[0] & 4) return fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size");
+    if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
+    c->universe = c->n ? f[1] + 1 : 1;
+    c->max_size = c->n ? c->h_sizes.back() : 0;
+    return HYSET_OK;
+}
+
+}  // namespace
+
+// ====================================================================== ABI
+
+extern "C" {
+
+void hyset_default_opts(hyset_join_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof *o);
+    o->sim = HYSET_JACCARD;
+    o->threshold = 0.8;
+    o->technique = HYSET_TECH_AUTO;
+}
+
+hyset_status hyset_create(int device, hyset_ctx** out) {
+    if (!out) return HYSET_E_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return HYSET_E_NODEVICE;
+    }
+    if (device < 0 && cudaGetDevice(&device) != cudaSuccess) return HYSET_E_NODEVICE;
+    if (device >= count) return HYSET_E_INVALID;
+    hyset_ctx* ctx = new (std::nothrow) hyset_ctx();
+    if (!ctx) return HYSET_E_NOMEM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ek0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ek1);
+    if (e == cudaSuccess) {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = UINT64_MAX;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+    }
+    if (e != cudaSuccess) {
+        hyset_destroy(ctx);
+        return HYSET_E_CUDA;
+    }
+    *out = ctx;
+    return HYSET_OK;
+}
+
+void hyset_destroy(hyset_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) {
+        cudaStream_t s = ctx->stream;
+        for (auto& kv : ctx->bounds) kv.second->dev.release(s);
+        DevBuf* bufs[] = {&ctx->s_len, &ctx->s_off, &ctx->s_tok, &ctx->s_set, &ctx->s_pos, &ctx->s_order,
+                          &ctx->s_altk, &ctx->s_altv, &ctx->s_counts, &ctx->s_scan, &ctx->s_firstge,
+                          &ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats};
+        for (DevBuf* b : bufs) b->release(s);
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+    }
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->ek0) cudaEventDestroy(ctx->ek0);
+    if (ctx->ek1) cudaEventDestroy(ctx->ek1);
+    delete ctx;
+}
+
+const char* hyset_last_error(const hyset_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+hyset_status hyset_collection_upload(hyset_ctx* ctx, const uint32_t* tokens, uint64_t n_tokens,
+                                     const uint32_t* starts, const uint32_t* sizes, uint32_t n_sets,
+                                     hyset_coll** out) {
+    if (!ctx || !out || (n_sets && (!sizes || (!tokens && n_tokens))))
+        return fail(ctx, HYSET_E_INVALID, "null argument");
+    if (n_tokens >= (1ull << 32)) return fail(ctx, HYSET_E_INVALID, "n_tokens must be < 2^32");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    auto c = std::make_unique<hyset_coll>();
+    c->ctx = ctx;
+    c->n = n_sets;
+    c->n_tokens = n_tokens;
+    cudaStream_t s = ctx->stream;
+    std::vector<uint32_t> st;
+    if (!starts && n_sets) {
+        st.resize(n_sets);
+        uint64_t run = 0;
+        for (uint32_t i = 0; i < n_sets; ++i) {
+            st[i] = (uint32_t)run;
+            run += sizes[i];
+        }
+        if (run > n_tokens) return fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens");
+        starts = st.data();
+    }
+    CK(c->tokens.ensure(n_tokens * 4 + 4, s));
+    CK(c->starts.ensure((size_t)n_sets * 4 + 4, s));
+    CK(c->sizes.ensure((size_t)n_sets * 4 + 4, s));
+    if (n_tokens) CK(cudaMemcpyAsync(c->tokens.p, tokens, n_tokens * 4, cudaMemcpyHostToDevice, s));
+    if (n_sets) {
+        CK(cudaMemcpyAsync(c->starts.p, starts, (size_t)n_sets * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(c->sizes.p, sizes, (size_t)n_sets * 4, cudaMemcpyHostToDevice, s));
+    }
+    c->d_tokens = c->tokens.as<uint32_t>();
+    c->d_starts = c->starts.as<uint32_t>();
+    c->d_sizes = c->sizes.as<uint32_t>();
+    hyset_status stt = make_collection(ctx, c.get(), sizes);
+    if (stt != HYSET_OK) {
+        hyset_collection_free(ctx, c.release());
+        return stt;
+    }
+    *out = c.release();
+    return HYSET_OK;
+}
+
+hyset_status hyset_collection_from_device(hyset_ctx* ctx, const uint32_t* d_tokens, uint64_t n_tokens,
+                                          const uint32_t* d_starts, const uint32_t* d_sizes, uint32_t n_sets,
+                                          hyset_coll** out) {
+    if (!ctx || !out || (n_sets && (!d_sizes || !d_starts || !d_tokens)))
+        return fail(ctx, HYSET_E_INVALID, "null argument");
+    if (n_tokens >= (1ull << 32)) return fail(ctx, HYSET_E_INVALID, "n_tokens must be < 2^32");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    auto c = std::make_unique<hyset_coll>();
+    c->ctx = ctx;
+    c->n = n_sets;
+    c->n_tokens = n_tokens;
+    c->d_tokens = d_tokens;
+    c->d_starts = d_starts;
+    c->d_sizes = d_sizes;
+    hyset_status stt = make_collection(ctx, c.get(), nullptr);
+    if (stt != HYSET_OK) {
+        hyset_collection_free(ctx, c.release());
+        return stt;
+    }
+    *out = c.release();
+    return HYSET_OK;
+}
+
+void hyset_collection_free(hyset_ctx* ctx, hyset_coll* c) {
+    if (!c) return;
+    cudaStream_t s = ctx ? ctx->stream : c->ctx->stream;
+    c->tokens.release(s);
+    c->starts.release(s);
+    c->sizes.release(s);
+    c->index.list_off.release(s);
+    c->index.set.release(s);
+    c->index.pos.release(s);
+    for (auto& kv : c->bitmaps) kv.second.release(s);
+    cudaStreamSynchronize(s);
+    delete c;
+}
+
+uint32_t hyset_collection_num_sets(const hyset_coll* c) { return c ? c->n : 0; }
+
+hyset_status hyset_self_join(hyset_ctx* ctx, const hyset_coll* coll, const hyset_join_opts* opts,
+                             hyset_result** out) {
+    if (!ctx || !coll || !out) return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    auto res = std::make_unique<hyset_result>();
+    hyset_coll* c = const_cast<hyset_coll*>(coll);  // caches (index, signatures) live in the collection
+    ST(do_join(ctx, c, c, opts, res.get()));
+    *out = res.release();
+    return HYSET_OK;
+}
+
+hyset_status hyset_rs_join(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                           const hyset_join_opts* opts, hyset_result** out) {
+    if (!ctx || !indexed || !probe || !out) return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    auto res = std::make_unique<hyset_result>();
+    hyset_coll* R = const_cast<hyset_coll*>(indexed);
+    hyset_coll* S = const_cast<hyset_coll*>(probe);
+    if (R == S) return fail(ctx, HYSET_E_INVALID, "use hyset_self_join for R join R");
+    ST(do_join(ctx, R, S, opts, res.get()));
+    *out = res.release();
+    return HYSET_OK;
+}
+
+hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_t n_joins,
+                              hyset_result** results) {
+    if (!ctx || (n_joins && (!joins || !results))) return fail(ctx, HYSET_E_INVALID, "null argument");
+    for (uint32_t i = 0; i < n_joins; ++i) results[i] = nullptr;
+    for (uint32_t i = 0; i < n_joins; ++i) {
+        const hyset_join_desc& d = joins[i];
+        hyset_status st = (d.probe == nullptr || d.probe == d.indexed)
+                              ? hyset_self_join(ctx, d.indexed, &d.opts, &results[i])
+                              : hyset_rs_join(ctx, d.indexed, d.probe, &d.opts, &results[i]);
+        if (st != HYSET_OK) {
+            for (uint32_t k = 0; k <= i; ++k) {
+                hyset_result_free(results[k]);
+                results[k] = nullptr;
+            }
+            return st;
+        }
+    }
+    return HYSET_OK;
+}
+
+uint64_t hyset_result_count(const hyset_result* r) { return r ? r->count : 0; }
+const hyset_pair* hyset_result_pairs(const hyset_result* r) {
+    return (r && r->has_pairs) ? r->pairs.data() : nullptr;
+}
+hyset_technique hyset_result_technique(const hyset_result* r) { return r ? r->technique : HYSET_TECH_AUTO; }
+double hyset_result_device_ms(const hyset_result* r) { return r ? r->device_ms : 0.0; }
+double hyset_result_kernel_ms(const hyset_result* r) { return r ? r->kernel_ms : 0.0; }
+const void* hyset_result_device_pairs(const hyset_result* r) { return r ? r->device_pairs : nullptr; }
+uint32_t hyset_result_stats(const hyset_result* r, uint64_t* out, uint32_t n) {
+    if (!r || !out) return 0;
+    uint32_t k = n < 8 ? n : 8;
+    for (uint32_t i = 0; i < k; ++i) out[i] = r->stats[i];
+    return k;
+}
+void hyset_result_free(hyset_result* r) { delete r; }
+
+// ---------------------------------------------------------------- handlers
+
+hyset_status hyset_handler_create(hyset_ctx* ctx, const hyset_coll* coll, hyset_technique technique, hyset_sim sim,
+                                  uint32_t bitmap_size, uint32_t block_size, int aggregate, double threshold,
+                                  hyset_handler** out) {
+    if (!ctx || !coll || !out) return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    if (technique != HYSET_TECH_BITMAP && technique != HYSET_TECH_FGSS)
+        return fail(ctx, HYSET_E_INVALID, "handler technique must be BITMAP or FGSS");
+    if (block_size == 0) return fail(ctx, HYSET_E_INVALID, "block size must be > 0");
+    hyset_join_opts o;
+    hyset_default_opts(&o);
+    o.sim = sim;
+    o.threshold = threshold;
+    ST(check_opts(ctx, &o));
+    if (technique == HYSET_TECH_BITMAP && bitmap_size != 64 && bitmap_size != 128 && bitmap_size != 256 &&
+        bitmap_size != 512)
+        return fail(ctx, HYSET_E_INVALID, "bitmap size must be 64, 128, 256 or 512");
+    CK(cudaSetDevice(ctx->device));
+    auto h = std::make_unique<hyset_handler>();
+    h->ctx = ctx;
+    h->coll = coll;
+    h->technique = technique;
+    h->sim = sim;
+    h->tau = threshold;
+    h->block_size = block_size;
+    h->aggregate = aggregate ? 1 : 0;
+    ST(get_bounds(ctx, sim, threshold, coll->max_size, 0, &h->bounds));
+    ST(upload_first_ge(ctx, coll, coll->max_size, h->first_ge));
+    cudaStream_t s = ctx->stream;
+    if (technique == HYSET_TECH_BITMAP) {
+        // bitmap::handler ctor generates every signature up front (device_algorithms.hpp:144-156)
+        h->words = (int)(bitmap_size / 64);
+        CK(h->bits.ensure((size_t)coll->n * h->words * 8 + 8, s));
+        CK(generate_bitmaps(coll->view(), h->words, h->bits.as<uint64_t>(), s));
+    }
+    CK(h->count.ensure(16, s));
+    CK(h->work.ensure(16, s));
+    h->cap = aggregate ? 0 : std::max<uint64_t>(1u << 16, (uint64_t)block_size * 4);
+    if (!aggregate) CK(h->pairs.ensure(h->cap * sizeof(uint2), s));
+    CK(cudaStreamSynchronize(s));
+    *out = h.release();
+    return HYSET_OK;
+}
+
+namespace {
+
+// Per-indexed-block inverted index in the reference's layout
+// (include/hyset/index.hpp:284-313): zero universe-sized counts, histogram of
+// the block's prefix entries, exclusive scan, atomic scatter (lists unsorted).
+hyset_status build_block_index(hyset_handler* h, const hyset_block& blk) {
+    hyset_ctx* ctx = h->ctx;
+    cudaStream_t s = ctx->stream;
+    const hyset_coll* c = h->coll;
+    const uint32_t lo = blk.start_id, hi = blk.end_id + 1, nb = hi - lo, U = c->universe;
+    uint64_t E = 0;
+    for (uint32_t i = lo; i < hi; ++i) E += h->bounds->index_prefix[c->h_sizes[i]];
+    const uint64_t E1 = E ? E : 1;
+    CK(h->counts.ensure(((size_t)U + 1) * 4, s));
+    CK(h->list_off.ensure(((size_t)U + 1) * 4, s));
+    CK(h->e_len.ensure((size_t)nb * 4 + 4, s));
+    CK(h->e_off.ensure((size_t)nb * 4 + 4, s));
+    CK(h->e_tok.ensure(E1 * 4, s));
+    CK(h->e_set.ensure(E1 * 4, s));
+    CK(h->e_pos.ensure(E1 * 4, s));
+    CK(h->idx_set.ensure(E1 * 4, s));
+    CK(h->idx_pos.ensure(E1 * 4, s));
+    CK(h->scan.ensure(std::max(scan_scratch_words(nb), scan_scratch_words((uint64_t)U + 1)) * 4, s));
+    CollView v = c->view();
+    uint32_t* scr = h->scan.as<uint32_t>();
+    CK(set_prefix_lengths(v, h->bounds->view.index_prefix, lo, hi, h->e_len.as<uint32_t>(), s));
+    CK(scan_exclusive(h->e_len.as<uint32_t>(), h->e_off.as<uint32_t>(), nb, scr, s));
+    CK(emit_prefix_entries(v, lo, hi, h->e_off.as<uint32_t>(), h->e_len.as<uint32_t>(), h->e_tok.as<uint32_t>(),
+                           h->e_set.as<uint32_t>(), h->e_pos.as<uint32_t>(), s));
+    CK(cudaMemsetAsync(h->counts.p, 0, ((size_t)U + 1) * 4, s));
+    CK(token_histogram(h->e_tok.as<uint32_t>(), E, h->counts.as<uint32_t>(), s));
+    CK(scan_exclusive(h->counts.as<uint32_t>(), h->list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
+    // the scatter advances a cursor copy of the list starts
+    CK(cudaMemcpyAsync(h->counts.p, h->list_off.p, ((size_t)U + 1) * 4, cudaMemcpyDeviceToDevice, s));
+    CK(scatter_entries(h->e_tok.as<uint32_t>(), h->e_set.as<uint32_t>(), h->e_pos.as<uint32_t>(), E,
+                       h->counts.as<uint32_t>(), h->idx_set.as<uint32_t>(), h->idx_pos.as<uint32_t>(), s));
+    h->indexed_block = blk.id;
+    return HYSET_OK;
+}
+
+hyset_status check_block(hyset_ctx* ctx, const hyset_coll* c, const hyset_block* b) {
+    if (!b || b->start_id > b->end_id || b->end_id >= c->n) return fail(ctx, HYSET_E_INVALID, "bad block range");
+    return HYSET_OK;
+}
+
+}  // namespace
+
+hyset_status hyset_handler_join_blocks(hyset_handler* h, const hyset_block* first, const hyset_block* second) {
+    if (!h) return HYSET_E_INVALID;
+    hyset_ctx* ctx = h->ctx;
+    ST(check_block(ctx, h->coll, first));
+    ST(check_block(ctx, h->coll, second));
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    if (h->technique == HYSET_TECH_FGSS && h->indexed_block != first->id) ST(build_block_index(h, *first));
+    JoinParams P{};
+    P.R = h->coll->view();
+    P.S = P.R;
+    P.B = h->bounds->view;
+    P.first_ge = h->first_ge.as<uint32_t>();
+    P.self = 1;
+    P.p_lo = second->start_id;
+    P.p_hi = second->end_id + 1;
+    P.r_lo = first->start_id;
+    P.r_hi = first->end_id + 1;
+    if (h->technique == HYSET_TECH_FGSS) {
+        P.X.list_off = h->list_off.as<uint32_t>();
+        P.X.set = h->idx_set.as<uint32_t>();
+        P.X.pos = h->idx_pos.as<uint32_t>();
+        P.X.universe = h->coll->universe;
+        P.X.sorted = 0;
+    } else {
+        P.bits_R = P.bits_S = h->bits.as<uint64_t>();
+        P.words = h->words;
+    }
+    const int tech = h->technique == HYSET_TECH_FGSS ? TECH_FGSS : TECH_BITMAP;
+    const int vmode = 1;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        P.out.pairs = h->aggregate ? nullptr : h->pairs.as<uint2>();
+        P.out.count = h->count.as<unsigned long long>();
+        P.out.cap = h->cap;
+        P.out.count_only = h->aggregate;
+        P.work = h->work.as<unsigned int>();
+        CK(cudaMemsetAsync(h->count.p, 0, 16, s));
+        CK(cudaMemsetAsync(h->work.p, 0, 16, s));
+        CK(launch_join(P, tech, vmode, ctx->sm_count, s));
+        unsigned long long count = 0;
+        CK(cudaMemcpyAsync(&count, h->count.p, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h->aggregate) {
+            h->out_count += count;
+            return HYSET_OK;
+        }
+        if (count <= h->cap) {
+            size_t old = h->out_pairs.size();
+            h->out_pairs.resize(old + count);
+            if (count)
+                CK(cudaMemcpyAsync(h->out_pairs.data() + old, h->pairs.p, count * sizeof(hyset_pair),
+                                   cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            h->out_count += count;
+            return HYSET_OK;
+        }
+        h->cap = count + count / 4 + 1024;
+        CK(h->pairs.ensure(h->cap * sizeof(uint2), s));
+    }
+    return fail(ctx, HYSET_E_OVERFLOW, "handler pair buffer overflow after resize");
+}
+
+hyset_status hyset_handler_join_partitions(hyset_handler* h, const hyset_block* first, uint32_t n_first,
+                                           const hyset_block* second, uint32_t n_second) {
+    if (!h || (n_first && !first) || (n_second && !second)) return HYSET_E_INVALID;
+    // device::length_filter (device_algorithms.hpp:21-53): probe block id >= indexed
+    // block id and size[last indexed] >= minsize(size[first probe]).
+    for (uint32_t i = 0; i < n_first; ++i) {
+        ST(check_block(h->ctx, h->coll, &first[i]));
+        for (uint32_t k = 0; k < n_second; ++k) {
+            ST(check_block(h->ctx, h->coll, &second[k]));
+            if (second[k].id < first[i].id) continue;
+            uint32_t last_indexed = h->coll->h_sizes[first[i].end_id];
+            uint32_t first_probe = h->coll->h_sizes[second[k].start_id];
+            if (last_indexed >= h->bounds->minsize[first_probe]) ST(hyset_handler_join_blocks(h, &first[i], &second[k]));
+        }
+    }
+    return HYSET_OK;
+}
+
+hyset_status hyset_handler_output(const hyset_handler* h, uint64_t* count, const hyset_pair** pairs) {
+    if (!h) return HYSET_E_INVALID;
+    if (count) *count = h->out_count;
+    if (pairs) *pairs = h->aggregate ? nullptr : h->out_pairs.data();
+    return HYSET_OK;
+}
+
+hyset_status hyset_handler_clear_output(hyset_handler* h) {
+    if (!h) return HYSET_E_INVALID;
+    h->out_count = 0;
+    h->out_pairs.clear();
+    return HYSET_OK;
+}
+
+void hyset_handler_destroy(hyset_handler* h) {
+    if (!h) return;
+    cudaStream_t s = h->ctx->stream;
+    DevBuf* bufs[] = {&h->first_ge, &h->counts, &h->list_off, &h->e_len, &h->e_off, &h->e_tok, &h->e_set, &h->e_pos,
+                      &h->idx_set, &h->idx_pos, &h->scan, &h->bits, &h->pairs, &h->count, &h->work};
+    for (DevBuf* b : bufs) b->release(s);
+    cudaStreamSynchronize(s);
+    delete h;
+}
+
+// ---------------------------------------------------------------- verifier
+
+hyset_status hyset_verifier_create(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe, hyset_sim sim,
+                                   uint32_t threads, uint32_t scenario, int aggregate, uint32_t max_probes,
+                                   uint32_t max_candidates, double threshold, hyset_verifier** out) {
+    (void)threads;  // the reference's CTA width; here one warp verifies a probe's candidates
+    if (!ctx || !indexed || !probe || !out) return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    if (scenario != 1 && scenario != 2) return fail(ctx, HYSET_E_INVALID, "scenario must be 1 or 2");
+    if (max_probes == 0 || max_candidates == 0) return fail(ctx, HYSET_E_INVALID, "capacities must be > 0");
+    hyset_join_opts o;
+    hyset_default_opts(&o);
+    o.sim = sim;
+    o.threshold = threshold;
+    ST(check_opts(ctx, &o));
+    CK(cudaSetDevice(ctx->device));
+    auto v = std::make_unique<hyset_verifier>();
+    v->ctx = ctx;
+    v->indexed = indexed;
+    v->probe = probe;
+    v->scenario = scenario;
+    v->aggregate = aggregate ? 1 : 0;
+    v->max_probes = max_probes;
+    v->max_candidates = max_candidates;
+    ST(get_bounds(ctx, sim, threshold, std::max(indexed->max_size, probe->max_size), 0, &v->bounds));
+    cudaStream_t s = ctx->stream;
+    CK(v->d_probes.ensure((size_t)max_probes * 4 + 8, s));
+    CK(v->d_offsets.ensure((size_t)max_probes * 4 + 8, s));
+    CK(v->d_cands.ensure((size_t)max_candidates * 4 + 4, s));
+    CK(v->pairs.ensure((size_t)max_candidates * sizeof(uint2), s));
+    CK(v->count.ensure(16, s));
+    CK(v->work.ensure(16, s));
+    CK(cudaStreamSynchronize(s));
+    *out = v.release();
+    return HYSET_OK;
+}
+
+namespace {
+hyset_status verifier_run(hyset_verifier* v) {
+    hyset_ctx* ctx = v->ctx;
+    cudaStream_t s = ctx->stream;
+    const uint32_t np = (uint32_t)v->h_probes.size();
+    if (np == 0) return HYSET_OK;
+    CK(cudaMemcpyAsync(v->d_probes.p, v->h_probes.data(), (size_t)np * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(v->d_offsets.p, v->h_offsets.data(), (size_t)np * 4, cudaMemcpyHostToDevice, s));
+    if (!v->h_cands.empty())
+        CK(cudaMemcpyAsync(v->d_cands.p, v->h_cands.data(), v->h_cands.size() * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(v->count.p, 0, 16, s));
+    CK(cudaMemsetAsync(v->work.p, 0, 16, s));
+    Sink out{v->aggregate ? nullptr : v->pairs.as<uint2>(), v->count.as<unsigned long long>(),
+             (unsigned long long)v->max_candidates, v->aggregate};
+    CK(launch_verify_candidates(v->indexed->view(), v->probe->view(), v->bounds->view, v->d_probes.as<uint32_t>(),
+                                v->d_offsets.as<uint32_t>(), v->d_cands.as<uint32_t>(), np, (int)v->scenario, out,
+                                v->work.as<unsigned int>(), ctx->sm_count, s));
+    unsigned long long count = 0;
+    CK(cudaMemcpyAsync(&count, v->count.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (!v->aggregate && count) {
+        size_t old = v->out_pairs.size();
+        v->out_pairs.resize(old + count);
+        CK(cudaMemcpyAsync(v->out_pairs.data() + old, v->pairs.p, count * sizeof(hyset_pair), cudaMemcpyDeviceToHost,
+                           s));
+        CK(cudaStreamSynchronize(s));
+    }
+    v->out_count += count;
+    v->h_probes.clear();
+    v->h_offsets.clear();
+    v->h_cands.clear();
+    return HYSET_OK;
+}
+}  // namespace
+
+hyset_status hyset_verifier_add_candidates(hyset_verifier* v, uint32_t probe_id, const uint32_t* candidates,
+                                           uint32_t n) {
+    if (!v || (n && !candidates)) return HYSET_E_INVALID;
+    hyset_ctx* ctx = v->ctx;
+    if (probe_id >= v->probe->n) return fail(ctx, HYSET_E_INVALID, "probe id out of range");
+    for (uint32_t k = 0; k < n; ++k)
+        if (candidates[k] >= v->indexed->n) return fail(ctx, HYSET_E_INVALID, "candidate id out of range");
+    // addCandidates (hybrid_algorithms.hpp:71-105): a candidate set that does not
+    // fit is split; the full batch is verified before the rest is queued.
+    uint32_t done = 0;
+    do {
+        if (v->h_probes.size() >= v->max_probes || v->h_cands.size() >= v->max_candidates) ST(verifier_run(v));
+        uint32_t room = v->max_candidates - (uint32_t)v->h_cands.size();
+        uint32_t take = std::min(room, n - done);
+        v->h_probes.push_back(probe_id);
+        v->h_cands.insert(v->h_cands.end(), candidates + done, candidates + done + take);
+        v->h_offsets.push_back((uint32_t)v->h_cands.size());
+        done += take;
+    } while (done < n);
+    return HYSET_OK;
+}
+
+hyset_status hyset_verifier_flush(hyset_verifier* v) {
+    if (!v) return HYSET_E_INVALID;
+    return verifier_run(v);
+}
+
+hyset_status hyset_verifier_output(const hyset_verifier* v, uint64_t* count, const hyset_pair** pairs) {
+    if (!v) return HYSET_E_INVALID;
+    if (count) *count = v->out_count;
+    if (pairs) *pairs = v->aggregate ? nullptr : v->out_pairs.data();
+    return HYSET_OK;
+}
+
+void hyset_verifier_destroy(hyset_verifier* v) {
+    if (!v) return;
+    cudaStream_t s = v->ctx->stream;
+    DevBuf* bufs[] = {&v->d_probes, &v->d_offsets, &v->d_cands, &v->pairs, &v->count, &v->work};
+    for (DevBuf* b : bufs) b->release(s);
+    cudaStreamSynchronize(s);
+    delete v;
+}
+
+}  // extern "C"

@@ -1,0 +1,151 @@
+// common.cuh — device-side views and helpers shared by the join kernels.
+//
+// Layout in HBM (all uint32, CSR):
+//   tokens[T]  the sets' tokens, each set sorted ascending
+//   starts[n]  offset of set i in tokens
+//   sizes[n]   |set i|, non-decreasing in i (the reference's size-sorted order)
+// Bounds are looked up in tables the host fills with the reference's own double
+// expressions (include/hyset/similarity.hpp:11-54); no floating point runs on
+// the device, so every bound is bit-identical to the reference's.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hs {
+
+constexpr unsigned FULL = 0xFFFFFFFFu;
+constexpr uint32_t NOWN = 0xFFFFFFFFu;  // "no ownership constraint"
+
+enum Sim : int { SIM_JACCARD = 0, SIM_COSINE = 1, SIM_DICE = 2 };
+
+struct CollView {
+    const uint32_t* __restrict__ tokens;
+    const uint32_t* __restrict__ starts;
+    const uint32_t* __restrict__ sizes;
+    uint32_t n;
+};
+
+// Host-computed bound tables over set lengths 0..L.
+struct BoundsView {
+    const uint32_t* __restrict__ minsize;       // [L+1]  Similarity::minsize
+    const uint32_t* __restrict__ probe_prefix;  // [L+1]  maxprefix
+    const uint32_t* __restrict__ index_prefix;  // [L+1]  midprefix (self-join) or maxprefix (R-S)
+    const uint32_t* __restrict__ max_partner;   // [L+1]  largest l with minsize(l) <= len
+    const uint32_t* __restrict__ mo_sum;        // [2L+1] raw minoverlap by l1+l2 (jaccard, dice)
+    const uint64_t* __restrict__ mo_row;        // [L+2]  cosine: row offsets by larger length
+    const uint32_t* __restrict__ mo_tab;        // cosine: raw minoverlap at (big, small)
+    uint32_t L;
+    int sim;
+};
+
+// generic_similarity::minoverlap (similarity.hpp:21-23): min(l2, min(l1, raw)).
+// Requires big >= small >= minsize(big) (guaranteed by every caller's length window).
+__device__ __forceinline__ uint32_t minoverlap(const BoundsView& B, uint32_t big, uint32_t small) {
+    uint32_t raw;
+    if (B.sim == SIM_COSINE)
+        raw = B.mo_tab[B.mo_row[big] + (small - B.minsize[big])];
+    else
+        raw = B.mo_sum[big + small];
+    return min(small, min(big, raw));
+}
+
+__device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* a, uint32_t lo, uint32_t hi, uint32_t key) {
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (a[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(FULL, v, o);
+        if (lane >= o) v += y;
+    }
+    return v;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt(int lane) { return (1u << lane) - 1u; }
+
+// Result sink.  `count` always advances (so the host learns the true count);
+// pairs past `cap` are dropped and the host re-runs with a larger buffer.
+struct Sink {
+    uint2* pairs;
+    unsigned long long* count;
+    unsigned long long cap;
+    int count_only;
+};
+
+// Warp-aggregated append; every lane of the warp must call it.
+__device__ __forceinline__ void emit(const Sink& out, bool want, uint32_t first, uint32_t second, int lane) {
+    unsigned m = __ballot_sync(FULL, want);
+    if (!m) return;
+    int leader = __ffs(m) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(out.count, (unsigned long long)__popc(m));
+    base = __shfl_sync(FULL, base, leader);
+    if (want && !out.count_only) {
+        unsigned long long pos = base + __popc(m & lanemask_lt(lane));
+        if (pos < out.cap) out.pairs[pos] = make_uint2(first, second);
+    }
+}
+
+// One lane, two-pointer merge with the reference's early-exit bounds
+// (include/hyset/verification.hpp:35-58), from the start of both sets.
+// own_a != NOWN: the pair belongs to the caller only if the smallest common
+// token sits at a[own_a]; otherwise the function returns false at the first
+// common token (another work item owns the pair).
+__device__ __forceinline__ bool verify_serial(const uint32_t* a, uint32_t na, const uint32_t* __restrict__ b,
+                                              uint32_t nb, uint32_t thr, uint32_t own_a) {
+    uint32_t i = 0, k = 0, found = 0, maxa = na, maxb = nb;
+    while (maxa >= thr && maxb >= thr && found < thr) {
+        uint32_t x = a[i], y = __ldg(b + k);
+        if (x == y) {
+            if (found == 0 && own_a != NOWN && i != own_a) return false;
+            ++i; ++k; ++found;
+        } else if (x < y) {
+            ++i; --maxa;
+        } else {
+            ++k; --maxb;
+        }
+    }
+    return found >= thr;
+}
+
+// Whole warp, merge-path style: 32 tokens of b per step (one coalesced 128-byte
+// load), each lane locates its token in a by binary search, matches are counted
+// with __ballot_sync.  After each step the exact remaining upper bound
+// found + min(|b| - consumed_b, |a| - consumed_a) ends the loop as soon as the
+// pair can no longer reach thr, and the loop also ends once found >= thr.
+// own_b != NOWN: a match at b[k], k < own_b, means a smaller common token
+// exists, so the pair is owned by another work item and false is returned.
+// All 32 lanes must call it with the same arguments.
+__device__ __forceinline__ bool verify_warp(const uint32_t* a, uint32_t na, const uint32_t* __restrict__ b,
+                                            uint32_t nb, uint32_t thr, uint32_t own_b, int lane) {
+    uint32_t found = 0, alo = 0;
+    for (uint32_t k0 = 0; k0 < nb; k0 += 32) {
+        uint32_t k = k0 + lane;
+        bool valid = k < nb;
+        uint32_t y = valid ? __ldg(b + k) : 0xFFFFFFFFu;
+        uint32_t pos = valid ? lower_bound_u32(a, alo, na, y) : na;
+        bool hit = valid && pos < na && a[pos] == y;
+        unsigned m = __ballot_sync(FULL, hit);
+        if (own_b != NOWN && own_b > k0) {
+            uint32_t lim = own_b - k0;
+            unsigned early = lim >= 32 ? FULL : ((1u << lim) - 1u);
+            if (m & early) return false;
+        }
+        found += __popc(m);
+        uint32_t last = min(31u, nb - 1 - k0);
+        uint32_t consumed_a = __shfl_sync(FULL, pos + (hit ? 1u : 0u), last);
+        uint32_t consumed_b = k0 + last + 1;
+        if (found >= thr) return true;
+        if (found + min(nb - consumed_b, na - consumed_a) < thr) return false;
+        alo = consumed_a;
+    }
+    return found >= thr;
+}
+
+}  // namespace hs

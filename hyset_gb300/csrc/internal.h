@@ -1,0 +1,142 @@
+// internal.h — host-side state behind the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "../../include/hyset_gb300.h"
+#include "kernels.h"
+
+namespace hs {
+
+// Device allocation from the stream-ordered pool; grows, never shrinks.
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b, cudaStream_t s) {
+        if (b <= bytes && p) return cudaSuccess;
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMallocAsync(&p, b ? b : 16, s);
+        if (e == cudaSuccess) bytes = b ? b : 16;
+        return e;
+    }
+    void release(cudaStream_t s) {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const { return static_cast<T*>(p); }
+};
+
+// Host-computed bound tables (exact reference doubles) and their device copy.
+struct Bounds {
+    int sim = 0;
+    double tau = 0;
+    uint32_t L = 0;
+    int index_maxprefix = 0;  // 0: index midprefix (self-join), 1: maxprefix (R-S)
+    std::vector<uint32_t> minsize, probe_prefix, index_prefix, max_partner, mo_sum, mo_tab;
+    std::vector<uint64_t> mo_row;
+    DevBuf dev;
+    BoundsView view{};
+};
+
+struct Index {
+    int sim = -1;
+    double tau = -1;
+    int kind = -1;
+    DevBuf list_off, set, pos;
+    uint32_t universe = 0;
+    uint64_t entries = 0;
+    IndexView view() const {
+        IndexView v;
+        v.list_off = list_off.as<uint32_t>();
+        v.set = set.as<uint32_t>();
+        v.pos = pos.as<uint32_t>();
+        v.universe = universe;
+        v.sorted = 1;
+        return v;
+    }
+};
+
+}  // namespace hs
+
+struct hyset_ctx {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ek0 = nullptr, ek1 = nullptr;
+    std::string err;
+    std::map<std::tuple<int, double, uint32_t, int>, std::unique_ptr<hs::Bounds>> bounds;
+    // scratch reused across joins
+    hs::DevBuf s_len, s_off, s_tok, s_set, s_pos, s_order, s_altk, s_altv, s_counts, s_scan;
+    hs::DevBuf s_firstge, s_pairs, s_count, s_work, s_stats;
+};
+
+struct hyset_coll {
+    hyset_ctx* ctx = nullptr;
+    hs::DevBuf tokens, starts, sizes;
+    const uint32_t* d_tokens = nullptr;  // may point at caller memory (from_device)
+    const uint32_t* d_starts = nullptr;
+    const uint32_t* d_sizes = nullptr;
+    uint32_t n = 0;
+    uint64_t n_tokens = 0;
+    uint32_t max_size = 0;
+    uint32_t universe = 0;  // max token + 1
+    std::vector<uint32_t> h_sizes;
+    hs::Index index;
+    std::map<int, hs::DevBuf> bitmaps;  // by words
+    hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, n}; }
+};
+
+struct hyset_result {
+    uint64_t count = 0;
+    std::vector<hyset_pair> pairs;
+    int has_pairs = 0;
+    const void* device_pairs = nullptr;
+    hyset_technique technique = HYSET_TECH_AUTO;
+    double device_ms = 0;
+    double kernel_ms = 0;
+    uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+
+struct hyset_handler {
+    hyset_ctx* ctx = nullptr;
+    const hyset_coll* coll = nullptr;
+    hyset_technique technique = HYSET_TECH_FGSS;
+    hyset_sim sim = HYSET_JACCARD;
+    double tau = 0;
+    uint32_t block_size = 0;
+    int aggregate = 0;
+    int words = 0;
+    hs::Bounds* bounds = nullptr;
+    hs::DevBuf first_ge;
+    // per-indexed-block inverted index (reference layout: unsorted lists)
+    hs::DevBuf counts, list_off, e_len, e_off, e_tok, e_set, e_pos, idx_set, idx_pos, scan;
+    uint32_t indexed_block = 0xFFFFFFFFu;
+    hs::DevBuf bits, pairs, count, work;
+    uint64_t cap = 0;
+    uint64_t out_count = 0;
+    std::vector<hyset_pair> out_pairs;
+};
+
+struct hyset_verifier {
+    hyset_ctx* ctx = nullptr;
+    const hyset_coll* indexed = nullptr;
+    const hyset_coll* probe = nullptr;
+    hs::Bounds* bounds = nullptr;
+    uint32_t scenario = 1;
+    int aggregate = 0;
+    uint32_t max_probes = 0, max_candidates = 0;
+    std::vector<uint32_t> h_probes, h_offsets, h_cands;
+    hs::DevBuf d_probes, d_offsets, d_cands, pairs, count, work;
+    uint64_t out_count = 0;
+    std::vector<hyset_pair> out_pairs;
+};

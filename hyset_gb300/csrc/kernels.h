@@ -1,0 +1,97 @@
+// kernels.h — host-side launchers of the CUDA kernels (defined in *.cu).
+// Everything here is asynchronous on the given stream and returns the first
+// CUDA error it sees.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace hs {
+
+// ---- primitives.cu -------------------------------------------------------
+// Exclusive prefix sum of n uint32 values (in may equal out).  `scratch` must
+// hold scan_scratch_words(n) words.
+size_t scan_scratch_words(uint64_t n);
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s);
+
+// Stable LSD radix sort of (key, value) pairs on the low `key_bits` bits of the
+// keys.  Result lands in keys/vals; alt_* are ping-pong buffers of n words;
+// `scratch` holds radix_scratch_words(n) words.
+size_t radix_scratch_words(uint64_t n);
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
+                             uint64_t n, int key_bits, uint32_t* scratch, cudaStream_t s);
+
+// Prefix entries of sets [lo, hi): the first prefix_len(size) tokens of every
+// set (include/hyset/collection.hpp:128-135).  entry_off must hold the
+// exclusive scan of the per-set prefix lengths over [lo, hi) (relative to lo).
+cudaError_t set_prefix_lengths(CollView c, const uint32_t* prefix_tab, uint32_t lo, uint32_t hi,
+                               uint32_t* out_len, cudaStream_t s);
+cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint32_t* entry_off,
+                                const uint32_t* len, uint32_t* e_token, uint32_t* e_set,
+                                uint32_t* e_pos, cudaStream_t s);
+
+// Token histogram of n entries into counts[universe] (warp-aggregated atomics;
+// the counts are NOT zeroed here).
+cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, cudaStream_t s);
+
+// Reference-style scatter (include/hyset/index.hpp:233-248): each entry goes to
+// cursor[token]++ (warp-aggregated); list order within a token is arbitrary.
+cudaError_t scatter_entries(const uint32_t* e_token, const uint32_t* e_set, const uint32_t* e_pos, uint64_t n,
+                            uint32_t* cursor, uint32_t* idx_set, uint32_t* idx_pos, cudaStream_t s);
+
+// After a stable sort by token of entry indices: idx_set[i] = e_set[order[i]], ...
+cudaError_t gather_entries(const uint32_t* order, uint64_t n, const uint32_t* e_set, const uint32_t* e_pos,
+                           uint32_t* idx_set, uint32_t* idx_pos, cudaStream_t s);
+
+cudaError_t iota_u32(uint32_t* out, uint64_t n, cudaStream_t s);
+
+// Input contract check of an uploaded collection.  flags[0] gets bit 1 for an
+// empty set, 2 for a set whose tokens are not strictly ascending, 4 for a size
+// smaller than the previous set's, 8 for a set reaching past n_tokens;
+// flags[1] gets the largest token (atomicMax).  flags must be zeroed first.
+cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s);
+
+// XOR bitmap signatures, bit (token mod bits) per token
+// (include/hyset/device_algorithms.hpp:58-74), words = bits / 64 in {1,2,4,8}.
+cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s);
+
+// ---- join.cu --------------------------------------------------------------
+struct IndexView {
+    const uint32_t* __restrict__ list_off;  // [universe+1]: list t = [list_off[t], list_off[t+1])
+    const uint32_t* __restrict__ set;       // entry set ids
+    const uint32_t* __restrict__ pos;       // entry positions within their sets
+    uint32_t universe;
+    int sorted;                             // lists ordered by set id
+};
+
+struct JoinParams {
+    CollView R;                 // indexed collection
+    CollView S;                 // probe collection (== R for a self-join)
+    BoundsView B;
+    const uint32_t* __restrict__ first_ge;  // [L+2] first id of R with size >= l
+    int self;                   // candidates c < p inside one collection
+    uint32_t p_lo, p_hi;        // probe ids [p_lo, p_hi)
+    uint32_t r_lo, r_hi;        // candidate ids restricted to [r_lo, r_hi)
+    IndexView X;                // FGSS only
+    const uint64_t* __restrict__ bits_R;    // signatures (nullptr = no bitmap filter)
+    const uint64_t* __restrict__ bits_S;
+    int words;
+    Sink out;
+    unsigned int* work;         // work-stealing counter, zero before launch
+    unsigned long long* stats;  // optional [8] counters (nullptr = off)
+};
+
+enum Technique : int { TECH_BITMAP = 1, TECH_FGSS = 2, TECH_DIRECT = 3 };
+
+// One persistent, work-stealing launch over probes [p_lo, p_hi).
+// vmode: 1 = lane per candidate, 2 = warp per candidate.
+cudaError_t launch_join(const JoinParams& P, int technique, int vmode, int sm_count, cudaStream_t s);
+
+// Explicit candidate lists (hybrid::device_handler): probes[i] owns candidates
+// [i ? offsets[i-1] : 0, offsets[i]).
+cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const uint32_t* probes,
+                                     const uint32_t* offsets, const uint32_t* cands, uint32_t n_probes,
+                                     int vmode, Sink out, unsigned int* work, int sm_count, cudaStream_t s);
+
+}  // namespace hs

@@ -1,0 +1,401 @@
+// primitives.cu — HBM-bound building blocks of the inverted index and the
+// signatures: device-wide scan, stable radix sort, warp-aggregated histogram and
+// scatter, prefix-entry emission, XOR bitmaps.
+//
+// Replaces the reference's index::histogram / thrust::exclusive_scan /
+// index::create_index / thrust::sort (include/hyset/index.hpp:217-313) and
+// bitmap::generate (include/hyset/device_algorithms.hpp:58-74).
+#include "kernels.h"
+
+namespace hs {
+
+namespace {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 2048
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_sums, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = warp_incl_scan(v, lane);
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (SCAN_THREADS / 32) ? warp_sums[lane] : 0;
+        uint32_t wi = warp_incl_scan(w, lane);
+        if (lane < (SCAN_THREADS / 32)) warp_sums[lane] = wi - w;
+        if (lane == (SCAN_THREADS / 32) - 1) warp_sums[SCAN_THREADS / 32] = wi;
+    }
+    __syncthreads();
+    uint32_t r = warp_sums[warp] + incl - v;
+    total = warp_sums[SCAN_THREADS / 32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_reduce(const uint32_t* in, uint64_t n, uint32_t* sums) {
+    __shared__ uint32_t ws[SCAN_THREADS / 32 + 1];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i)
+        if (base + i < n) s += in[base + i];
+    uint32_t total;
+    block_excl_scan(s, ws, total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// in/out may alias: every tile reads all its inputs before writing.
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const uint32_t* in, uint32_t* out, uint64_t n,
+                                                            const uint32_t* tile_off) {
+    __shared__ uint32_t ws[SCAN_THREADS / 32 + 1];
+    uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        v[i] = base + i < n ? in[base + i] : 0;
+        s += v[i];
+    }
+    uint32_t total;
+    uint32_t run = block_excl_scan(s, ws, total) + (tile_off ? tile_off[blockIdx.x] : 0);
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) {
+        if (base + i < n) out[base + i] = run;
+        run += v[i];
+    }
+}
+
+// ---- radix sort -----------------------------------------------------------
+constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_WARPS = RADIX_THREADS / 32;
+constexpr int RADIX_ROUNDS = 16;                                  // 32-item rounds per warp
+constexpr uint32_t RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;     // 4096
+constexpr int RADIX_BINS = 256;
+
+__global__ void __launch_bounds__(RADIX_THREADS) k_radix_upsweep(const uint32_t* keys, uint64_t n, int shift,
+                                                                 uint32_t* tile_counts, uint32_t tiles) {
+    __shared__ uint32_t hist[RADIX_BINS];
+    hist[threadIdx.x] = 0;
+    __syncthreads();
+    uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE;
+    for (uint32_t i = threadIdx.x; i < RADIX_TILE; i += RADIX_THREADS) {
+        uint64_t idx = base + i;
+        if (idx < n) atomicAdd(&hist[(keys[idx] >> shift) & (RADIX_BINS - 1)], 1u);
+    }
+    __syncthreads();
+    tile_counts[(uint64_t)threadIdx.x * tiles + blockIdx.x] = hist[threadIdx.x];
+}
+
+// Stable scatter: an item's rank inside its tile is the number of equal digits
+// before it (warp w owns items [w*512, w*512+512) of the tile, processed in
+// order, 32 at a time, peers found with __match_any_sync).
+__global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_t* __restrict__ keys,
+                                                                   const uint32_t* __restrict__ vals, uint64_t n,
+                                                                   int shift, const uint32_t* __restrict__ tile_off,
+                                                                   uint32_t tiles, uint32_t* keys_out,
+                                                                   uint32_t* vals_out) {
+    __shared__ uint32_t whist[RADIX_WARPS][RADIX_BINS];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int i = threadIdx.x; i < RADIX_WARPS * RADIX_BINS; i += RADIX_THREADS) (&whist[0][0])[i] = 0;
+    __syncthreads();
+    uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE + (uint64_t)warp * (32 * RADIX_ROUNDS);
+    uint32_t k[RADIX_ROUNDS], v[RADIX_ROUNDS], rank[RADIX_ROUNDS];
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        uint64_t idx = base + (uint64_t)r * 32 + lane;
+        bool valid = idx < n;
+        uint32_t key = valid ? keys[idx] : 0;
+        uint32_t d = valid ? ((key >> shift) & (RADIX_BINS - 1)) : RADIX_BINS;
+        unsigned peers = __match_any_sync(FULL, d);
+        int leader = __ffs(peers) - 1;
+        uint32_t cnt = valid ? whist[warp][d] : 0;
+        __syncwarp();
+        if (valid && lane == leader) whist[warp][d] = cnt + __popc(peers);
+        __syncwarp();
+        rank[r] = cnt + __popc(peers & lanemask_lt(lane));
+        k[r] = key;
+        v[r] = valid ? vals[idx] : 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < RADIX_BINS) {
+        uint32_t run = 0;
+#pragma unroll
+        for (int w = 0; w < RADIX_WARPS; ++w) {
+            uint32_t t = whist[w][threadIdx.x];
+            whist[w][threadIdx.x] = run;
+            run += t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        uint64_t idx = base + (uint64_t)r * 32 + lane;
+        if (idx < n) {
+            uint32_t d = (k[r] >> shift) & (RADIX_BINS - 1);
+            uint32_t pos = tile_off[(uint64_t)d * tiles + blockIdx.x] + whist[warp][d] + rank[r];
+            keys_out[pos] = k[r];
+            vals_out[pos] = v[r];
+        }
+    }
+}
+
+// ---- index and signatures --------------------------------------------------
+__global__ void k_prefix_len(CollView c, const uint32_t* __restrict__ tab, uint32_t lo, uint32_t hi,
+                             uint32_t* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; lo + i < hi; i += gridDim.x * blockDim.x)
+        out[i] = tab[c.sizes[lo + i]];
+}
+
+// One warp per set: the first len tokens become entries (token, set, position).
+__global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint32_t* __restrict__ off,
+                               const uint32_t* __restrict__ len, uint32_t* e_token, uint32_t* e_set,
+                               uint32_t* e_pos) {
+    const int lane = threadIdx.x & 31;
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; lo + w < hi; w += warps) {
+        uint32_t s = lo + w, l = len[w], o = off[w];
+        const uint32_t* t = c.tokens + c.starts[s];
+        for (uint32_t i = lane; i < l; i += 32) {
+            e_token[o + i] = t[i];
+            e_set[o + i] = s;
+            e_pos[o + i] = i;
+        }
+    }
+}
+
+__global__ void k_histogram(const uint32_t* __restrict__ tok, uint64_t n, uint32_t* counts) {
+    const int lane = threadIdx.x & 31;
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        uint64_t i = i0 + threadIdx.x;
+        bool valid = i < n;
+        uint32_t t = valid ? tok[i] : 0xFFFFFFFFu;
+        unsigned peers = __match_any_sync(FULL, t);
+        if (valid && lane == __ffs(peers) - 1) atomicAdd(&counts[t], (uint32_t)__popc(peers));
+    }
+}
+
+__global__ void k_scatter(const uint32_t* __restrict__ tok, const uint32_t* __restrict__ eset,
+                          const uint32_t* __restrict__ epos, uint64_t n, uint32_t* cursor, uint32_t* idx_set,
+                          uint32_t* idx_pos) {
+    const int lane = threadIdx.x & 31;
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
+        uint64_t i = i0 + threadIdx.x;
+        bool valid = i < n;
+        uint32_t t = valid ? tok[i] : 0xFFFFFFFFu;
+        unsigned peers = __match_any_sync(FULL, t);
+        int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (valid && lane == leader) base = atomicAdd(&cursor[t], (uint32_t)__popc(peers));
+        base = __shfl_sync(FULL, base, leader);
+        if (valid) {
+            uint32_t at = base + __popc(peers & lanemask_lt(lane));
+            idx_set[at] = eset[i];
+            idx_pos[at] = epos[i];
+        }
+    }
+}
+
+__global__ void k_gather(const uint32_t* __restrict__ order, uint64_t n, const uint32_t* __restrict__ eset,
+                         const uint32_t* __restrict__ epos, uint32_t* idx_set, uint32_t* idx_pos) {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint32_t e = order[i];
+        idx_set[i] = eset[e];
+        idx_pos[i] = epos[e];
+    }
+}
+
+__global__ void k_iota(uint32_t* out, uint64_t n) {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (uint32_t)i;
+}
+
+// One warp per set; each lane folds its tokens into W register words, then the
+// warp XOR-reduces them.  Bit b of the signature is word b/64, bit b%64.
+template <int W>
+__global__ void k_bitmaps(CollView c, uint64_t* out) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t bits = 64u * W;
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < c.n; s += warps) {
+        uint64_t w[W];
+#pragma unroll
+        for (int i = 0; i < W; ++i) w[i] = 0;
+        const uint32_t* t = c.tokens + c.starts[s];
+        uint32_t l = c.sizes[s];
+        for (uint32_t i = lane; i < l; i += 32) {
+            uint32_t b = t[i] % bits;
+#pragma unroll
+            for (int q = 0; q < W; ++q)
+                if ((b >> 6) == (uint32_t)q) w[q] ^= 1ull << (b & 63);
+        }
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) w[q] ^= __shfl_xor_sync(FULL, w[q], o);
+        }
+        if (lane == 0) {
+#pragma unroll
+            for (int q = 0; q < W; ++q) out[(uint64_t)s * W + q] = w[q];
+        }
+    }
+}
+
+__global__ void k_validate(CollView c, uint64_t n_tokens, uint32_t* flags) {
+    const int lane = threadIdx.x & 31;
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < c.n; s += warps) {
+        uint32_t l = c.sizes[s], st = c.starts[s];
+        uint32_t f = 0;
+        if (l == 0) f |= 1;
+        if (s > 0 && c.sizes[s - 1] > l) f |= 4;
+        if ((uint64_t)st + l > n_tokens) f |= 8;
+        if (!(f & 8) && l > 0) {
+            const uint32_t* t = c.tokens + st;
+            for (uint32_t i = lane; i + 1 < l; i += 32)
+                if (t[i] >= t[i + 1]) f |= 2;
+            if (lane == 0) atomicMax(&flags[1], t[l - 1]);
+        }
+        if (f) atomicOr(&flags[0], f);
+    }
+}
+
+unsigned grid_for(uint64_t n, unsigned threads, unsigned cap = 152u * 32u) {
+    uint64_t g = (n + threads - 1) / threads;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned)g;
+}
+
+}  // namespace
+
+size_t scan_scratch_words(uint64_t n) {
+    size_t words = 0;
+    while (n > SCAN_TILE) {
+        n = (n + SCAN_TILE - 1) / SCAN_TILE;
+        words += n;
+    }
+    return words + 1;
+}
+
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    if (n <= SCAN_TILE) {
+        k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        return cudaGetLastError();
+    }
+    uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
+    uint32_t* sums = scratch;
+    k_tile_reduce<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = scan_exclusive(sums, sums, tiles, scratch + tiles, s);
+    if (e != cudaSuccess) return e;
+    k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    return cudaGetLastError();
+}
+
+size_t radix_scratch_words(uint64_t n) {
+    uint64_t tiles = (n + RADIX_TILE - 1) / RADIX_TILE;
+    uint64_t counts = tiles * RADIX_BINS;
+    return counts + scan_scratch_words(counts);
+}
+
+cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, uint64_t n,
+                             int key_bits, uint32_t* scratch, cudaStream_t s) {
+    if (n <= 1) return cudaSuccess;
+    uint32_t tiles = (uint32_t)((n + RADIX_TILE - 1) / RADIX_TILE);
+    uint64_t counts = (uint64_t)tiles * RADIX_BINS;
+    uint32_t* tile_counts = scratch;
+    uint32_t* scan_tmp = scratch + counts;
+    int passes = (key_bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    uint32_t *kin = keys, *vin = vals, *kout = alt_keys, *vout = alt_vals;
+    for (int p = 0; p < passes; ++p) {
+        int shift = 8 * p;
+        k_radix_upsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, n, shift, tile_counts, tiles);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        e = scan_exclusive(tile_counts, tile_counts, counts, scan_tmp, s);
+        if (e != cudaSuccess) return e;
+        k_radix_downsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, vin, n, shift, tile_counts, tiles, kout, vout);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        uint32_t* t;
+        t = kin; kin = kout; kout = t;
+        t = vin; vin = vout; vout = t;
+    }
+    if (kin != keys) {
+        cudaError_t e = cudaMemcpyAsync(keys, kin, n * 4, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+        e = cudaMemcpyAsync(vals, vin, n * 4, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t set_prefix_lengths(CollView c, const uint32_t* prefix_tab, uint32_t lo, uint32_t hi, uint32_t* out_len,
+                               cudaStream_t s) {
+    if (hi <= lo) return cudaSuccess;
+    k_prefix_len<<<grid_for(hi - lo, 256), 256, 0, s>>>(c, prefix_tab, lo, hi, out_len);
+    return cudaGetLastError();
+}
+
+cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint32_t* entry_off, const uint32_t* len,
+                                uint32_t* e_token, uint32_t* e_set, uint32_t* e_pos, cudaStream_t s) {
+    if (hi <= lo) return cudaSuccess;
+    k_emit_entries<<<grid_for((uint64_t)(hi - lo) * 32, 256), 256, 0, s>>>(c, lo, hi, entry_off, len, e_token,
+                                                                            e_set, e_pos);
+    return cudaGetLastError();
+}
+
+cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_histogram<<<grid_for(n, 256), 256, 0, s>>>(e_token, n, counts);
+    return cudaGetLastError();
+}
+
+cudaError_t scatter_entries(const uint32_t* e_token, const uint32_t* e_set, const uint32_t* e_pos, uint64_t n,
+                            uint32_t* cursor, uint32_t* idx_set, uint32_t* idx_pos, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_scatter<<<grid_for(n, 256), 256, 0, s>>>(e_token, e_set, e_pos, n, cursor, idx_set, idx_pos);
+    return cudaGetLastError();
+}
+
+cudaError_t gather_entries(const uint32_t* order, uint64_t n, const uint32_t* e_set, const uint32_t* e_pos,
+                           uint32_t* idx_set, uint32_t* idx_pos, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_gather<<<grid_for(n, 256), 256, 0, s>>>(order, n, e_set, e_pos, idx_set, idx_pos);
+    return cudaGetLastError();
+}
+
+cudaError_t iota_u32(uint32_t* out, uint64_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_iota<<<grid_for(n, 256), 256, 0, s>>>(out, n);
+    return cudaGetLastError();
+}
+
+cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s) {
+    if (c.n == 0) return cudaSuccess;
+    k_validate<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, n_tokens, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s) {
+    if (c.n == 0) return cudaSuccess;
+    unsigned g = grid_for((uint64_t)c.n * 32, 256);
+    switch (words) {
+    case 1: k_bitmaps<1><<<g, 256, 0, s>>>(c, out); break;
+    case 2: k_bitmaps<2><<<g, 256, 0, s>>>(c, out); break;
+    case 4: k_bitmaps<4><<<g, 256, 0, s>>>(c, out); break;
+    case 8: k_bitmaps<8><<<g, 256, 0, s>>>(c, out); break;
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace hs

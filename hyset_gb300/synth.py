@@ -1,0 +1,115 @@
+"""Seeded synthetic collections (wraps libhyset_synth.so, include/hyset_gb300_synth.h).
+
+Workload presets follow the benchmark configurations of this project: Zipf
+tokens drawn without replacement, tokens renumbered 1..U by ascending global
+frequency, sets sorted, collection sorted by (size, tokens).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+SYNTH_PATH = os.path.join(_HERE, "libhyset_synth.so")
+
+UNIFORM, LOGNORMAL = 0, 1
+
+
+class _Params(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("n_sets", C.c_uint32), ("universe", C.c_uint32), ("zipf_s", C.c_double),
+                ("size_dist", C.c_int), ("size_a", C.c_double), ("size_b", C.c_double), ("size_min", C.c_uint32),
+                ("size_max", C.c_uint32), ("dup_frac", C.c_double), ("dup_edit_lo", C.c_double),
+                ("dup_edit_hi", C.c_double), ("threads", C.c_int)]
+
+
+@dataclass
+class SynthSpec:
+    n_sets: int
+    universe: int
+    zipf_s: float
+    size_dist: int
+    size_a: float
+    size_b: float
+    size_min: int
+    size_max: int
+    dup_frac: float = 0.0
+    dup_edit_lo: float = 0.0
+    dup_edit_hi: float = 0.0
+    seed: int = 0x5E7
+
+
+# The benchmark configurations (sizes, universes, Zipf exponents, planted duplicates).
+C1 = SynthSpec(10_000, 5_000, 1.0, UNIFORM, 5, 50, 5, 50)
+C2 = SynthSpec(200_000, 100_000, 1.1, LOGNORMAL, 3.2, 0.6, 2, 500, 0.03, 0.10, 0.10)
+C3 = SynthSpec(1_000_000, 1_000_000, 0.9, LOGNORMAL, 4.4, 0.8, 10, 2000, 0.05, 0.05, 0.15)
+
+
+@dataclass
+class Collection:
+    """CSR collection in the reference's input contract (sorted sets, size-sorted)."""
+    tokens: np.ndarray  # uint32 [T]
+    starts: np.ndarray  # uint32 [n]
+    sizes: np.ndarray   # uint32 [n]
+
+    @property
+    def n(self) -> int:
+        return int(self.sizes.shape[0])
+
+    def set(self, i: int) -> np.ndarray:
+        s = int(self.starts[i])
+        return self.tokens[s:s + int(self.sizes[i])]
+
+    def write_text(self, path: str) -> None:
+        with open(path, "w") as f:
+            for i in range(self.n):
+                f.write(" ".join(map(str, self.set(i).tolist())) + "\n")
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(SYNTH_PATH):
+            raise RuntimeError(f"{SYNTH_PATH} missing: build with hyset_gb300._build")
+        lib = C.CDLL(SYNTH_PATH)
+        lib.hyset_synth_generate.argtypes = [C.POINTER(_Params), C.POINTER(C.c_void_p)]
+        lib.hyset_synth_generate.restype = C.c_int
+        for name, res in (("num_sets", C.c_uint32), ("num_tokens", C.c_uint64), ("max_token", C.c_uint32)):
+            fn = getattr(lib, "hyset_synth_" + name)
+            fn.argtypes = [C.c_void_p]
+            fn.restype = res
+        for name in ("tokens", "sizes", "starts"):
+            fn = getattr(lib, "hyset_synth_" + name)
+            fn.argtypes = [C.c_void_p]
+            fn.restype = C.POINTER(C.c_uint32)
+        lib.hyset_synth_free.argtypes = [C.c_void_p]
+        lib.hyset_synth_free.restype = None
+        _lib = lib
+    return _lib
+
+
+def generate(spec: SynthSpec, threads: int = 0, **overrides) -> Collection:
+    fields = dict(spec.__dict__)
+    fields.update(overrides)
+    lib = _load()
+    p = _Params(int(fields["seed"]), int(fields["n_sets"]), int(fields["universe"]), float(fields["zipf_s"]),
+                int(fields["size_dist"]), float(fields["size_a"]), float(fields["size_b"]), int(fields["size_min"]),
+                int(fields["size_max"]), float(fields["dup_frac"]), float(fields["dup_edit_lo"]),
+                float(fields["dup_edit_hi"]), int(threads))
+    h = C.c_void_p()
+    if lib.hyset_synth_generate(C.byref(p), C.byref(h)) != 0:
+        raise ValueError(f"invalid synthetic spec {fields}")
+    try:
+        n = lib.hyset_synth_num_sets(h)
+        T = lib.hyset_synth_num_tokens(h)
+        tok = np.ctypeslib.as_array(lib.hyset_synth_tokens(h), (T,)).copy() if T else np.zeros(0, np.uint32)
+        sz = np.ctypeslib.as_array(lib.hyset_synth_sizes(h), (n,)).copy()
+        st = np.ctypeslib.as_array(lib.hyset_synth_starts(h), (n,)).copy()
+    finally:
+        lib.hyset_synth_free(h)
+    return Collection(tok, st, sz)

@@ -1,0 +1,190 @@
+/*
+ * hyset_gb300.h — C ABI of the GB300 (sm_103a) exact set-similarity join.
+ *
+ * Drop-in boundary for chribell/hyset's GPU join path.  The reference exposes
+ * C++ templates and structs only (no C ABI); each entry point below names the
+ * reference interface it replaces (paths relative to the reference source tree).
+ * Plain pointers and sizes only; no C++ or torch types cross this boundary.
+ *
+ * Conventions
+ *   - Every call returns hyset_status; HYSET_OK is 0.  hyset_last_error(ctx)
+ *     returns a human-readable message for the last failure on that context.
+ *   - One context per host thread; a context owns one CUDA stream on one device.
+ *   - Results are owned by the library until hyset_result_free.
+ *   - Pairs are (probe set id, indexed set id).  In a self-join the ids are the
+ *     positions in the size-sorted collection and first > second, exactly as the
+ *     reference emits them (include/hyset/verification.hpp:120-122).
+ *   - The output pair SET is bit-exact to the reference's host::allpairs on the
+ *     same input; the ORDER of pairs is unspecified unless sorted on request.
+ *   - The library never falls back to a CPU implementation: without a usable
+ *     device every compute call fails with HYSET_E_NODEVICE.
+ */
+#ifndef HYSET_GB300_H
+#define HYSET_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    HYSET_OK = 0,
+    HYSET_E_INVALID = 1,     /* bad argument (null pointer, unsorted input, ...) */
+    HYSET_E_CUDA = 2,        /* a CUDA runtime call failed */
+    HYSET_E_NOMEM = 3,       /* device or host allocation failed */
+    HYSET_E_OVERFLOW = 4,    /* a fixed-capacity output could not hold the result */
+    HYSET_E_TIMEOUT = 5,     /* a bounded device wait gave up */
+    HYSET_E_UNSUPPORTED = 6, /* option combination not implemented */
+    HYSET_E_NODEVICE = 7     /* no CUDA device, or the library was built without one */
+} hyset_status;
+
+typedef enum { HYSET_JACCARD = 0, HYSET_COSINE = 1, HYSET_DICE = 2 } hyset_sim;
+
+/* Filter technique.  BITMAP and FGSS are the reference's two GPU techniques
+ * (src/bitmap.cu, src/fgss.cu); DIRECT verifies every length-compatible pair.
+ * AUTO lets the library choose (learned selector, analytic cost model fallback).
+ * The choice never changes the output. */
+typedef enum {
+    HYSET_TECH_AUTO = 0,
+    HYSET_TECH_BITMAP = 1,
+    HYSET_TECH_FGSS = 2,
+    HYSET_TECH_DIRECT = 3
+} hyset_technique;
+
+/* hyset::structs::block (include/hyset/structs.hpp:10-54), same field order. */
+typedef struct {
+    uint32_t id, start_id, end_id, first_entry_position, last_entry_position, num_tokens, entries, size;
+} hyset_block;
+
+/* hyset::structs::pair (include/hyset/structs.hpp:76-81). */
+typedef struct {
+    uint32_t first, second;
+} hyset_pair;
+
+typedef struct {
+    hyset_sim sim;
+    double threshold;          /* in (0, 1] */
+    hyset_technique technique;
+    uint32_t bitmap_bits;      /* 0 = no signature filter; else 64, 128, 256 or 512 */
+    uint32_t count_only;       /* 1 = count result pairs, do not materialise them */
+    uint32_t verify_mode;      /* 0 = auto, 1 = one lane per candidate, 2 = one warp per candidate */
+    uint32_t sort_pairs;       /* 1 = return pairs sorted by (first, second) */
+    uint64_t pair_capacity;    /* initial device pair buffer; 0 = automatic (grows on demand) */
+    uint32_t device_pairs;     /* 1 = leave the pairs in device memory (hyset_result_device_pairs) */
+    uint32_t collect_stats;    /* 1 = count filter work (hyset_result_stats); costs a few atomics */
+} hyset_join_opts;
+
+typedef struct hyset_ctx hyset_ctx;
+typedef struct hyset_coll hyset_coll;
+typedef struct hyset_result hyset_result;
+typedef struct hyset_handler hyset_handler;
+typedef struct hyset_verifier hyset_verifier;
+
+/* ---- context --------------------------------------------------------- */
+/* Replaces the implicit cuda-api-wrappers current-device setup of every driver
+ * (e.g. src/bitmap.cu:77-80).  device < 0 selects the current device. */
+hyset_status hyset_create(int device, hyset_ctx** out);
+void hyset_destroy(hyset_ctx* ctx);
+const char* hyset_last_error(const hyset_ctx* ctx);
+void hyset_default_opts(hyset_join_opts* opts);
+
+/* ---- collections ----------------------------------------------------- */
+/* hyset::collection::device_collection(host_collection&) (include/hyset/collection.hpp:54-71):
+ * uploads the CSR arrays of a collection whose sets are sorted ascending and
+ * whose sets are ordered by size (the reference's input contract,
+ * collection.hpp:93-177).  starts may be NULL (then sets are contiguous).
+ * Returns HYSET_E_INVALID if sizes are not non-decreasing, a set is empty or
+ * unsorted, or n_tokens >= 2^32. */
+hyset_status hyset_collection_upload(hyset_ctx* ctx, const uint32_t* tokens, uint64_t n_tokens,
+                                     const uint32_t* starts, const uint32_t* sizes, uint32_t n_sets,
+                                     hyset_coll** out);
+/* Same, from arrays already resident on the context's device (no host copy of tokens). */
+hyset_status hyset_collection_from_device(hyset_ctx* ctx, const uint32_t* d_tokens, uint64_t n_tokens,
+                                          const uint32_t* d_starts, const uint32_t* d_sizes,
+                                          uint32_t n_sets, hyset_coll** out);
+void hyset_collection_free(hyset_ctx* ctx, hyset_coll* coll);
+uint32_t hyset_collection_num_sets(const hyset_coll* coll);
+
+/* ---- whole joins ----------------------------------------------------- */
+/* Self-join R ⋈ R: what src/bitmap.cu:112-121 and src/fgss.cu:108-116 compute
+ * with bitmap::handler / fgssjoin::handler over one partition of all blocks,
+ * and what cpu_single computes with host::allpairs (src/cpu_single.cu:116-136). */
+hyset_status hyset_self_join(hyset_ctx* ctx, const hyset_coll* coll, const hyset_join_opts* opts,
+                             hyset_result** out);
+/* R-S join: every (s, r), s in probe, r in indexed, with m >= minsize(b) and
+ * |s ∩ r| >= minoverlap(b, m), (b, m) = (larger, smaller) size.  The reference
+ * declares --foreign-input (e.g. src/bitmap.cu:31) but never reads it; this is
+ * the self-join's predicate applied across two collections. */
+hyset_status hyset_rs_join(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                           const hyset_join_opts* opts, hyset_result** out);
+
+/* Many independent joins in one persistent, work-stealing launch (the
+ * device-resident form of src/queue.cu:142-281's block-pair queue).
+ * probe == NULL (or probe == indexed) means a self-join. */
+typedef struct {
+    const hyset_coll* indexed;
+    const hyset_coll* probe;
+    hyset_join_opts opts;
+} hyset_join_desc;
+hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_t n_joins,
+                              hyset_result** results /* [n_joins] */);
+
+uint64_t hyset_result_count(const hyset_result* r);
+const hyset_pair* hyset_result_pairs(const hyset_result* r); /* NULL when count_only */
+hyset_technique hyset_result_technique(const hyset_result* r);
+double hyset_result_device_ms(const hyset_result* r);       /* CUDA-event time of the join's device work */
+double hyset_result_kernel_ms(const hyset_result* r);       /* CUDA-event time of the filter+verify launch */
+/* Device pointer to count (first, second) uint32 pairs when device_pairs was
+ * set; valid until the next join on the same context. */
+const void* hyset_result_device_pairs(const hyset_result* r);
+/* Work counters when collect_stats was set: [0] filter items examined,
+ * [1] items reaching verification, [2] candidate tokens of those items,
+ * [3] index entries, [4] probe tokens; returns the number written (<= n). */
+uint32_t hyset_result_stats(const hyset_result* r, uint64_t* out, uint32_t n);
+void hyset_result_free(hyset_result* r);
+
+/* ---- reference-shaped handlers -------------------------------------- */
+/* bitmap::handler(timer, hostCollection, deviceCollection, bitmapSize, blockSize,
+ *                 aggregate, threshold)     include/hyset/device_algorithms.hpp:138-171
+ * fgssjoin::handler(timer, hostCollection, deviceCollection, blockSize,
+ *                   aggregate, threshold)   include/hyset/device_algorithms.hpp:322-348
+ * technique selects which; bitmap_size is ignored for FGSS.  sim extends the
+ * reference (which hard-codes jaccard). */
+hyset_status hyset_handler_create(hyset_ctx* ctx, const hyset_coll* coll, hyset_technique technique,
+                                  hyset_sim sim, uint32_t bitmap_size, uint32_t block_size,
+                                  int aggregate, double threshold, hyset_handler** out);
+/* handler::join(block*, block*): first = indexed block, second = probe block
+ * (device_algorithms.hpp:177-229, :363-412).  Pairs/count accumulate in the
+ * handler's output, like the pairs_handler / count_handler the reference
+ * appends to. */
+hyset_status hyset_handler_join_blocks(hyset_handler* h, const hyset_block* first, const hyset_block* second);
+/* handler::join(partition*, partition*): block-level length filter, then every
+ * surviving block pair (device_algorithms.hpp:21-53, :232-247, :416-432). */
+hyset_status hyset_handler_join_partitions(hyset_handler* h, const hyset_block* first, uint32_t n_first,
+                                           const hyset_block* second, uint32_t n_second);
+/* output::pairs_handler::getPairs / count_handler::count (include/hyset/output.hpp:19-37). */
+hyset_status hyset_handler_output(const hyset_handler* h, uint64_t* count, const hyset_pair** pairs);
+hyset_status hyset_handler_clear_output(hyset_handler* h);
+void hyset_handler_destroy(hyset_handler* h);
+
+/* ---- candidate verifier (hybrid::device_handler) ------------------- */
+/* hybrid::device_handler(indexed, probe, threads, scenario, aggregate, maxProbes,
+ * maxCandidates, threshold)   include/hyset/hybrid_algorithms.hpp:41-62.
+ * scenario 1 = one lane per candidate, 2 = one warp per candidate (merge-path). */
+hyset_status hyset_verifier_create(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                                   hyset_sim sim, uint32_t threads, uint32_t scenario, int aggregate,
+                                   uint32_t max_probes, uint32_t max_candidates, double threshold,
+                                   hyset_verifier** out);
+/* device_handler::addCandidates(probeID, candidate_set&)  hybrid_algorithms.hpp:71-105 */
+hyset_status hyset_verifier_add_candidates(hyset_verifier* v, uint32_t probe_id, const uint32_t* candidates,
+                                           uint32_t n_candidates);
+/* device_handler::flush()  hybrid_algorithms.hpp:195-200 */
+hyset_status hyset_verifier_flush(hyset_verifier* v);
+hyset_status hyset_verifier_output(const hyset_verifier* v, uint64_t* count, const hyset_pair** pairs);
+void hyset_verifier_destroy(hyset_verifier* v);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,70 @@
+/*
+ * oracle.h — CPU restatement of the reference's set-similarity self-join.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the checker for the CUDA path, and the
+ * timed CPU baseline of the benchmark; the product library never links, loads
+ * or calls it.  Each function cites the reference file:line it restates
+ * (paths relative to the chribell/hyset source tree).
+ *
+ * Parity pinning: the restatement is checked against the reference's own
+ * host::allpairs / host::ppjoin, compiled from its headers by oracle/Makefile
+ * (target `ref`) and run on seeded inputs; the fixtures in tests/golden/ were
+ * produced that way (tests/golden/make_golden.py).
+ */
+#ifndef HYSET_ORACLE_H
+#define HYSET_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORACLE_JACCARD = 0, ORACLE_COSINE = 1, ORACLE_DICE = 2 };
+
+/* Similarity bounds exactly as include/hyset/similarity.hpp:11-54 computes them
+ * (double arithmetic, same expression order, `hyset::min(int,int)` clamps).
+ * Cosine and dice have no reference code; they follow the same style. */
+uint32_t oracle_minoverlap(int sim, uint32_t len1, uint32_t len2, double t); /* generic, clamped */
+uint32_t oracle_minsize(int sim, uint32_t len, double t);
+uint32_t oracle_maxsize(int sim, uint32_t len, double t);
+uint32_t oracle_maxprefix(int sim, uint32_t len, double t);
+uint32_t oracle_midprefix(int sim, uint32_t len, double t);
+
+typedef struct oracle_pairs oracle_pairs;
+
+/* AllPairs (algo 0) or PPJoin (algo 1) of probes [probe_lo, probe_hi] against an
+ * inverted index over the midprefix entries of sets [index_lo, index_hi]
+ * (include/hyset/host_algorithms.hpp:16-129 and :131-250).  Pairs are
+ * (probe, indexed) with indexed < probe. */
+oracle_pairs* oracle_join(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
+                          uint32_t n_sets, uint32_t universe, int sim, double t, int algo,
+                          uint32_t index_lo, uint32_t index_hi, uint32_t probe_lo, uint32_t probe_hi);
+
+/* cpu_multi: `threads` std::thread-style workers over sqrt-balanced probe
+ * ranges, each with its own index over sets [0, end of its range]
+ * (src/cpu_multi.cu:118-149, :177-207).  The union of the workers' pairs. */
+oracle_pairs* oracle_join_multi(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
+                                uint32_t n_sets, uint32_t universe, int sim, double t, int algo,
+                                int threads);
+
+/* Exhaustive check of every pair: (p, c) with c < p, sizes[c] >= minsize(sizes[p])
+ * and |p ∩ c| >= minoverlap(sizes[p], sizes[c]).  Small inputs only. */
+oracle_pairs* oracle_brute(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
+                           uint32_t n_sets, int sim, double t);
+
+/* R-S join by exhaustive check: (s, r) for s in S, r in R with, for
+ * (b, m) = (max, min) of the two sizes, m >= minsize(b) and overlap >= minoverlap(b, m).
+ * Pairs are (probe s, indexed r).  Small inputs only. */
+oracle_pairs* oracle_brute_rs(const uint32_t* r_tokens, const uint32_t* r_starts, const uint32_t* r_sizes,
+                              uint32_t r_n, const uint32_t* s_tokens, const uint32_t* s_starts,
+                              const uint32_t* s_sizes, uint32_t s_n, int sim, double t);
+
+uint64_t oracle_pairs_count(const oracle_pairs* p);
+const uint32_t* oracle_pairs_data(const oracle_pairs* p); /* 2*count: (first, second) */
+void oracle_pairs_free(oracle_pairs* p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
