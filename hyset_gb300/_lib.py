@@ -34,7 +34,8 @@ TECH_NAMES = {v: k for k, v in TECH.items()}
 class JoinOpts(C.Structure):
     _fields_ = [("sim", C.c_int), ("threshold", C.c_double), ("technique", C.c_int), ("bitmap_bits", C.c_uint32),
                 ("count_only", C.c_uint32), ("verify_mode", C.c_uint32), ("sort_pairs", C.c_uint32),
-                ("pair_capacity", C.c_uint64), ("device_pairs", C.c_uint32), ("collect_stats", C.c_uint32)]
+                ("pair_capacity", C.c_uint64), ("device_pairs", C.c_uint32), ("collect_stats", C.c_uint32),
+                ("probe_begin", C.c_uint32), ("probe_end", C.c_uint32)]
 
 
 class Block(C.Structure):
@@ -70,6 +71,7 @@ PROTOTYPES = {
     "hyset_result_kernel_ms": (C.c_double, [C.c_void_p]),
     "hyset_result_device_pairs": (C.c_void_p, [C.c_void_p]),
     "hyset_result_stats": (C.c_uint32, [C.c_void_p, C.POINTER(C.c_uint64), C.c_uint32]),
+    "hyset_result_launches": (C.c_uint64, [C.c_void_p]),
     "hyset_result_free": (None, [C.c_void_p]),
     "hyset_handler_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_int,
                                        C.c_double, C.POINTER(C.c_void_p)]),

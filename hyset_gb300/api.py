@@ -27,18 +27,21 @@ class JoinResult:
     kernel_ms: float = 0.0
     stats: Optional[list] = None
     device_pairs: int = 0  # device address when device_pairs was requested
+    launches: int = 0      # kernel launches the join issued
 
 
 def make_opts(threshold: float = 0.8, sim: str = "jaccard", technique: str = "auto", bitmap: int = 0,
               count_only: bool = False, verify_mode: int = 0, sort_pairs: bool = False,
-              pair_capacity: int = 0, device_pairs: bool = False, collect_stats: bool = False) -> JoinOpts:
+              pair_capacity: int = 0, device_pairs: bool = False, collect_stats: bool = False,
+              probe_range=None) -> JoinOpts:
     if sim not in SIM:
         raise ValueError(f"unknown similarity {sim!r}")
     if technique not in TECH:
         raise ValueError(f"unknown technique {technique!r}")
     return JoinOpts(SIM[sim], float(threshold), TECH[technique], int(bitmap), int(bool(count_only)),
                     int(verify_mode), int(bool(sort_pairs)), int(pair_capacity), int(bool(device_pairs)),
-                    int(bool(collect_stats)))
+                    int(bool(collect_stats)), int(probe_range[0]) if probe_range else 0,
+                    int(probe_range[1]) if probe_range else 0)
 
 
 def _take_result(lib, r) -> JoinResult:
@@ -53,7 +56,8 @@ def _take_result(lib, r) -> JoinResult:
         k = lib.hyset_result_stats(r, st, 8)
         return JoinResult(int(n), pairs, TECH_NAMES.get(lib.hyset_result_technique(r), "?"),
                           float(lib.hyset_result_device_ms(r)), float(lib.hyset_result_kernel_ms(r)),
-                          [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0))
+                          [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0),
+                          int(lib.hyset_result_launches(r)))
     finally:
         lib.hyset_result_free(r)
 

@@ -148,15 +148,29 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
     return HYSET_OK;
 }
 
-// first_ge[l] = first id of the collection with size >= l, l in [0, L+1].
-hyset_status upload_first_ge(hyset_ctx* ctx, const hyset_coll* c, uint32_t L, DevBuf& buf) {
+// Per-collection size metadata, built once at upload: sets per size and
+// first_ge[l] = first id with size >= l (l in [0, max_size + 1]).
+hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c) {
+    const uint32_t L = c->max_size;
+    c->size_hist.assign((size_t)L + 1, 0);
+    for (uint32_t v : c->h_sizes) c->size_hist[v]++;
     std::vector<uint32_t> f((size_t)L + 2);
-    for (uint32_t l = 0; l <= L + 1; ++l)
-        f[l] = (uint32_t)(std::lower_bound(c->h_sizes.begin(), c->h_sizes.end(), l) - c->h_sizes.begin());
-    CK(buf.ensure(f.size() * 4, ctx->stream));
-    CK(cudaMemcpyAsync(buf.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    uint64_t run = 0;
+    for (uint32_t l = 0; l <= L + 1; ++l) {
+        f[l] = (uint32_t)run;
+        if (l <= L) run += c->size_hist[l];
+    }
+    CK(c->first_ge.ensure(f.size() * 4, ctx->stream));
+    CK(cudaMemcpyAsync(c->first_ge.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));  // f goes out of scope
     return HYSET_OK;
+}
+
+// Prefix entries of sets [lo, hi) (all sets when hi == n) from the size histogram.
+uint64_t prefix_entries(const hyset_coll* c, const std::vector<uint32_t>& pre) {
+    uint64_t E = 0;
+    for (size_t l = 0; l < c->size_hist.size(); ++l) E += c->size_hist[l] * (uint64_t)pre[l];
+    return E;
 }
 
 int key_bits_for(uint32_t universe) {
@@ -174,9 +188,7 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     Index& ix = c->index;
     cudaStream_t s = ctx->stream;
     const uint32_t n = c->n, U = c->universe;
-    uint64_t E = 0;
-    const std::vector<uint32_t>& pre = b->index_prefix;
-    for (uint32_t i = 0; i < n; ++i) E += pre[c->h_sizes[i]];
+    const uint64_t E = prefix_entries(c, b->index_prefix);
     if (E >= (1ull << 32)) return fail(ctx, HYSET_E_UNSUPPORTED, "more than 2^32 prefix entries");
     const uint64_t E1 = E ? E : 1;
     CK(ctx->s_len.ensure((size_t)n * 4 + 4, s));
@@ -320,16 +332,19 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     hyset_technique tech = o->technique == HYSET_TECH_AUTO ? choose_technique(R, o) : o->technique;
     int vmode = choose_vmode(R, o);
     res->technique = tech;
+    if (o->probe_end > S->n || o->probe_begin > o->probe_end)
+        return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
+    const unsigned long long launches0 = launches();
     CK(cudaEventRecord(ctx->ev0, ctx->stream));
-    ST(upload_first_ge(ctx, R, L, ctx->s_firstge));
     JoinParams P{};
     P.R = R->view();
     P.S = S->view();
     P.B = b->view;
-    P.first_ge = ctx->s_firstge.as<uint32_t>();
+    P.first_ge = R->first_ge.as<uint32_t>();
+    P.R_L = R->max_size;
     P.self = self ? 1 : 0;
-    P.p_lo = 0;
-    P.p_hi = S->n;
+    P.p_lo = o->probe_end ? o->probe_begin : 0;
+    P.p_hi = o->probe_end ? o->probe_end : S->n;
     P.r_lo = 0;
     P.r_hi = R->n;
     if (tech == HYSET_TECH_FGSS) {
@@ -354,6 +369,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
         res->stats[3] = R->index.entries;
     }
     res->stats[4] = S->n_tokens;
+    res->launches = launches() - launches0;
     if (o->sort_pairs && res->has_pairs)
         std::sort(res->pairs.begin(), res->pairs.end(), [](const hyset_pair& x, const hyset_pair& y) {
             return x.first != y.first ? x.first < y.first : x.second < y.second;
@@ -383,7 +399,7 @@ hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_si
     if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
     c->universe = c->n ? f[1] + 1 : 1;
     c->max_size = c->n ? c->h_sizes.back() : 0;
-    return HYSET_OK;
+    return build_size_meta(ctx, c);
 }
 
 }  // namespace
@@ -442,7 +458,7 @@ void hyset_destroy(hyset_ctx* ctx) {
         cudaStream_t s = ctx->stream;
         for (auto& kv : ctx->bounds) kv.second->dev.release(s);
         DevBuf* bufs[] = {&ctx->s_len, &ctx->s_off, &ctx->s_tok, &ctx->s_set, &ctx->s_pos, &ctx->s_order,
-                          &ctx->s_altk, &ctx->s_altv, &ctx->s_counts, &ctx->s_scan, &ctx->s_firstge,
+                          &ctx->s_altk, &ctx->s_altv, &ctx->s_counts, &ctx->s_scan,
                           &ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats};
         for (DevBuf* b : bufs) b->release(s);
         cudaStreamSynchronize(s);
@@ -534,6 +550,7 @@ void hyset_collection_free(hyset_ctx* ctx, hyset_coll* c) {
     c->index.list_off.release(s);
     c->index.set.release(s);
     c->index.pos.release(s);
+    c->first_ge.release(s);
     for (auto& kv : c->bitmaps) kv.second.release(s);
     cudaStreamSynchronize(s);
     delete c;
@@ -589,8 +606,11 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
 
 uint64_t hyset_result_count(const hyset_result* r) { return r ? r->count : 0; }
 const hyset_pair* hyset_result_pairs(const hyset_result* r) {
-    return (r && r->has_pairs) ? r->pairs.data() : nullptr;
+    static const hyset_pair none = {0, 0};
+    if (!r || !r->has_pairs) return nullptr;
+    return r->pairs.empty() ? &none : r->pairs.data();
 }
+uint64_t hyset_result_launches(const hyset_result* r) { return r ? r->launches : 0; }
 hyset_technique hyset_result_technique(const hyset_result* r) { return r ? r->technique : HYSET_TECH_AUTO; }
 double hyset_result_device_ms(const hyset_result* r) { return r ? r->device_ms : 0.0; }
 double hyset_result_kernel_ms(const hyset_result* r) { return r ? r->kernel_ms : 0.0; }
@@ -631,7 +651,6 @@ hyset_status hyset_handler_create(hyset_ctx* ctx, const hyset_coll* coll, hyset_
     h->block_size = block_size;
     h->aggregate = aggregate ? 1 : 0;
     ST(get_bounds(ctx, sim, threshold, coll->max_size, 0, &h->bounds));
-    ST(upload_first_ge(ctx, coll, coll->max_size, h->first_ge));
     cudaStream_t s = ctx->stream;
     if (technique == HYSET_TECH_BITMAP) {
         // bitmap::handler ctor generates every signature up front (device_algorithms.hpp:144-156)
@@ -658,7 +677,7 @@ hyset_status build_block_index(hyset_handler* h, const hyset_block& blk) {
     cudaStream_t s = ctx->stream;
     const hyset_coll* c = h->coll;
     const uint32_t lo = blk.start_id, hi = blk.end_id + 1, nb = hi - lo, U = c->universe;
-    uint64_t E = 0;
+    uint64_t E = 0;  // the block's prefix entries (block.entries in the reference)
     for (uint32_t i = lo; i < hi; ++i) E += h->bounds->index_prefix[c->h_sizes[i]];
     const uint64_t E1 = E ? E : 1;
     CK(h->counts.ensure(((size_t)U + 1) * 4, s));
@@ -707,7 +726,8 @@ hyset_status hyset_handler_join_blocks(hyset_handler* h, const hyset_block* firs
     P.R = h->coll->view();
     P.S = P.R;
     P.B = h->bounds->view;
-    P.first_ge = h->first_ge.as<uint32_t>();
+    P.first_ge = h->coll->first_ge.as<uint32_t>();
+    P.R_L = h->coll->max_size;
     P.self = 1;
     P.p_lo = second->start_id;
     P.p_hi = second->end_id + 1;
@@ -792,7 +812,7 @@ hyset_status hyset_handler_clear_output(hyset_handler* h) {
 void hyset_handler_destroy(hyset_handler* h) {
     if (!h) return;
     cudaStream_t s = h->ctx->stream;
-    DevBuf* bufs[] = {&h->first_ge, &h->counts, &h->list_off, &h->e_len, &h->e_off, &h->e_tok, &h->e_set, &h->e_pos,
+    DevBuf* bufs[] = {&h->counts, &h->list_off, &h->e_len, &h->e_off, &h->e_tok, &h->e_set, &h->e_pos,
                       &h->idx_set, &h->idx_pos, &h->scan, &h->bits, &h->pairs, &h->count, &h->work};
     for (DevBuf* b : bufs) b->release(s);
     cudaStreamSynchronize(s);

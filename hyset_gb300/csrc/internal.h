@@ -77,7 +77,7 @@ struct hyset_ctx {
     std::map<std::tuple<int, double, uint32_t, int>, std::unique_ptr<hs::Bounds>> bounds;
     // scratch reused across joins
     hs::DevBuf s_len, s_off, s_tok, s_set, s_pos, s_order, s_altk, s_altv, s_counts, s_scan;
-    hs::DevBuf s_firstge, s_pairs, s_count, s_work, s_stats;
+    hs::DevBuf s_pairs, s_count, s_work, s_stats;
 };
 
 struct hyset_coll {
@@ -91,6 +91,8 @@ struct hyset_coll {
     uint32_t max_size = 0;
     uint32_t universe = 0;  // max token + 1
     std::vector<uint32_t> h_sizes;
+    std::vector<uint64_t> size_hist;  // sets per size, [max_size+1]
+    hs::DevBuf first_ge;              // [max_size+2] first id with size >= l
     hs::Index index;
     std::map<int, hs::DevBuf> bitmaps;  // by words
     hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, n}; }
@@ -105,6 +107,7 @@ struct hyset_result {
     double device_ms = 0;
     double kernel_ms = 0;
     uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    uint64_t launches = 0;
 };
 
 struct hyset_handler {
@@ -117,7 +120,6 @@ struct hyset_handler {
     int aggregate = 0;
     int words = 0;
     hs::Bounds* bounds = nullptr;
-    hs::DevBuf first_ge;
     // per-indexed-block inverted index (reference layout: unsorted lists)
     hs::DevBuf counts, list_off, e_len, e_off, e_tok, e_set, e_pos, idx_set, idx_pos, scan;
     uint32_t indexed_block = 0xFFFFFFFFu;

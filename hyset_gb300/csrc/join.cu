@@ -40,12 +40,12 @@ struct Window {
 __device__ __forceinline__ Window candidate_window(const JoinParams& P, uint32_t p, uint32_t lp) {
     Window w;
     const uint32_t ms = P.B.minsize[lp];
-    w.lo = max(P.first_ge[ms], P.r_lo);
+    w.lo = max(P.first_ge[min(ms, P.R_L + 1)], P.r_lo);
     if (P.self) {
         w.hi = min(p, P.r_hi);
     } else {
-        uint32_t mx = min(P.B.max_partner[lp], P.B.L);
-        w.hi = min(P.first_ge[mx + 1], P.r_hi);
+        uint32_t mx = P.B.max_partner[lp];
+        w.hi = min(P.first_ge[min(mx + 1, P.R_L + 1)], P.r_hi);
     }
     return w;
 }
@@ -78,9 +78,10 @@ template <int VMODE>
 __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p, const uint32_t* a, uint32_t lp,
                                                 bool keep, uint32_t c, uint32_t lc, uint32_t mo, uint32_t own_a,
                                                 uint32_t own_b, int lane) {
+    uint32_t used = 0;
     if constexpr (VMODE == 1) {
         bool ok = false;
-        if (keep) ok = verify_serial(a, lp, P.R.tokens + P.R.starts[c], lc, mo, own_a);
+        if (keep) ok = verify_serial(a, lp, P.R.tokens + P.R.starts[c], lc, mo, own_a, &used);
         emit(P.out, ok, p, c, lane);
     } else {
         unsigned m = __ballot_sync(FULL, keep);
@@ -91,10 +92,13 @@ __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p,
             uint32_t ll = __shfl_sync(FULL, lc, src);
             uint32_t mm = __shfl_sync(FULL, mo, src);
             uint32_t ob = __shfl_sync(FULL, own_b, src);
-            bool ok = verify_warp(a, lp, P.R.tokens + P.R.starts[cc], ll, mm, ob, lane);
+            uint32_t u = 0;
+            bool ok = verify_warp(a, lp, P.R.tokens + P.R.starts[cc], ll, mm, ob, lane, &u);
+            if (lane == 0) used += u;
             emit(P.out, ok && lane == 0, p, cc, lane);
         }
     }
+    count_stat(P, 6, used, lane);
 }
 
 template <int VMODE, int W>
@@ -161,6 +165,7 @@ __device__ void fgss_probe(const JoinParams& P, uint32_t p, uint32_t* sbuf, int 
                 keep = 1u + min(lp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
             }
             count_stat(P, 0, q < total ? 1u : 0u, lane);
+            count_stat(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
             if (keep) keep = bitmap_pass<W>(P, bp, c, lp, lc, mo);
             count_stat(P, 1, keep ? 1u : 0u, lane);
             count_stat(P, 2, keep ? lc : 0u, lane);
@@ -199,6 +204,7 @@ __device__ void enum_probe(const JoinParams& P, uint32_t p, uint32_t* sbuf, int 
             keep = bitmap_pass<W>(P, bp, c, lp, lc, mo);
         }
         count_stat(P, 0, c < win.hi ? 1u : 0u, lane);
+        count_stat(P, 5, (W > 0 && c < win.hi) ? 1u : 0u, lane);
         count_stat(P, 1, keep ? 1u : 0u, lane);
         count_stat(P, 2, keep ? lc : 0u, lane);
         verify_and_emit<VMODE>(P, p, a, lp, keep, c, lc, mo, NOWN, NOWN, lane);
@@ -284,6 +290,7 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
 
 template <typename K>
 cudaError_t launch_persistent(K kernel, int sm_count, cudaStream_t s, const JoinParams& P) {
+    note_launches();
     const size_t smem = JOIN_WARPS * MAXP * sizeof(uint32_t);
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, JOIN_THREADS, smem);
@@ -321,6 +328,7 @@ cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const
                                      const uint32_t* offsets, const uint32_t* cands, uint32_t n_probes, int vmode,
                                      Sink out, unsigned int* work, int sm_count, cudaStream_t s) {
     if (n_probes == 0) return cudaSuccess;
+    note_launches();
     const size_t smem = JOIN_WARPS * MAXP * sizeof(uint32_t);
     int per_sm = 0;
     cudaError_t e;

@@ -9,6 +9,10 @@
 
 namespace hs {
 
+// Kernel launches issued by this library since load (bench bookkeeping).
+unsigned long long launches();
+void note_launches(unsigned n = 1);
+
 // ---- primitives.cu -------------------------------------------------------
 // Exclusive prefix sum of n uint32 values (in may equal out).  `scratch` must
 // hold scan_scratch_words(n) words.
@@ -69,7 +73,8 @@ struct JoinParams {
     CollView R;                 // indexed collection
     CollView S;                 // probe collection (== R for a self-join)
     BoundsView B;
-    const uint32_t* __restrict__ first_ge;  // [L+2] first id of R with size >= l
+    const uint32_t* __restrict__ first_ge;  // [R_L+2] first id of R with size >= l
+    uint32_t R_L;               // largest set size in R
     int self;                   // candidates c < p inside one collection
     uint32_t p_lo, p_hi;        // probe ids [p_lo, p_hi)
     uint32_t r_lo, r_hi;        // candidate ids restricted to [r_lo, r_hi)

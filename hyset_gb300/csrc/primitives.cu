@@ -7,7 +7,13 @@
 // bitmap::generate (include/hyset/device_algorithms.hpp:58-74).
 #include "kernels.h"
 
+#include <atomic>
+
 namespace hs {
+
+static std::atomic<unsigned long long> g_launches{0};
+unsigned long long launches() { return g_launches.load(); }
+void note_launches(unsigned n) { g_launches += n; }
 
 namespace {
 
@@ -285,11 +291,13 @@ size_t scan_scratch_words(uint64_t n) {
 cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     if (n <= SCAN_TILE) {
+        note_launches();
         k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
         return cudaGetLastError();
     }
     uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     uint32_t* sums = scratch;
+    note_launches(2);
     k_tile_reduce<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
@@ -317,6 +325,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
     uint32_t *kin = keys, *vin = vals, *kout = alt_keys, *vout = alt_vals;
     for (int p = 0; p < passes; ++p) {
         int shift = 8 * p;
+        note_launches(2);
         k_radix_upsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, n, shift, tile_counts, tiles);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
@@ -341,6 +350,7 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
 cudaError_t set_prefix_lengths(CollView c, const uint32_t* prefix_tab, uint32_t lo, uint32_t hi, uint32_t* out_len,
                                cudaStream_t s) {
     if (hi <= lo) return cudaSuccess;
+    note_launches();
     k_prefix_len<<<grid_for(hi - lo, 256), 256, 0, s>>>(c, prefix_tab, lo, hi, out_len);
     return cudaGetLastError();
 }
@@ -348,6 +358,7 @@ cudaError_t set_prefix_lengths(CollView c, const uint32_t* prefix_tab, uint32_t 
 cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint32_t* entry_off, const uint32_t* len,
                                 uint32_t* e_token, uint32_t* e_set, uint32_t* e_pos, cudaStream_t s) {
     if (hi <= lo) return cudaSuccess;
+    note_launches();
     k_emit_entries<<<grid_for((uint64_t)(hi - lo) * 32, 256), 256, 0, s>>>(c, lo, hi, entry_off, len, e_token,
                                                                             e_set, e_pos);
     return cudaGetLastError();
@@ -355,6 +366,7 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
 
 cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    note_launches();
     k_histogram<<<grid_for(n, 256), 256, 0, s>>>(e_token, n, counts);
     return cudaGetLastError();
 }
@@ -362,6 +374,7 @@ cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* count
 cudaError_t scatter_entries(const uint32_t* e_token, const uint32_t* e_set, const uint32_t* e_pos, uint64_t n,
                             uint32_t* cursor, uint32_t* idx_set, uint32_t* idx_pos, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    note_launches();
     k_scatter<<<grid_for(n, 256), 256, 0, s>>>(e_token, e_set, e_pos, n, cursor, idx_set, idx_pos);
     return cudaGetLastError();
 }
@@ -369,18 +382,21 @@ cudaError_t scatter_entries(const uint32_t* e_token, const uint32_t* e_set, cons
 cudaError_t gather_entries(const uint32_t* order, uint64_t n, const uint32_t* e_set, const uint32_t* e_pos,
                            uint32_t* idx_set, uint32_t* idx_pos, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    note_launches();
     k_gather<<<grid_for(n, 256), 256, 0, s>>>(order, n, e_set, e_pos, idx_set, idx_pos);
     return cudaGetLastError();
 }
 
 cudaError_t iota_u32(uint32_t* out, uint64_t n, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
+    note_launches();
     k_iota<<<grid_for(n, 256), 256, 0, s>>>(out, n);
     return cudaGetLastError();
 }
 
 cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s) {
     if (c.n == 0) return cudaSuccess;
+    note_launches();
     k_validate<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, n_tokens, flags);
     return cudaGetLastError();
 }
@@ -388,6 +404,7 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
 cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s) {
     if (c.n == 0) return cudaSuccess;
     unsigned g = grid_for((uint64_t)c.n * 32, 256);
+    note_launches();
     switch (words) {
     case 1: k_bitmaps<1><<<g, 256, 0, s>>>(c, out); break;
     case 2: k_bitmaps<2><<<g, 256, 0, s>>>(c, out); break;

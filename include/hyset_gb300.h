@@ -73,6 +73,8 @@ typedef struct {
     uint64_t pair_capacity;    /* initial device pair buffer; 0 = automatic (grows on demand) */
     uint32_t device_pairs;     /* 1 = leave the pairs in device memory (hyset_result_device_pairs) */
     uint32_t collect_stats;    /* 1 = count filter work (hyset_result_stats); costs a few atomics */
+    uint32_t probe_begin;      /* probe id range [probe_begin, probe_end) of this call; */
+    uint32_t probe_end;        /* 0, 0 = every probe (a shard of a join, e.g. one rank's part) */
 } hyset_join_opts;
 
 typedef struct hyset_ctx hyset_ctx;
@@ -140,8 +142,11 @@ double hyset_result_kernel_ms(const hyset_result* r);       /* CUDA-event time o
 const void* hyset_result_device_pairs(const hyset_result* r);
 /* Work counters when collect_stats was set: [0] filter items examined,
  * [1] items reaching verification, [2] candidate tokens of those items,
- * [3] index entries, [4] probe tokens; returns the number written (<= n). */
+ * [3] index entries, [4] probe tokens, [5] signature checks, [6] candidate
+ * tokens read by verification; returns the number written (<= n). */
 uint32_t hyset_result_stats(const hyset_result* r, uint64_t* out, uint32_t n);
+/* Kernel launches the join issued (index build, signatures, filter+verify). */
+uint64_t hyset_result_launches(const hyset_result* r);
 void hyset_result_free(hyset_result* r);
 
 /* ---- reference-shaped handlers -------------------------------------- */

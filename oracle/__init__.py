@@ -39,6 +39,12 @@ def _load():
         lib.oracle_join_multi.argtypes = [U32P, U32P, U32P, C.c_uint32, C.c_uint32, C.c_int, C.c_double, C.c_int,
                                           C.c_int]
         lib.oracle_join_multi.restype = C.c_void_p
+        lib.oracle_join_multi_range.argtypes = [U32P, U32P, U32P, C.c_uint32, C.c_uint32, C.c_int, C.c_double,
+                                                C.c_int, C.c_int, C.c_uint32, C.c_uint32]
+        lib.oracle_join_multi_range.restype = C.c_void_p
+        for name in ("oracle_last_timing", "oracle_last_multi_timing"):
+            getattr(lib, name).argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+            getattr(lib, name).restype = None
         lib.oracle_brute.argtypes = [U32P, U32P, U32P, C.c_uint32, C.c_int, C.c_double]
         lib.oracle_brute.restype = C.c_void_p
         lib.oracle_brute_rs.argtypes = [U32P, U32P, U32P, C.c_uint32, U32P, U32P, U32P, C.c_uint32, C.c_int,
@@ -100,6 +106,25 @@ def join_multi(tokens, starts, sizes, threshold, threads, sim="jaccard", algorit
     z, zp = _p(sizes)
     return _take(lib.oracle_join_multi(tp, sp, zp, len(z), universe_of(t), SIM[sim], float(threshold),
                                        1 if algorithm == "ppjoin" else 0, int(threads)))
+
+
+def join_multi_range(tokens, starts, sizes, threshold, threads, probe_range, sim="jaccard",
+                     algorithm="allpairs") -> np.ndarray:
+    """cpu_multi semantics restricted to probes [lo, hi] (a bounded sample)."""
+    lib = _load()
+    t, tp = _p(tokens)
+    s, sp = _p(starts)
+    z, zp = _p(sizes)
+    lo, hi = probe_range
+    return _take(lib.oracle_join_multi_range(tp, sp, zp, len(z), universe_of(t), SIM[sim], float(threshold),
+                                             1 if algorithm == "ppjoin" else 0, int(threads), int(lo), int(hi)))
+
+
+def last_timing(multi: bool = False):
+    """(index seconds, join seconds) of the last oracle join on this thread (or the last multi join)."""
+    a, b = C.c_double(), C.c_double()
+    (_load().oracle_last_multi_timing if multi else _load().oracle_last_timing)(C.byref(a), C.byref(b))
+    return a.value, b.value
 
 
 def brute(tokens, starts, sizes, threshold, sim="jaccard") -> np.ndarray:

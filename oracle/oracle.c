@@ -22,6 +22,25 @@
 #include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
+
+/* Seconds spent in the last index build / probe loop of this thread (the
+ * reference times the join separately from indexing, src/cpu_single.cu:98-140). */
+static _Thread_local double t_index_s, t_join_s;
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+static double g_multi_index_s, g_multi_join_s;
+void oracle_last_timing(double* index_s, double* join_s) {
+    if (index_s) *index_s = t_index_s;
+    if (join_s) *join_s = t_join_s;
+}
+void oracle_last_multi_timing(double* index_s, double* join_s) {
+    if (index_s) *index_s = g_multi_index_s;
+    if (join_s) *join_s = g_multi_join_s;
+}
 
 /* ---------------------------------------------------------------- bounds */
 
@@ -192,10 +211,13 @@ static int join_range(oracle_pairs* out, const uint32_t* tokens, const uint32_t*
                       double t, int algo, uint32_t index_lo, uint32_t index_hi,
                       uint32_t probe_lo, uint32_t probe_hi) {
     cpu_index ix;
+    double t0 = now_s();
     if (index_build(&ix, tokens, starts, sizes, universe, sim, t, index_lo, index_hi)) {
         index_free(&ix);
         return 1;
     }
+    double t1 = now_s();
+    t_index_s = t1 - t0;
     cand_data* cd = (cand_data*)calloc(n_sets ? n_sets : 1, sizeof(cand_data));
     uint32_t* cands = (uint32_t*)malloc((n_sets ? n_sets : 1) * sizeof(uint32_t));
     if (!cd || !cands) {
@@ -280,6 +302,7 @@ static int join_range(oracle_pairs* out, const uint32_t* tokens, const uint32_t*
             c->count = 0;
         }
     }
+    t_join_s = now_s() - t1;
     free(cd);
     free(cands);
     index_free(&ix);
@@ -305,7 +328,7 @@ typedef struct {
     const uint32_t *tokens, *starts, *sizes;
     uint32_t n_sets, universe, lo, hi;
     int sim, algo, err;
-    double t;
+    double t, index_s, join_s;
     oracle_pairs* out;
 } worker_arg;
 
@@ -313,31 +336,43 @@ static void* worker(void* a) {
     worker_arg* w = (worker_arg*)a;
     w->out = pairs_new();
     if (!w->out) { w->err = 1; return NULL; }
-    if (w->lo <= w->hi)
+    if (w->lo <= w->hi) {
         w->err = join_range(w->out, w->tokens, w->starts, w->sizes, w->n_sets, w->universe, w->sim,
                             w->t, w->algo, 0, w->hi, w->lo, w->hi);
+        w->index_s = t_index_s;
+        w->join_s = t_join_s;
+    }
     return NULL;
 }
 
 oracle_pairs* oracle_join_multi(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
                                 uint32_t n_sets, uint32_t universe, int sim, double t, int algo,
                                 int threads) {
+    return oracle_join_multi_range(tokens, starts, sizes, n_sets, universe, sim, t, algo, threads, 0,
+                                   n_sets ? n_sets - 1 : 0);
+}
+
+oracle_pairs* oracle_join_multi_range(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
+                                      uint32_t n_sets, uint32_t universe, int sim, double t, int algo,
+                                      int threads, uint32_t probe_lo, uint32_t probe_hi) {
     if (threads < 1) threads = 1;
     oracle_pairs* out = pairs_new();
-    if (!out || n_sets == 0) return out;
+    if (!out || n_sets == 0 || probe_lo > probe_hi || probe_hi >= n_sets) return out;
+    const uint32_t k = probe_hi - probe_lo + 1;
     worker_arg* args = (worker_arg*)calloc((size_t)threads, sizeof(worker_arg));
     pthread_t* th = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
     if (!args || !th) { free(args); free(th); oracle_pairs_free(out); return NULL; }
     /* x_i = k * sqrt((i + 1) / P), truncated: cpu_multi.cu:118-125 */
-    uint32_t prev = 0;
+    uint32_t prev = probe_lo;
     for (int i = 0; i < threads; ++i) {
-        uint32_t point = (uint32_t)((double)n_sets * sqrt((double)(i + 1) / (double)threads));
+        uint32_t point = probe_lo + (uint32_t)((double)k * sqrt((double)(i + 1) / (double)threads));
         worker_arg* w = &args[i];
         w->tokens = tokens; w->starts = starts; w->sizes = sizes;
         w->n_sets = n_sets; w->universe = universe; w->sim = sim; w->algo = algo; w->t = t;
         w->lo = prev;
         w->hi = point ? point - 1 : 0;
         if (point <= prev) w->hi = 0, w->lo = 1; /* empty range */
+        if (i == threads - 1 && point <= probe_hi && point > prev) w->hi = probe_hi;
         prev = point > prev ? point : prev;
     }
     int err = 0;
@@ -345,6 +380,11 @@ oracle_pairs* oracle_join_multi(const uint32_t* tokens, const uint32_t* starts, 
         if (pthread_create(&th[i], NULL, worker, &args[i])) { worker(&args[i]); th[i] = 0; }
     for (int i = 0; i < threads; ++i)
         if (th[i]) pthread_join(th[i], NULL);
+    g_multi_index_s = g_multi_join_s = 0;
+    for (int i = 0; i < threads; ++i) {
+        if (args[i].index_s > g_multi_index_s) g_multi_index_s = args[i].index_s;
+        if (args[i].join_s > g_multi_join_s) g_multi_join_s = args[i].join_s;
+    }
     for (int i = 0; i < threads; ++i) {
         if (args[i].err || !args[i].out || pairs_append(out, args[i].out)) err = 1;
         oracle_pairs_free(args[i].out);

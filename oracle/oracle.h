@@ -48,6 +48,17 @@ oracle_pairs* oracle_join_multi(const uint32_t* tokens, const uint32_t* starts, 
                                 uint32_t n_sets, uint32_t universe, int sim, double t, int algo,
                                 int threads);
 
+/* The same over probes [probe_lo, probe_hi] only (sqrt split within the range;
+ * a bounded sample of a join). */
+oracle_pairs* oracle_join_multi_range(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
+                                      uint32_t n_sets, uint32_t universe, int sim, double t, int algo,
+                                      int threads, uint32_t probe_lo, uint32_t probe_hi);
+
+/* Wall seconds of the last index build and probe loop on the calling thread
+ * (oracle_join), or the slowest worker of the last multi-threaded join. */
+void oracle_last_timing(double* index_s, double* join_s);
+void oracle_last_multi_timing(double* index_s, double* join_s);
+
 /* Exhaustive check of every pair: (p, c) with c < p, sizes[c] >= minsize(sizes[p])
  * and |p ∩ c| >= minoverlap(sizes[p], sizes[c]).  Small inputs only. */
 oracle_pairs* oracle_brute(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
