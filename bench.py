@@ -192,7 +192,7 @@ def run_ours(args, ws, rank, local):
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     kw = dict(threshold=THRESHOLD, technique=args.technique, bitmap=args.bitmap, device_pairs=True,
-              probe_range=(p_lo, p_hi))
+              probe_range=(p_lo, p_hi), probe_major=args.probe_major, verify_mode=args.vmode)
 
     def barrier():
         torch.cuda.synchronize()
@@ -200,8 +200,7 @@ def run_ours(args, ws, rank, local):
             dist.barrier()
 
     # untimed: work counters for the roofline, and a parity spot check of the shard
-    st_run = ctx.self_join(coll, threshold=THRESHOLD, technique=args.technique, bitmap=args.bitmap,
-                           collect_stats=True, device_pairs=True, probe_range=(p_lo, p_hi))
+    st_run = ctx.self_join(coll, collect_stats=True, **kw)
     for _ in range(args.warmup):
         ctx.self_join(coll, **kw)
     barrier()
@@ -297,7 +296,7 @@ def run_ours(args, ws, rank, local):
                           "kernel_ms": kms},
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                            "algorithmic_bytes_per_launch": alg, "kernel": "k_join (fgss filter+verify)"},
+                            "algorithmic_bytes_per_launch": alg, "kernel": "k_join (probe-major FGSS filter + verify, persistent)"},
                "cpu_baseline": cpu,
                "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": e2e_pairs_bytes + 8, "ms_per_step": 1000.0 * e2e_mean},
@@ -322,6 +321,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the block-pair baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
+    ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
+    ap.add_argument("--vmode", type=int, default=0, help="verification: 0 auto, 1 lane, 2 warp per candidate")
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.impl == "reference":

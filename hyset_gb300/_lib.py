@@ -35,7 +35,8 @@ class JoinOpts(C.Structure):
     _fields_ = [("sim", C.c_int), ("threshold", C.c_double), ("technique", C.c_int), ("bitmap_bits", C.c_uint32),
                 ("count_only", C.c_uint32), ("verify_mode", C.c_uint32), ("sort_pairs", C.c_uint32),
                 ("pair_capacity", C.c_uint64), ("device_pairs", C.c_uint32), ("collect_stats", C.c_uint32),
-                ("probe_begin", C.c_uint32), ("probe_end", C.c_uint32)]
+                ("probe_begin", C.c_uint32), ("probe_end", C.c_uint32), ("probe_major", C.c_uint32),
+                ("fgss_batch", C.c_uint32)]
 
 
 class Block(C.Structure):

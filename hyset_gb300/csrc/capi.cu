@@ -173,6 +173,15 @@ uint64_t prefix_entries(const hyset_coll* c, const std::vector<uint32_t>& pre) {
     return E;
 }
 
+// Bits needed to represent v (at least 1).
+uint32_t bits_for(uint64_t v) {
+    uint32_t b = 1;
+    while (b < 64 && (v >> b)) ++b;
+    return b;
+}
+
+uint32_t pre_len(const Bounds* b, uint32_t l) { return b->index_prefix[l]; }
+
 int key_bits_for(uint32_t universe) {
     int bits = 1;
     while (bits < 32 && (universe - 1) >> bits) ++bits;
@@ -212,6 +221,27 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     uint32_t* scr = ctx->s_scan.as<uint32_t>();
     CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
     CK(scan_exclusive(len, off, n, scr, s));
+    // Packed entries (set << pb | position) when set ids up to n and positions
+    // below the longest prefix fit 32 bits: the sorted values are the index.
+    uint32_t max_pre = 1;
+    for (size_t l = 0; l < c->size_hist.size(); ++l)
+        if (c->size_hist[l]) max_pre = std::max(max_pre, pre_len(b, (uint32_t)l));
+    const uint32_t pb = bits_for(max_pre), sb = bits_for(n);
+    if (pb + sb <= 32) {
+        uint32_t* counts = ctx->s_counts.as<uint32_t>();
+        CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+        CK(emit_packed_entries(v, off, len, pb, ctx->s_tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
+        CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
+        CK(radix_sort_pairs(ctx->s_tok.as<uint32_t>(), ix.set.as<uint32_t>(), ctx->s_altk.as<uint32_t>(),
+                            ctx->s_altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
+        ix.sim = b->sim;
+        ix.tau = b->tau;
+        ix.kind = kind;
+        ix.universe = U;
+        ix.entries = E;
+        ix.pos_bits = pb;
+        return HYSET_OK;
+    }
     CK(emit_prefix_entries(v, 0, n, off, len, ctx->s_tok.as<uint32_t>(), ctx->s_set.as<uint32_t>(),
                            ctx->s_pos.as<uint32_t>(), s));
     uint32_t* counts = ctx->s_counts.as<uint32_t>();
@@ -228,6 +258,29 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     ix.kind = kind;
     ix.universe = U;
     ix.entries = E;
+    ix.pos_bits = 0;
+    return HYSET_OK;
+}
+
+// Token groups of the first pre[size] tokens of every set (histogram, scan,
+// atomic scatter).  Rebuilt on every join; buffers are reused.
+hyset_status build_groups(hyset_ctx* ctx, hyset_coll* c, const uint32_t* d_pre, const std::vector<uint32_t>& pre,
+                          uint32_t U, uint64_t* entries) {
+    cudaStream_t s = ctx->stream;
+    const uint64_t E = prefix_entries(c, pre);
+    if (E >= (1ull << 32)) return fail(ctx, HYSET_E_UNSUPPORTED, "more than 2^32 prefix entries");
+    CK(c->g_off.ensure(((size_t)U + 1) * 4, s));
+    CK(c->g_cursor.ensure(((size_t)U + 1) * 4, s));
+    CK(c->g_set.ensure((E ? E : 1) * 4, s));
+    CK(c->g_ps.ensure((E ? E : 1) * 4, s));
+    CK(ctx->s_scan.ensure(scan_scratch_words((uint64_t)U + 1) * 4, s));
+    uint32_t* cnt = c->g_cursor.as<uint32_t>();
+    CK(cudaMemsetAsync(cnt, 0, ((size_t)U + 1) * 4, s));
+    CK(group_count(c->view(), d_pre, cnt, s));
+    CK(scan_exclusive(cnt, c->g_off.as<uint32_t>(), (uint64_t)U + 1, ctx->s_scan.as<uint32_t>(), s));
+    CK(cudaMemcpyAsync(cnt, c->g_off.p, ((size_t)U + 1) * 4, cudaMemcpyDeviceToDevice, s));
+    CK(group_scatter(c->view(), d_pre, cnt, c->g_set.as<uint32_t>(), c->g_ps.as<uint32_t>(), s));
+    *entries = E;
     return HYSET_OK;
 }
 
@@ -253,26 +306,42 @@ hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
     return HYSET_OK;
 }
 
-// Heuristic technique choice used until the learned selector is loaded: short
-// sets favour enumerating the length window with signatures, long sets the
-// prefix index.
-hyset_technique choose_technique(const hyset_coll* R, const hyset_join_opts* o) {
-    double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
-    if (R->n <= 20000 && avg <= 64) return HYSET_TECH_BITMAP;
-    (void)o;
-    return HYSET_TECH_FGSS;
-}
+// The autotuner's per-join configuration (technique, kernel variant, signature
+// width, batch, verification mode).  Explicit options always win; AUTO fills
+// the rest from collection statistics with rules measured on GB300
+// (1M-set long-set workload: probe-major, batch 4, 256-bit signatures; 200K-set
+// short-set workload: 128-bit signatures; token-major only on request, it wins
+// only where every token group is small, i.e. high thresholds; enumerating the
+// length window only for small collections).
+struct Tuned {
+    hyset_technique tech;
+    int probe_major;
+    uint32_t batch;
+    uint32_t bits;
+    int vmode;
+};
 
-int choose_vmode(const hyset_coll* R, const hyset_join_opts* o) {
-    if (o->verify_mode) return (int)o->verify_mode;
-    double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
-    return avg <= 48 ? 1 : 2;
+Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o) {
+    Tuned t{};
+    const double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
+    const uint64_t pairs_window = (uint64_t)R->n * (uint64_t)S->n;
+    t.tech = o->technique;
+    if (t.tech == HYSET_TECH_AUTO) t.tech = (pairs_window <= 4000000ull) ? HYSET_TECH_BITMAP : HYSET_TECH_FGSS;
+    // explicit FGSS defaults to the token-major kernel; AUTO to probe-major
+    t.probe_major = (o->technique == HYSET_TECH_FGSS && !o->probe_major) ? 0 : 1;
+    t.batch = o->fgss_batch ? o->fgss_batch : 4;
+    t.bits = o->bitmap_bits;
+    if (o->technique == HYSET_TECH_AUTO && t.bits == 0) t.bits = avg <= 48.0 ? 128 : 256;
+    if (t.tech == HYSET_TECH_BITMAP && t.bits == 0) t.bits = 64;
+    if (t.tech == HYSET_TECH_DIRECT) t.bits = 0;
+    t.vmode = o->verify_mode ? (int)o->verify_mode : 1;
+    return t;
 }
 
 // Runs one configured join launch into the context's pair buffer, growing the
 // buffer and re-running when the first pass overflowed.
 hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const hyset_join_opts* o,
-                      hyset_result* res, bool timed_from_ev0) {
+                      hyset_result* res, bool timed_from_ev0, TokenJoinParams* T = nullptr) {
     cudaStream_t s = ctx->stream;
     const int count_only = o->count_only ? 1 : 0;
     uint64_t cap = o->pair_capacity ? o->pair_capacity : std::max<uint64_t>(1u << 20, 4ull * P.S.n);
@@ -293,7 +362,14 @@ hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const h
         CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
         if (P.stats) CK(cudaMemsetAsync(P.stats, 0, 64, s));
         CK(cudaEventRecord(ctx->ek0, s));
-        CK(launch_join(P, tech, vmode, ctx->sm_count, s));
+        if (T) {
+            T->out = P.out;
+            T->work = P.work;
+            T->stats = P.stats;
+            CK(launch_join_tm(*T, ctx->sm_count, s));
+        } else {
+            CK(launch_join(P, tech, vmode, ctx->sm_count, s));
+        }
         CK(cudaEventRecord(ctx->ek1, s));
         CK(cudaEventRecord(ctx->ev1, s));
         unsigned long long count = 0;
@@ -329,8 +405,9 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     const uint32_t L = std::max(R->max_size, S->max_size);
     Bounds* b = nullptr;
     ST(get_bounds(ctx, o->sim, o->threshold, L, self ? 0 : 1, &b));
-    hyset_technique tech = o->technique == HYSET_TECH_AUTO ? choose_technique(R, o) : o->technique;
-    int vmode = choose_vmode(R, o);
+    const Tuned tn = tune(R, S, o);
+    const hyset_technique tech = tn.tech;
+    const int vmode = tn.vmode;
     res->technique = tech;
     if (o->probe_end > S->n || o->probe_begin > o->probe_end)
         return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
@@ -343,17 +420,41 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     P.first_ge = R->first_ge.as<uint32_t>();
     P.R_L = R->max_size;
     P.self = self ? 1 : 0;
+    P.grab = tech == HYSET_TECH_FGSS ? std::min<uint32_t>(tn.batch, 32) : 1;
     P.p_lo = o->probe_end ? o->probe_begin : 0;
     P.p_hi = o->probe_end ? o->probe_end : S->n;
     P.r_lo = 0;
     P.r_hi = R->n;
-    if (tech == HYSET_TECH_FGSS) {
+    const bool token_major = tech == HYSET_TECH_FGSS && L < 65536 && !tn.probe_major;
+    uint64_t group_entries = 0;
+    TokenJoinParams T{};
+    if (token_major) {
+        // probes: maxprefix entries of S; candidates: the same groups (self-join,
+        // midprefix filter in the kernel) or R's maxprefix entries (R-S join)
+        const uint32_t U = std::max(R->universe, S->universe);
+        ST(build_groups(ctx, S, b->view.probe_prefix, b->probe_prefix, U, &group_entries));
+        if (!self) {
+            uint64_t er = 0;
+            ST(build_groups(ctx, R, b->view.index_prefix, b->index_prefix, U, &er));
+            group_entries += er;
+        }
+        T.R = R->view();
+        T.S = S->view();
+        T.B = b->view;
+        T.gs_off = S->g_off.as<uint32_t>();
+        T.gs_set = S->g_set.as<uint32_t>();
+        T.gs_ps = S->g_ps.as<uint32_t>();
+        T.gr_off = R->g_off.as<uint32_t>();
+        T.gr_set = R->g_set.as<uint32_t>();
+        T.gr_ps = R->g_ps.as<uint32_t>();
+        T.universe = U;
+        T.self = self ? 1 : 0;
+        T.grab = 16;
+    } else if (tech == HYSET_TECH_FGSS) {
         ST(build_sorted_index(ctx, R, b, self ? 0 : 1));
         P.X = R->index.view();
     }
-    int words = (int)(o->bitmap_bits / 64);
-    if (tech == HYSET_TECH_BITMAP && words == 0) words = 1;  // the bitmap technique needs signatures
-    if (tech == HYSET_TECH_DIRECT) words = 0;
+    const int words = (int)(tn.bits / 64);
     if (words) {
         const uint64_t *br = nullptr, *bs = nullptr;
         ST(get_bitmaps(ctx, R, words, &br));
@@ -364,11 +465,20 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
         P.words = words;
     }
     int ktech = tech == HYSET_TECH_FGSS ? TECH_FGSS : (tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
-    ST(run_join(ctx, P, ktech, vmode, o, res, true));
-    if (P.X.set && o->collect_stats) {
+    if (token_major) {
+        T.bits_R = P.bits_R;
+        T.bits_S = P.bits_S;
+        T.words = P.words;
+        if (o->probe_end && (o->probe_begin || o->probe_end != S->n))
+            return fail(ctx, HYSET_E_UNSUPPORTED, "probe ranges need the probe-major kernel (probe_major = 1)");
+        ST(run_join(ctx, P, ktech, vmode, o, res, true, &T));
+        res->stats[3] = group_entries;
+    } else {
+        ST(run_join(ctx, P, ktech, vmode, o, res, true));
+    }
+    if (P.X.set && o->collect_stats && !token_major) {
         res->stats[3] = R->index.entries;
     }
-    res->stats[4] = S->n_tokens;
     res->launches = launches() - launches0;
     if (o->sort_pairs && res->has_pairs)
         std::sort(res->pairs.begin(), res->pairs.end(), [](const hyset_pair& x, const hyset_pair& y) {
@@ -387,6 +497,7 @@ hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_si
     DevBuf flags;
     CK(flags.ensure(16, s));
     CK(cudaMemsetAsync(flags.p, 0, 16, s));
+    CK(c->meta.ensure((size_t)c->n * sizeof(uint2) + 8, s));
     CK(validate_collection(c->view(), c->n_tokens, flags.as<uint32_t>(), s));
     uint32_t f[2] = {0, 0};
     CK(cudaMemcpyAsync(f, flags.p, 8, cudaMemcpyDeviceToHost, s));
@@ -399,6 +510,7 @@ hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_si
     if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
     c->universe = c->n ? f[1] + 1 : 1;
     c->max_size = c->n ? c->h_sizes.back() : 0;
+    CK(build_meta(c->view(), c->meta.as<uint2>(), s));
     return build_size_meta(ctx, c);
 }
 
@@ -547,10 +659,15 @@ void hyset_collection_free(hyset_ctx* ctx, hyset_coll* c) {
     c->tokens.release(s);
     c->starts.release(s);
     c->sizes.release(s);
+    c->meta.release(s);
     c->index.list_off.release(s);
     c->index.set.release(s);
     c->index.pos.release(s);
     c->first_ge.release(s);
+    c->g_off.release(s);
+    c->g_set.release(s);
+    c->g_ps.release(s);
+    c->g_cursor.release(s);
     for (auto& kv : c->bitmaps) kv.second.release(s);
     cudaStreamSynchronize(s);
     delete c;
@@ -729,6 +846,7 @@ hyset_status hyset_handler_join_blocks(hyset_handler* h, const hyset_block* firs
     P.first_ge = h->coll->first_ge.as<uint32_t>();
     P.R_L = h->coll->max_size;
     P.self = 1;
+    P.grab = h->technique == HYSET_TECH_FGSS ? 4 : 1;
     P.p_lo = second->start_id;
     P.p_hi = second->end_id + 1;
     P.r_lo = first->start_id;

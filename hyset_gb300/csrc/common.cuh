@@ -22,6 +22,7 @@ struct CollView {
     const uint32_t* __restrict__ tokens;
     const uint32_t* __restrict__ starts;
     const uint32_t* __restrict__ sizes;
+    const uint2* __restrict__ meta;  // (start, size) per set: one 8-byte load instead of two
     uint32_t n;
 };
 

@@ -55,12 +55,14 @@ struct Index {
     DevBuf list_off, set, pos;
     uint32_t universe = 0;
     uint64_t entries = 0;
+    uint32_t pos_bits = 0;  // > 0: packed (set << pos_bits) | position entries
     IndexView view() const {
         IndexView v;
         v.list_off = list_off.as<uint32_t>();
         v.set = set.as<uint32_t>();
-        v.pos = pos.as<uint32_t>();
+        v.pos = pos_bits ? nullptr : pos.as<uint32_t>();
         v.universe = universe;
+        v.pos_bits = pos_bits;
         v.sorted = 1;
         return v;
     }
@@ -82,7 +84,7 @@ struct hyset_ctx {
 
 struct hyset_coll {
     hyset_ctx* ctx = nullptr;
-    hs::DevBuf tokens, starts, sizes;
+    hs::DevBuf tokens, starts, sizes, meta;
     const uint32_t* d_tokens = nullptr;  // may point at caller memory (from_device)
     const uint32_t* d_starts = nullptr;
     const uint32_t* d_sizes = nullptr;
@@ -94,8 +96,9 @@ struct hyset_coll {
     std::vector<uint64_t> size_hist;  // sets per size, [max_size+1]
     hs::DevBuf first_ge;              // [max_size+2] first id with size >= l
     hs::Index index;
+    hs::DevBuf g_off, g_set, g_ps, g_cursor;  // token groups of the prefix entries (token-major join)
     std::map<int, hs::DevBuf> bitmaps;  // by words
-    hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, n}; }
+    hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, meta.as<uint2>(), n}; }
 };
 
 struct hyset_result {

@@ -34,6 +34,10 @@ cudaError_t set_prefix_lengths(CollView c, const uint32_t* prefix_tab, uint32_t 
 cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint32_t* entry_off,
                                 const uint32_t* len, uint32_t* e_token, uint32_t* e_set,
                                 uint32_t* e_pos, cudaStream_t s);
+// Packed form: e_token[k] = token, e_val[k] = (set << pos_bits) | position, and the
+// token histogram counts[token]++ (warp-aggregated) in the same pass.
+cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
+                                uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s);
 
 // Token histogram of n entries into counts[universe] (warp-aggregated atomics;
 // the counts are NOT zeroed here).
@@ -56,6 +60,9 @@ cudaError_t iota_u32(uint32_t* out, uint64_t n, cudaStream_t s);
 // flags[1] gets the largest token (atomicMax).  flags must be zeroed first.
 cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s);
 
+// meta[i] = (starts[i], sizes[i]).
+cudaError_t build_meta(CollView c, uint2* meta, cudaStream_t s);
+
 // XOR bitmap signatures, bit (token mod bits) per token
 // (include/hyset/device_algorithms.hpp:58-74), words = bits / 64 in {1,2,4,8}.
 cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s);
@@ -63,9 +70,10 @@ cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t 
 // ---- join.cu --------------------------------------------------------------
 struct IndexView {
     const uint32_t* __restrict__ list_off;  // [universe+1]: list t = [list_off[t], list_off[t+1])
-    const uint32_t* __restrict__ set;       // entry set ids
-    const uint32_t* __restrict__ pos;       // entry positions within their sets
+    const uint32_t* __restrict__ set;       // entry set ids, or (set << pos_bits) | position when pos == nullptr
+    const uint32_t* __restrict__ pos;       // entry positions within their sets (unpacked layout)
     uint32_t universe;
+    uint32_t pos_bits;                      // packed layout: bits of the position field
     int sorted;                             // lists ordered by set id
 };
 
@@ -84,6 +92,7 @@ struct JoinParams {
     int words;
     Sink out;
     unsigned int* work;         // work-stealing counter, zero before launch
+    uint32_t grab;              // probes taken per steal
     unsigned long long* stats;  // optional [8] counters (nullptr = off)
 };
 
@@ -92,6 +101,37 @@ enum Technique : int { TECH_BITMAP = 1, TECH_FGSS = 2, TECH_DIRECT = 3 };
 // One persistent, work-stealing launch over probes [p_lo, p_hi).
 // vmode: 1 = lane per candidate, 2 = warp per candidate.
 cudaError_t launch_join(const JoinParams& P, int technique, int vmode, int sm_count, cudaStream_t s);
+
+// ---- join_tm.cu ------------------------------------------------------------
+// Token groups: for every token, the entries (set, pos | size << 16) of the sets
+// whose first pre[size] tokens contain it.  counts must be zeroed; cursor holds
+// the groups' start offsets and advances.
+cudaError_t group_count(CollView c, const uint32_t* pre, uint32_t* counts, cudaStream_t s);
+cudaError_t group_scatter(CollView c, const uint32_t* pre, uint32_t* cursor, uint32_t* gset, uint32_t* gps,
+                          cudaStream_t s);
+
+struct TokenJoinParams {
+    CollView R, S;
+    BoundsView B;
+    const uint32_t* __restrict__ gs_off;  // probe groups (S, maxprefix entries), [universe+1]
+    const uint32_t* __restrict__ gs_set;
+    const uint32_t* __restrict__ gs_ps;
+    const uint32_t* __restrict__ gr_off;  // candidate groups (R), [universe+1]
+    const uint32_t* __restrict__ gr_set;
+    const uint32_t* __restrict__ gr_ps;
+    uint32_t universe;
+    int self;
+    const uint64_t* __restrict__ bits_R;
+    const uint64_t* __restrict__ bits_S;
+    int words;
+    Sink out;
+    unsigned int* work;
+    uint32_t grab;
+    unsigned long long* stats;
+};
+
+// One persistent launch; warps steal token groups, largest token ids first.
+cudaError_t launch_join_tm(const TokenJoinParams& P, int sm_count, cudaStream_t s);
 
 // Explicit candidate lists (hybrid::device_handler): probes[i] owns candidates
 // [i ? offsets[i-1] : 0, offsets[i]).

@@ -7,6 +7,7 @@
 // bitmap::generate (include/hyset/device_algorithms.hpp:58-74).
 #include "kernels.h"
 
+#include <algorithm>
 #include <atomic>
 
 namespace hs {
@@ -74,24 +75,28 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const uint32_t* in, 
 }
 
 // ---- radix sort -----------------------------------------------------------
+// Digits of up to 10 bits (a 20-bit token key sorts in two passes).
 constexpr int RADIX_THREADS = 256;
 constexpr int RADIX_WARPS = RADIX_THREADS / 32;
 constexpr int RADIX_ROUNDS = 16;                                  // 32-item rounds per warp
 constexpr uint32_t RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;     // 4096
-constexpr int RADIX_BINS = 256;
+constexpr int RADIX_MAX_BITS = 10;
+constexpr int RADIX_BINS = 1 << RADIX_MAX_BITS;
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_upsweep(const uint32_t* keys, uint64_t n, int shift,
-                                                                 uint32_t* tile_counts, uint32_t tiles) {
+                                                                 uint32_t mask, uint32_t* tile_counts,
+                                                                 uint32_t tiles) {
     __shared__ uint32_t hist[RADIX_BINS];
-    hist[threadIdx.x] = 0;
+    for (uint32_t d = threadIdx.x; d <= mask; d += RADIX_THREADS) hist[d] = 0;
     __syncthreads();
     uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE;
     for (uint32_t i = threadIdx.x; i < RADIX_TILE; i += RADIX_THREADS) {
         uint64_t idx = base + i;
-        if (idx < n) atomicAdd(&hist[(keys[idx] >> shift) & (RADIX_BINS - 1)], 1u);
+        if (idx < n) atomicAdd(&hist[(keys[idx] >> shift) & mask], 1u);
     }
     __syncthreads();
-    tile_counts[(uint64_t)threadIdx.x * tiles + blockIdx.x] = hist[threadIdx.x];
+    for (uint32_t d = threadIdx.x; d <= mask; d += RADIX_THREADS)
+        tile_counts[(uint64_t)d * tiles + blockIdx.x] = hist[d];
 }
 
 // Stable scatter: an item's rank inside its tile is the number of equal digits
@@ -99,12 +104,16 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_upsweep(const uint32_t*
 // order, 32 at a time, peers found with __match_any_sync).
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_t* __restrict__ keys,
                                                                    const uint32_t* __restrict__ vals, uint64_t n,
-                                                                   int shift, const uint32_t* __restrict__ tile_off,
+                                                                   int shift, uint32_t mask,
+                                                                   const uint32_t* __restrict__ tile_off,
                                                                    uint32_t tiles, uint32_t* keys_out,
                                                                    uint32_t* vals_out) {
     __shared__ uint32_t whist[RADIX_WARPS][RADIX_BINS];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int i = threadIdx.x; i < RADIX_WARPS * RADIX_BINS; i += RADIX_THREADS) (&whist[0][0])[i] = 0;
+    const uint32_t bins = mask + 1;
+    for (uint32_t d = threadIdx.x; d < bins; d += RADIX_THREADS)
+#pragma unroll
+        for (int w = 0; w < RADIX_WARPS; ++w) whist[w][d] = 0;
     __syncthreads();
     uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE + (uint64_t)warp * (32 * RADIX_ROUNDS);
     uint32_t k[RADIX_ROUNDS], v[RADIX_ROUNDS], rank[RADIX_ROUNDS];
@@ -113,7 +122,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_
         uint64_t idx = base + (uint64_t)r * 32 + lane;
         bool valid = idx < n;
         uint32_t key = valid ? keys[idx] : 0;
-        uint32_t d = valid ? ((key >> shift) & (RADIX_BINS - 1)) : RADIX_BINS;
+        uint32_t d = valid ? ((key >> shift) & mask) : 0xFFFFFFFFu;
         unsigned peers = __match_any_sync(FULL, d);
         int leader = __ffs(peers) - 1;
         uint32_t cnt = valid ? whist[warp][d] : 0;
@@ -125,12 +134,12 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_
         v[r] = valid ? vals[idx] : 0;
     }
     __syncthreads();
-    if (threadIdx.x < RADIX_BINS) {
-        uint32_t run = 0;
+    for (uint32_t d = threadIdx.x; d < bins; d += RADIX_THREADS) {
+        uint32_t run = tile_off[(uint64_t)d * tiles + blockIdx.x];
 #pragma unroll
         for (int w = 0; w < RADIX_WARPS; ++w) {
-            uint32_t t = whist[w][threadIdx.x];
-            whist[w][threadIdx.x] = run;
+            uint32_t t = whist[w][d];
+            whist[w][d] = run;
             run += t;
         }
     }
@@ -139,8 +148,8 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
         uint64_t idx = base + (uint64_t)r * 32 + lane;
         if (idx < n) {
-            uint32_t d = (k[r] >> shift) & (RADIX_BINS - 1);
-            uint32_t pos = tile_off[(uint64_t)d * tiles + blockIdx.x] + whist[warp][d] + rank[r];
+            uint32_t d = (k[r] >> shift) & mask;
+            uint32_t pos = whist[warp][d] + rank[r];
             keys_out[pos] = k[r];
             vals_out[pos] = v[r];
         }
@@ -167,6 +176,29 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
             e_token[o + i] = t[i];
             e_set[o + i] = s;
             e_pos[o + i] = i;
+        }
+    }
+}
+
+// One warp per set: (token, (set << pos_bits) | position) for the first len
+// tokens, and the token histogram with one atomic per distinct token per warp.
+__global__ void k_emit_packed(CollView c, const uint32_t* __restrict__ off, const uint32_t* __restrict__ len,
+                              uint32_t pos_bits, uint32_t* e_token, uint32_t* e_val, uint32_t* counts) {
+    const int lane = threadIdx.x & 31;
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < c.n; s += warps) {
+        const uint32_t l = len[s], o = off[s];
+        const uint32_t* t = c.tokens + c.meta[s].x;
+        for (uint32_t i0 = 0; i0 < l; i0 += 32) {
+            const uint32_t i = i0 + lane;
+            const bool valid = i < l;
+            const uint32_t tok = valid ? __ldg(t + i) : 0xFFFFFFFFu;
+            if (valid) {
+                e_token[o + i] = tok;
+                e_val[o + i] = (s << pos_bits) | i;
+            }
+            // tokens inside one set are distinct: one atomic per lane
+            if (valid) atomicAdd(&counts[tok], 1u);
         }
     }
 }
@@ -220,33 +252,44 @@ __global__ void k_iota(uint32_t* out, uint64_t n) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (uint32_t)i;
 }
 
-// One warp per set; each lane folds its tokens into W register words, then the
-// warp XOR-reduces them.  Bit b of the signature is word b/64, bit b%64.
+// Eight lanes per set (four sets per warp): each lane folds its tokens into 2W
+// 32-bit register words, the group XOR-reduces them, and the group's lanes
+// store the words (coalesced).  Bit b of the signature is bit b%32 of 32-bit
+// word b/32 (the popcount of a XOR of two signatures does not depend on the
+// bit layout).
 template <int W>
 __global__ void k_bitmaps(CollView c, uint64_t* out) {
-    const int lane = threadIdx.x & 31;
+    constexpr int NW = 2 * W;
+    const int lane = threadIdx.x & 31, g = lane & 7;
     const uint32_t bits = 64u * W;
-    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < c.n; s += warps) {
-        uint64_t w[W];
+    const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
+    uint32_t* out32 = reinterpret_cast<uint32_t*>(out);
+    // every lane iterates the same number of times so the shuffles stay converged
+    const uint32_t rounds = (c.n + groups - 1) / groups;
+    uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    for (uint32_t r = 0; r < rounds; ++r, s += groups) {
+        uint32_t w[NW];
 #pragma unroll
-        for (int i = 0; i < W; ++i) w[i] = 0;
-        const uint32_t* t = c.tokens + c.starts[s];
-        uint32_t l = c.sizes[s];
-        for (uint32_t i = lane; i < l; i += 32) {
-            uint32_t b = t[i] % bits;
+        for (int i = 0; i < NW; ++i) w[i] = 0;
+        const bool live = s < c.n;
+        uint2 m = make_uint2(0, 0);
+        if (live) m = c.meta[s];
+        const uint32_t* t = c.tokens + m.x;
+        for (uint32_t i = g; i < m.y; i += 8) {
+            const uint32_t b = __ldg(t + i) % bits;
+            const uint32_t word = b >> 5, bit = 1u << (b & 31);
 #pragma unroll
-            for (int q = 0; q < W; ++q)
-                if ((b >> 6) == (uint32_t)q) w[q] ^= 1ull << (b & 63);
+            for (int q = 0; q < NW; ++q) w[q] ^= (word == (uint32_t)q) ? bit : 0u;
         }
 #pragma unroll
-        for (int q = 0; q < W; ++q) {
+        for (int q = 0; q < NW; ++q) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) w[q] ^= __shfl_xor_sync(FULL, w[q], o);
+            for (int o = 4; o > 0; o >>= 1) w[q] ^= __shfl_xor_sync(FULL, w[q], o);
         }
-        if (lane == 0) {
+        if (live) {
 #pragma unroll
-            for (int q = 0; q < W; ++q) out[(uint64_t)s * W + q] = w[q];
+            for (int q = 0; q < NW; ++q)
+                if ((q & 7) == g) out32[(uint64_t)s * NW + q] = w[q];
         }
     }
 }
@@ -268,6 +311,11 @@ __global__ void k_validate(CollView c, uint64_t n_tokens, uint32_t* flags) {
         }
         if (f) atomicOr(&flags[0], f);
     }
+}
+
+__global__ void k_meta(CollView c, uint2* meta) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < c.n; i += gridDim.x * blockDim.x)
+        meta[i] = make_uint2(c.starts[i], c.sizes[i]);
 }
 
 unsigned grid_for(uint64_t n, unsigned threads, unsigned cap = 152u * 32u) {
@@ -317,21 +365,24 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
                              int key_bits, uint32_t* scratch, cudaStream_t s) {
     if (n <= 1) return cudaSuccess;
     uint32_t tiles = (uint32_t)((n + RADIX_TILE - 1) / RADIX_TILE);
-    uint64_t counts = (uint64_t)tiles * RADIX_BINS;
-    uint32_t* tile_counts = scratch;
-    uint32_t* scan_tmp = scratch + counts;
-    int passes = (key_bits + 7) / 8;
+    int passes = (key_bits + RADIX_MAX_BITS - 1) / RADIX_MAX_BITS;
     if (passes < 1) passes = 1;
+    const int digit = (key_bits + passes - 1) / passes;
     uint32_t *kin = keys, *vin = vals, *kout = alt_keys, *vout = alt_vals;
     for (int p = 0; p < passes; ++p) {
-        int shift = 8 * p;
+        const int shift = digit * p;
+        const int width = std::min(digit, key_bits - shift);
+        const uint32_t mask = (1u << width) - 1u;
+        const uint64_t counts = (uint64_t)tiles * (mask + 1);
+        uint32_t* tile_counts = scratch;
+        uint32_t* scan_tmp = scratch + counts;
         note_launches(2);
-        k_radix_upsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, n, shift, tile_counts, tiles);
+        k_radix_upsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, n, shift, mask, tile_counts, tiles);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         e = scan_exclusive(tile_counts, tile_counts, counts, scan_tmp, s);
         if (e != cudaSuccess) return e;
-        k_radix_downsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, vin, n, shift, tile_counts, tiles, kout, vout);
+        k_radix_downsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, vin, n, shift, mask, tile_counts, tiles, kout, vout);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         uint32_t* t;
@@ -361,6 +412,15 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
     note_launches();
     k_emit_entries<<<grid_for((uint64_t)(hi - lo) * 32, 256), 256, 0, s>>>(c, lo, hi, entry_off, len, e_token,
                                                                             e_set, e_pos);
+    return cudaGetLastError();
+}
+
+cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
+                                uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s) {
+    if (c.n == 0) return cudaSuccess;
+    note_launches();
+    k_emit_packed<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, entry_off, len, pos_bits, e_token, e_val,
+                                                                     counts);
     return cudaGetLastError();
 }
 
@@ -401,9 +461,16 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
     return cudaGetLastError();
 }
 
+cudaError_t build_meta(CollView c, uint2* meta, cudaStream_t s) {
+    if (c.n == 0) return cudaSuccess;
+    note_launches();
+    k_meta<<<grid_for(c.n, 256), 256, 0, s>>>(c, meta);
+    return cudaGetLastError();
+}
+
 cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s) {
     if (c.n == 0) return cudaSuccess;
-    unsigned g = grid_for((uint64_t)c.n * 32, 256);
+    unsigned g = grid_for((uint64_t)c.n * 8, 256);
     note_launches();
     switch (words) {
     case 1: k_bitmaps<1><<<g, 256, 0, s>>>(c, out); break;

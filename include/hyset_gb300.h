@@ -75,6 +75,10 @@ typedef struct {
     uint32_t collect_stats;    /* 1 = count filter work (hyset_result_stats); costs a few atomics */
     uint32_t probe_begin;      /* probe id range [probe_begin, probe_end) of this call; */
     uint32_t probe_end;        /* 0, 0 = every probe (a shard of a join, e.g. one rank's part) */
+    uint32_t probe_major;      /* technique FGSS: 1 = probe-major kernel (set-id-sorted index, one warp
+                                  per probe batch), 0 = token-major kernel (token groups in shared
+                                  memory).  AUTO always uses probe-major; probe ranges need it */
+    uint32_t fgss_batch;       /* probe-major FGSS: probes per warp batch (1..32); 0 = tuned default */
 } hyset_join_opts;
 
 typedef struct hyset_ctx hyset_ctx;
@@ -142,7 +146,7 @@ double hyset_result_kernel_ms(const hyset_result* r);       /* CUDA-event time o
 const void* hyset_result_device_pairs(const hyset_result* r);
 /* Work counters when collect_stats was set: [0] filter items examined,
  * [1] items reaching verification, [2] candidate tokens of those items,
- * [3] index entries, [4] probe tokens, [5] signature checks, [6] candidate
+ * [3] index entries, [4] probe tokens read, [5] signature checks, [6] candidate
  * tokens read by verification; returns the number written (<= n). */
 uint32_t hyset_result_stats(const hyset_result* r, uint64_t* out, uint32_t n);
 /* Kernel launches the join issued (index build, signatures, filter+verify). */

@@ -12,8 +12,18 @@ from hyset_gb300.handlers import BitmapHandler, DeviceHandler, FgssHandler
 
 pytestmark = pytest.mark.gpu
 
-TECHS = [("fgss", 0, 1), ("fgss", 0, 2), ("fgss", 256, 2), ("bitmap", 64, 1), ("bitmap", 256, 2),
-         ("bitmap", 512, 1), ("direct", 0, 1)]
+TECHS = [
+    dict(technique="fgss"),                                     # token-major (default FGSS kernel)
+    dict(technique="fgss", bitmap=256),
+    dict(technique="fgss", bitmap=64),
+    dict(technique="fgss", probe_major=True, verify_mode=1),    # probe-major kernel, sorted index
+    dict(technique="fgss", probe_major=True, verify_mode=2, bitmap=256),
+    dict(technique="bitmap", bitmap=64, verify_mode=1),
+    dict(technique="bitmap", bitmap=256, verify_mode=2),
+    dict(technique="bitmap", bitmap=512, verify_mode=1),
+    dict(technique="direct", verify_mode=1),
+]
+TECH_IDS = ["-".join(f"{k}{v}" for k, v in t.items()) for t in TECHS]
 
 
 def as_set_checked(pairs):
@@ -23,15 +33,15 @@ def as_set_checked(pairs):
 
 
 @pytest.mark.parametrize("name", GOLDEN_SETS)
-@pytest.mark.parametrize("tech,bits,vmode", TECHS)
-def test_self_join_matches_reference_golden(ctx, name, tech, bits, vmode):
+@pytest.mark.parametrize("kw", TECHS, ids=TECH_IDS)
+def test_self_join_matches_reference_golden(ctx, name, kw):
     tokens, starts, sizes, results = load_golden(name)
     coll = ctx.upload(tokens, sizes, starts)
     for tau, want in results.items():
-        r = ctx.self_join(coll, threshold=tau, technique=tech, bitmap=bits, verify_mode=vmode)
+        r = ctx.self_join(coll, threshold=tau, **kw)
         assert r.count == want["count"], (name, tau)
         assert as_set_checked(r.pairs) == {tuple(p) for p in want["pairs"]}, (name, tau)
-        rc = ctx.self_join(coll, threshold=tau, technique=tech, bitmap=bits, verify_mode=vmode, count_only=True)
+        rc = ctx.self_join(coll, threshold=tau, count_only=True, **kw)
         assert rc.count == want["count"] and rc.pairs is None
 
 
@@ -49,9 +59,12 @@ def test_self_join_matches_oracle_on_workloads(ctx, label, spec, kw, taus, sim):
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
     for tau in taus:
         exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, tau, sim=sim))
-        for tech, bits, vmode in (("fgss", 0, 2), ("fgss", 128, 1), ("bitmap", 256, 2)):
-            r = ctx.self_join(coll, threshold=tau, sim=sim, technique=tech, bitmap=bits, verify_mode=vmode)
-            assert as_set_checked(r.pairs) == exp, (label, sim, tau, tech, bits, vmode)
+        for kw in (dict(technique="fgss"), dict(technique="fgss", bitmap=128),
+                   dict(technique="fgss", probe_major=True, verify_mode=2),
+                   dict(technique="fgss", probe_major=True, bitmap=128, verify_mode=1),
+                   dict(technique="bitmap", bitmap=256, verify_mode=2)):
+            r = ctx.self_join(coll, threshold=tau, sim=sim, **kw)
+            assert as_set_checked(r.pairs) == exp, (label, sim, tau, kw)
 
 
 @pytest.mark.parametrize("sim", ["jaccard", "cosine", "dice"])
@@ -70,9 +83,11 @@ def test_rs_join_matches_brute_force(ctx, sim):
     for tau in (0.6, 0.85):
         exp = oracle.as_set(oracle.brute_rs((R.tokens, R.starts, R.sizes), (s_tok, s_st, s_sizes), tau, sim=sim))
         assert len(exp) > 0
-        for tech, bits in (("fgss", 0), ("fgss", 64), ("bitmap", 128), ("direct", 0)):
-            r = ctx.rs_join(cr, cs, threshold=tau, sim=sim, technique=tech, bitmap=bits)
-            assert as_set_checked(r.pairs) == exp, (sim, tau, tech, bits)
+        for kw in (dict(technique="fgss"), dict(technique="fgss", bitmap=64),
+                   dict(technique="fgss", probe_major=True), dict(technique="bitmap", bitmap=128),
+                   dict(technique="direct")):
+            r = ctx.rs_join(cr, cs, threshold=tau, sim=sim, **kw)
+            assert as_set_checked(r.pairs) == exp, (sim, tau, kw)
 
 
 @pytest.mark.parametrize("tech", ["bitmap", "fgss"])
@@ -136,14 +151,28 @@ def test_edge_cases(ctx):
     one = ctx.upload(np.array([1, 2, 3], np.uint32), np.array([3], np.uint32))
     assert ctx.self_join(one, threshold=0.5).count == 0
     same = ctx.upload(np.tile(np.array([2, 5, 9], np.uint32), 40), np.full(40, 3, np.uint32))
-    for tech in ("fgss", "bitmap", "direct"):
-        r = ctx.self_join(same, threshold=1.0, technique=tech)
-        assert r.count == 40 * 39 // 2
+    for kw in (dict(technique="fgss"), dict(technique="fgss", probe_major=True), dict(technique="bitmap"),
+               dict(technique="direct")):
+        r = ctx.self_join(same, threshold=1.0, **kw)
+        assert r.count == 40 * 39 // 2, kw
     singles = ctx.upload(np.array([1, 1, 2, 3, 3], np.uint32), np.ones(5, np.uint32))
     r = ctx.self_join(singles, threshold=0.9, technique="fgss", sort_pairs=True)
     assert r.pairs.tolist() == [[1, 0], [4, 3]]
     empty = ctx.upload(np.zeros(0, np.uint32), np.zeros(0, np.uint32))
     assert ctx.self_join(empty, threshold=0.8).count == 0
+
+
+def test_probe_ranges_shard_a_join(ctx):
+    c = synth.generate(synth.C2, n_sets=20000)
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.7))
+    got = set()
+    for lo, hi in ((0, 7000), (7000, 15000), (15000, 20000)):
+        r = ctx.self_join(coll, threshold=0.7, technique="fgss", probe_major=True, probe_range=(lo, hi))
+        got |= as_set_checked(r.pairs)
+    assert got == exp
+    with pytest.raises(hs.HysetError):
+        ctx.self_join(coll, threshold=0.7, technique="fgss", probe_range=(0, 10))  # token-major: whole joins
 
 
 def test_invalid_inputs_fail_loudly(ctx):
@@ -161,5 +190,6 @@ def test_invalid_inputs_fail_loudly(ctx):
 def test_pair_buffer_growth(ctx):
     # 300 identical sets -> 44850 pairs with a 16-pair initial buffer
     coll = ctx.upload(np.tile(np.arange(1, 9, dtype=np.uint32), 300), np.full(300, 8, np.uint32))
-    r = ctx.self_join(coll, threshold=0.9, technique="fgss", pair_capacity=16)
-    assert r.count == 300 * 299 // 2 and len(oracle.as_set(r.pairs)) == r.count
+    for pm in (False, True):
+        r = ctx.self_join(coll, threshold=0.9, technique="fgss", pair_capacity=16, probe_major=pm)
+        assert r.count == 300 * 299 // 2 and len(oracle.as_set(r.pairs)) == r.count
