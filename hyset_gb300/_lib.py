@@ -88,6 +88,9 @@ PROTOTYPES = {
     "hyset_verifier_flush": (C.c_int, [C.c_void_p]),
     "hyset_verifier_output": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_void_p)]),
     "hyset_verifier_destroy": (None, [C.c_void_p]),
+    "hyset_verify_candidates_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_uint32] + [C.c_void_p] * 3 +
+                                        [C.c_uint32, C.c_int, C.c_double, C.c_uint32, C.c_void_p, C.c_uint64,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

@@ -193,6 +193,43 @@ hyset_status hyset_verifier_flush(hyset_verifier* v);
 hyset_status hyset_verifier_output(const hyset_verifier* v, uint64_t* count, const hyset_pair** pairs);
 void hyset_verifier_destroy(hyset_verifier* v);
 
+/* ---- verification without allocation ------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory when they verify: a host engine that owns all GPU memory through its
+ * own pool, code running while the stream is being captured into a CUDA graph
+ * (cudaMalloc cannot be captured), or a latency-critical path that cannot
+ * afford cudaMalloc's implicit device synchronisation.
+ *
+ * Verifies explicit candidate lists exactly like hyset_verifier (scenario 1:
+ * one lane per candidate, 2: one warp per candidate): probe d_probes[i] of the
+ * probe collection S owns candidates [d_offsets[i-1] (0 for i = 0),
+ * d_offsets[i]) of the indexed collection R; (probe, candidate) is appended to
+ * d_pairs when |probe ∩ candidate| >= minoverlap(|probe|, |candidate|).  All
+ * inputs and outputs are device pointers; nothing is allocated and the call is
+ * asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream, on
+ * the current device).  *d_count receives the number of result pairs (pairs
+ * past pair_capacity are counted but not written); *d_skipped (optional)
+ * receives the number of candidates skipped because a set is longer than
+ * max_set_size.
+ *
+ * Limits: Jaccard and dice only (HYSET_E_UNSUPPORTED for cosine); sets of at
+ * most HYSET_NOALLOC_MAX_SET_SIZE tokens (larger max_set_size is rejected with
+ * HYSET_E_UNSUPPORTED).  The scratch (counters and the minoverlap table) is one
+ * HYSET_NOALLOC_SCRATCH_BYTES array in device memory that every GPU loading
+ * the library keeps until exit.  All calls share it and it keeps the last
+ * call's contents; each call clears and rewrites it first, so calls that
+ * overlap on the GPU race and must be serialised by the caller.  The first
+ * call on a device looks up the array's device address (with that device
+ * current); make that first call before any stream capture. */
+#define HYSET_NOALLOC_SCRATCH_BYTES 65536
+#define HYSET_NOALLOC_MAX_SET_SIZE 4096
+hyset_status hyset_verify_candidates_noalloc(
+    const uint32_t* d_r_tokens, const uint32_t* d_r_starts, const uint32_t* d_r_sizes,
+    const uint32_t* d_s_tokens, const uint32_t* d_s_starts, const uint32_t* d_s_sizes, uint32_t max_set_size,
+    const uint32_t* d_probes, const uint32_t* d_offsets, const uint32_t* d_candidates, uint32_t n_probes,
+    hyset_sim sim, double threshold, uint32_t scenario, hyset_pair* d_pairs, uint64_t pair_capacity,
+    unsigned long long* d_count, unsigned int* d_skipped, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
