@@ -119,12 +119,15 @@ def ncu_traffic():
         return None
 
 
-def algorithmic_bytes(st, count, words):
-    """Bytes the filter+verify launch must touch: probe tokens, index entries
-    (set id + position + candidate size), signatures checked, candidate tokens
-    consumed by verification, pairs written."""
-    probe_tokens, items, bitmap_checks, cand_tokens = st[4], st[0], st[5], st[6]
-    return 4 * probe_tokens + 12 * items + 8 * words * bitmap_checks + 4 * cand_tokens + 8 * count
+def algorithmic_bytes(st, count, words, n_probes):
+    """Bytes the probe-major filter+verify launch must touch, from its own work
+    counters: per probe its (start, size) record (8); per prefix token the token
+    and its list bounds (12); per index entry in a window the packed entry and
+    the candidate's (start, size) (12); per signature check both signatures
+    (16 W); per token read by verification 4; per result pair 8."""
+    prefix_tokens, items, bitmap_checks, verify_tokens = st[4], st[0], st[5], st[6]
+    return (8 * n_probes + 12 * prefix_tokens + 12 * items + 16 * words * bitmap_checks + 4 * verify_tokens
+            + 8 * count)
 
 
 def cpu_baseline(c, threads, sample_note):
@@ -274,7 +277,7 @@ def run_ours(args, ws, rank, local):
         peak, peak_kind = measured_peaks()
         words = (args.bitmap // 64) if args.bitmap else 0
         st = st_run.stats
-        alg = algorithmic_bytes(st, st_run.count, words)
+        alg = algorithmic_bytes(st, st_run.count, words, p_hi - p_lo)
         kms = statistics.mean(kern_ms)
         achieved = alg / (kms / 1000.0) / 1e9
         traffic = ncu_traffic()

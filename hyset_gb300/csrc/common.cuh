@@ -98,7 +98,7 @@ __device__ __forceinline__ void emit(const Sink& out, bool want, uint32_t first,
 // own_a != NOWN: the pair belongs to the caller only if the smallest common
 // token sits at a[own_a]; otherwise the function returns false at the first
 // common token (another work item owns the pair).
-// *used (optional) receives the number of b tokens read.
+// *used (optional) receives the number of tokens read from a and b.
 __device__ __forceinline__ bool verify_serial(const uint32_t* a, uint32_t na, const uint32_t* __restrict__ b,
                                               uint32_t nb, uint32_t thr, uint32_t own_a, uint32_t* used = nullptr) {
     uint32_t i = 0, k = 0, found = 0, maxa = na, maxb = nb;
@@ -117,7 +117,7 @@ __device__ __forceinline__ bool verify_serial(const uint32_t* a, uint32_t na, co
             ++k; --maxb;
         }
     }
-    if (used) *used = k;
+    if (used) *used = i + k + (ok ? 0u : 1u);
     return ok && found >= thr;
 }
 
@@ -129,14 +129,15 @@ __device__ __forceinline__ bool verify_serial(const uint32_t* a, uint32_t na, co
 // own_b != NOWN: a match at b[k], k < own_b, means a smaller common token
 // exists, so the pair is owned by another work item and false is returned.
 // All 32 lanes must call it with the same arguments.
-// *used (optional) receives the number of b tokens read.
+// *used (optional) receives the number of tokens of b read plus the positions
+// of a searched past (a bound on the tokens of a read).
 __device__ __forceinline__ bool verify_warp(const uint32_t* a, uint32_t na, const uint32_t* __restrict__ b,
                                             uint32_t nb, uint32_t thr, uint32_t own_b, int lane,
                                             uint32_t* used = nullptr) {
     uint32_t found = 0, alo = 0;
     if (used) *used = nb;
     for (uint32_t k0 = 0; k0 < nb; k0 += 32) {
-        if (used) *used = min(nb, k0 + 32);
+        if (used) *used = min(nb, k0 + 32) + alo;
         uint32_t k = k0 + lane;
         bool valid = k < nb;
         uint32_t y = valid ? __ldg(b + k) : 0xFFFFFFFFu;

@@ -269,7 +269,6 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             if constexpr (VMODE == 1) {
                 bool ok = false;
                 if (keep) ok = verify_serial(a, ilp, P.R.tokens + cstart, lc, mo, jp, &used);
-                if (keep) count_stat_lane(P, 4, ilp);
                 emit(P.out, ok, ip, c, lane);
             } else {
                 unsigned m = __ballot_sync(FULL, keep);
@@ -282,7 +281,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                     const uint32_t pl = __shfl_sync(FULL, ilp, src), ps = __shfl_sync(FULL, ipst, src);
                     uint32_t u = 0;
                     const bool ok = verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
-                    if (lane == 0) used += u + pl;
+                    if (lane == 0) used += u;
                     emit(P.out, ok && lane == 0, pp, cc, lane);
                 }
             }

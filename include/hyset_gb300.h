@@ -146,8 +146,9 @@ double hyset_result_kernel_ms(const hyset_result* r);       /* CUDA-event time o
 const void* hyset_result_device_pairs(const hyset_result* r);
 /* Work counters when collect_stats was set: [0] filter items examined,
  * [1] items reaching verification, [2] candidate tokens of those items,
- * [3] index entries, [4] probe tokens read, [5] signature checks, [6] candidate
- * tokens read by verification; returns the number written (<= n). */
+ * [3] index entries, [4] prefix tokens read by the filter, [5] signature
+ * checks, [6] tokens read by verification (both sets); returns the number
+ * written (<= n). */
 uint32_t hyset_result_stats(const hyset_result* r, uint64_t* out, uint32_t n);
 /* Kernel launches the join issued (index build, signatures, filter+verify). */
 uint64_t hyset_result_launches(const hyset_result* r);
