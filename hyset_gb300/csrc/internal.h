@@ -68,6 +68,35 @@ struct Index {
     }
 };
 
+struct Bounds;
+
+// One join of a batch with the buffers it owns (stable across graph replays).
+struct BatchJoin {
+    hyset_coll* R = nullptr;
+    hyset_coll* S = nullptr;
+    bool self = false;
+    hyset_join_opts o{};
+    Bounds* b = nullptr;
+    Index ix;
+    DevBuf bits_r, bits_s, pairs;
+    uint64_t cap = 0;
+    int words = 0;
+    int ktech = 0;
+    hyset_technique tech = HYSET_TECH_AUTO;
+    uint32_t units = 0;
+};
+
+// A captured batch: signature (collections and options), per-join buffers,
+// device descriptors, and the instantiated graph of its device work.
+struct BatchPlan {
+    std::vector<std::string> sig;
+    std::vector<std::unique_ptr<BatchJoin>> joins;
+    std::vector<uint32_t> order;  // joins[order[k]] is descriptor k (heaviest first)
+    DevBuf desc, unit_off, counts, work;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
 }  // namespace hs
 
 struct hyset_ctx {
@@ -80,6 +109,7 @@ struct hyset_ctx {
     // scratch reused across joins
     hs::DevBuf s_len, s_off, s_tok, s_set, s_pos, s_order, s_altk, s_altv, s_counts, s_scan;
     hs::DevBuf s_pairs, s_count, s_work, s_stats;
+    std::unique_ptr<hs::BatchPlan> batch;
 };
 
 struct hyset_coll {

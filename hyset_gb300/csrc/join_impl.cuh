@@ -1,0 +1,306 @@
+// join_impl.cuh — per-probe filter + verify routines shared by the single-join
+// kernel (join.cu) and the batched multi-join kernel (batch.cu).
+#pragma once
+#include "kernels.h"
+
+namespace hs {
+namespace {
+
+#ifndef HS_JOIN_MIN_BLOCKS
+#define HS_JOIN_MIN_BLOCKS 1  // resident blocks per SM the join kernel is compiled for
+#endif
+constexpr int JOIN_THREADS = 256;
+constexpr int JOIN_WARPS = JOIN_THREADS / 32;
+constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per warp
+constexpr uint32_t SHORT_LIST = 8;   // inverted lists this short are windowed without bisection
+
+struct Window {
+    uint32_t lo, hi;
+};
+
+__device__ __forceinline__ Window candidate_window(const JoinParams& P, uint32_t p, uint32_t lp) {
+    Window w;
+    const uint32_t ms = P.B.minsize[lp];
+    w.lo = max(P.first_ge[min(ms, P.R_L + 1)], P.r_lo);
+    if (P.self) {
+        w.hi = min(p, P.r_hi);
+    } else {
+        uint32_t mx = P.B.max_partner[lp];
+        w.hi = min(P.first_ge[min(mx + 1, P.R_L + 1)], P.r_hi);
+    }
+    return w;
+}
+
+__device__ __forceinline__ void count_stat(const JoinParams& P, int k, uint32_t v, int lane) {
+    if (P.stats == nullptr) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+    if (lane == 0 && v) atomicAdd(P.stats + k, (unsigned long long)v);
+}
+
+// Per-lane counter update (divergent-safe; stats runs only).
+__device__ __forceinline__ void count_stat_lane(const JoinParams& P, int k, uint32_t v) {
+    if (P.stats != nullptr && v) atomicAdd(P.stats + k, (unsigned long long)v);
+}
+
+template <int W>
+__device__ __forceinline__ bool bitmap_pass(const JoinParams& P, const uint64_t (&bp)[W > 0 ? W : 1], uint32_t c,
+                                            uint32_t lp, uint32_t lc, uint32_t mo) {
+    if constexpr (W == 0) {
+        return true;
+    } else {
+        uint32_t pop = 0;
+        const uint64_t* bc = P.bits_R + (uint64_t)c * W;
+#pragma unroll
+        for (int q = 0; q < W; ++q) pop += __popcll(bp[q] ^ __ldg(bc + q));
+        return lp + lc - pop >= 2u * mo;
+    }
+}
+
+// Stages the probe's tokens in this warp's shared-memory slot (once per probe,
+// and only when an item survives the filters); long probes stay in HBM/L2.
+__device__ __forceinline__ const uint32_t* stage_probe(const uint32_t* pg, uint32_t lp, uint32_t* sbuf,
+                                                       bool& staged, int lane) {
+    if (lp > MAXP) return pg;
+    if (!staged) {
+        for (uint32_t i = lane; i < lp; i += 32) sbuf[i] = pg[i];
+        __syncwarp();
+        staged = true;
+    }
+    return sbuf;
+}
+
+template <int W>
+__device__ __forceinline__ uint32_t bitmap_xor_pop(const JoinParams& P, const uint64_t (&bp)[W], uint32_t c) {
+    uint32_t pop = 0;
+    const uint64_t* bc = P.bits_R + (uint64_t)c * W;
+#pragma unroll
+    for (int q = 0; q < W; ++q) pop += __popcll(bp[q] ^ __ldg(bc + q));
+    return pop;
+}
+
+// Verifies the warp's surviving items and appends the accepted pairs.
+// own_a / own_b: the item's position in the probe / candidate (ownership test)
+// or NOWN.
+template <int VMODE>
+__device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p, const uint32_t* pg, uint32_t lp,
+                                                uint32_t* sbuf, bool& staged, bool keep, uint32_t cstart,
+                                                uint32_t c, uint32_t lc, uint32_t mo, uint32_t own_a,
+                                                uint32_t own_b, int lane) {
+    unsigned m = __ballot_sync(FULL, keep);
+    uint32_t used = 0;
+    if (m) {
+        const bool before = staged;
+        const uint32_t* a = stage_probe(pg, lp, sbuf, staged, lane);
+        if (!before) count_stat(P, 4, lane == 0 ? lp : 0u, lane);  // probe tokens read for verification
+        if constexpr (VMODE == 1) {
+            bool ok = false;
+            if (keep) ok = verify_serial(a, lp, P.R.tokens + cstart, lc, mo, own_a, &used);
+            emit(P.out, ok, p, c, lane);
+        } else {
+            while (m) {
+                int src = __ffs(m) - 1;
+                m &= m - 1;
+                uint32_t cc = __shfl_sync(FULL, c, src);
+                uint32_t cs = __shfl_sync(FULL, cstart, src);
+                uint32_t ll = __shfl_sync(FULL, lc, src);
+                uint32_t mm = __shfl_sync(FULL, mo, src);
+                uint32_t ob = __shfl_sync(FULL, own_b, src);
+                uint32_t u = 0;
+                bool ok = verify_warp(a, lp, P.R.tokens + cs, ll, mm, ob, lane, &u);
+                if (lane == 0) used += u;
+                emit(P.out, ok && lane == 0, p, cc, lane);
+            }
+        }
+    }
+    count_stat(P, 6, used, lane);
+}
+
+// Lane k of the warp holds the k-th value of a non-decreasing inclusive scan;
+// returns the first lane whose value exceeds q (q < the warp total).
+__device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
+    int jj = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+        uint32_t v = __shfl_sync(FULL, incl, jj + step - 1);
+        if (v <= q) jj += step;
+    }
+    return jj;
+}
+
+// FGSS for a batch of up to 32 probes per warp.  The probes' prefix slots
+// (probe, position) are flattened across lanes, then the index entries their
+// inverted lists contribute; every round trip to memory is shared by the whole
+// batch, so a warp keeps several probes' loads in flight at once.
+template <int VMODE, int W>
+__device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
+    // lane t < k: probe t of the batch (largest sets first)
+    uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0;
+    if ((uint32_t)lane < k) {
+        p = P.p_hi - 1 - (i0 + (uint32_t)lane);
+        const uint2 pm = P.S.meta[p];
+        lp = pm.y;
+        pst = pm.x;
+        if (lp) {
+            const Window w = candidate_window(P, p, lp);
+            lo = w.lo;
+            hi = w.hi;
+            if (lo < hi) mp = P.B.probe_prefix[lp];
+        }
+    }
+    count_stat(P, 4, mp, lane);  // prefix tokens read by the filter
+    const uint32_t mp_incl = warp_incl_scan(mp, lane);
+    const uint32_t slots = __shfl_sync(FULL, mp_incl, 31);
+    for (uint32_t s0 = 0; s0 < slots; s0 += 32) {
+        // ---- slot = (probe t, prefix position j): window of the token's list
+        const uint32_t sl = s0 + lane;
+        const bool sv = sl < slots;
+        const int t = scan_owner(mp_incl, sv ? sl : 0);
+        const uint32_t t_incl = __shfl_sync(FULL, mp_incl, t), t_mp = __shfl_sync(FULL, mp, t);
+        const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp);
+        const uint32_t t_pst = __shfl_sync(FULL, pst, t);
+        const uint32_t t_lo = __shfl_sync(FULL, lo, t), t_hi = __shfl_sync(FULL, hi, t);
+        uint32_t first = 0, cnt = 0;
+        if (sv) {
+            const uint32_t tok = __ldg(P.S.tokens + t_pst + j);
+            if (tok < P.X.universe) {
+                uint32_t b0 = P.X.list_off[tok], b1 = P.X.list_off[tok + 1];
+                if (P.X.sorted) {
+                    const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
+                    const uint32_t len = b1 - b0;
+                    if (len <= SHORT_LIST) {
+                        // one round trip: independent loads instead of dependent bisection
+                        uint32_t v[SHORT_LIST];
+#pragma unroll
+                        for (int q = 0; q < (int)SHORT_LIST; ++q)
+                            v[q] = (uint32_t)q < len ? __ldg(P.X.set + b0 + q) : 0xFFFFFFFFu;
+                        uint32_t nlo = 0, nhi = 0;
+#pragma unroll
+                        for (int q = 0; q < (int)SHORT_LIST; ++q) {
+                            nlo += v[q] < klo;
+                            nhi += v[q] < khi;
+                        }
+                        b1 = b0 + nhi;
+                        b0 = b0 + nlo;
+                    } else {
+                        b0 = lower_bound_u32(P.X.set, b0, b1, klo);
+                        b1 = lower_bound_u32(P.X.set, b0, b1, khi);
+                    }
+                }
+                first = b0;
+                cnt = b1 - b0;
+            }
+        }
+        const uint32_t incl = warp_incl_scan(cnt, lane);
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        for (uint32_t q0 = 0; q0 < total; q0 += 32) {
+            // ---- item = one index entry of one slot
+            const uint32_t q = q0 + lane;
+            bool keep = q < total;
+            const int jj = scan_owner(incl, keep ? q : 0);
+            const uint32_t f_jj = __shfl_sync(FULL, first, jj);
+            const uint32_t i_jj = __shfl_sync(FULL, incl, jj);
+            const uint32_t c_jj = __shfl_sync(FULL, cnt, jj);
+            const uint32_t jp = __shfl_sync(FULL, j, jj);
+            const int it = __shfl_sync(FULL, t, jj);
+            const uint32_t ip = __shfl_sync(FULL, p, it);
+            const uint32_t ilp = __shfl_sync(FULL, lp, it);
+            const uint32_t ipst = __shfl_sync(FULL, pst, it);
+            const uint32_t ilo = __shfl_sync(FULL, lo, it), ihi = __shfl_sync(FULL, hi, it);
+            const uint32_t e = f_jj + ((keep ? q : 0) - (i_jj - c_jj));
+            uint32_t c = 0, pc = 0, lc = 0, mo = 0, cstart = 0, pop = 0;
+            if (keep) {
+                const uint32_t v = P.X.set[e];
+                if (P.X.pos) {
+                    c = v;
+                    pc = P.X.pos[e];
+                } else {
+                    c = v >> P.X.pos_bits;
+                    pc = v & ((1u << P.X.pos_bits) - 1u);
+                }
+                if (!P.X.sorted) keep = c >= ilo && c < ihi;
+            }
+            if (keep) {
+                // the candidate's (start, size) and signature depend only on c: issue together
+                const uint2 cm = P.R.meta[c];
+                if constexpr (W > 0) {
+                    const uint64_t* bs = P.bits_S + (uint64_t)ip * W;
+                    const uint64_t* bc = P.bits_R + (uint64_t)c * W;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) pop += __popcll(__ldg(bs + w) ^ __ldg(bc + w));
+                }
+                cstart = cm.x;
+                lc = cm.y;
+                const uint32_t big = max(ilp, lc), small = min(ilp, lc);
+                mo = minoverlap(P.B, big, small);
+                keep = 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
+            }
+            count_stat(P, 0, q < total ? 1u : 0u, lane);
+            count_stat(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
+            if constexpr (W > 0) keep = keep && ilp + lc - pop >= 2u * mo;
+            count_stat(P, 1, keep ? 1u : 0u, lane);
+            count_stat(P, 2, keep ? lc : 0u, lane);
+            // ---- verification: the probe is read from HBM/L2 (it was just touched)
+            uint32_t used = 0;
+            const uint32_t* a = P.S.tokens + ipst;
+            if constexpr (VMODE == 1) {
+                bool ok = false;
+                if (keep) ok = verify_serial(a, ilp, P.R.tokens + cstart, lc, mo, jp, &used);
+                emit(P.out, ok, ip, c, lane);
+            } else {
+                unsigned m = __ballot_sync(FULL, keep);
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1;
+                    const uint32_t cc = __shfl_sync(FULL, c, src), cs = __shfl_sync(FULL, cstart, src);
+                    const uint32_t ll = __shfl_sync(FULL, lc, src), mm = __shfl_sync(FULL, mo, src);
+                    const uint32_t ob = __shfl_sync(FULL, pc, src), pp = __shfl_sync(FULL, ip, src);
+                    const uint32_t pl = __shfl_sync(FULL, ilp, src), ps = __shfl_sync(FULL, ipst, src);
+                    uint32_t u = 0;
+                    const bool ok = verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
+                    if (lane == 0) used += u;
+                    emit(P.out, ok && lane == 0, pp, cc, lane);
+                }
+            }
+            count_stat(P, 6, used, lane);
+        }
+    }
+}
+
+template <int VMODE, int W>
+__device__ void enum_probe(const JoinParams& P, uint32_t p, uint32_t* sbuf, int lane) {
+    const uint2 pm = P.S.meta[p];
+    const uint32_t lp = pm.y;
+    if (lp == 0) return;
+    const Window win = candidate_window(P, p, lp);
+    if (win.lo >= win.hi) return;
+    const uint32_t* pg = P.S.tokens + pm.x;
+    bool staged = false;
+    uint64_t bp[W > 0 ? W : 1];
+    if constexpr (W > 0) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) bp[q] = __ldg(P.bits_S + (uint64_t)p * W + q);
+    }
+    for (uint32_t c0 = win.lo; c0 < win.hi; c0 += 32) {
+        const uint32_t c = c0 + lane;
+        bool keep = c < win.hi;
+        uint32_t lc = 0, mo = 0, cstart = 0;
+        if (keep) {
+            const uint2 cm = P.R.meta[c];
+            cstart = cm.x;
+            lc = cm.y;
+            const uint32_t big = max(lp, lc), small = min(lp, lc);
+            mo = minoverlap(P.B, big, small);
+            keep = bitmap_pass<W>(P, bp, c, lp, lc, mo);
+        }
+        count_stat(P, 0, c < win.hi ? 1u : 0u, lane);
+        count_stat(P, 5, (W > 0 && c < win.hi) ? 1u : 0u, lane);
+        count_stat(P, 1, keep ? 1u : 0u, lane);
+        count_stat(P, 2, keep ? lc : 0u, lane);
+        verify_and_emit<VMODE>(P, p, pg, lp, sbuf, staged, keep, cstart, c, lc, mo, NOWN, NOWN, lane);
+    }
+    __syncwarp();
+}
+
+}  // namespace
+}  // namespace hs

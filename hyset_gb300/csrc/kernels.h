@@ -133,6 +133,19 @@ struct TokenJoinParams {
 // One persistent launch; warps steal token groups, largest token ids first.
 cudaError_t launch_join_tm(const TokenJoinParams& P, int sm_count, cudaStream_t s);
 
+// ---- batch.cu ----------------------------------------------------------------
+// One join of a batch: its parameters plus how its probes split into units.
+struct BatchDesc {
+    JoinParams P;
+    uint32_t tech;         // TECH_FGSS, TECH_BITMAP or TECH_DIRECT
+    uint32_t words;        // signature words (0: none)
+    uint32_t unit_probes;  // probes per work unit
+    uint32_t pad;
+};
+// unit_off[j] = first unit of join j, unit_off[n_joins] = all units; work zeroed.
+cudaError_t launch_batch_join(const BatchDesc* d_desc, const uint32_t* d_unit_off, uint32_t n_joins,
+                              unsigned int* d_work, int sm_count, cudaStream_t s);
+
 // Explicit candidate lists (hybrid::device_handler): probes[i] owns candidates
 // [i ? offsets[i-1] : 0, offsets[i]).
 cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const uint32_t* probes,

@@ -193,3 +193,48 @@ def test_pair_buffer_growth(ctx):
     for pm in (False, True):
         r = ctx.self_join(coll, threshold=0.9, technique="fgss", pair_capacity=16, probe_major=pm)
         assert r.count == 300 * 299 // 2 and len(oracle.as_set(r.pairs)) == r.count
+
+
+def _mixed_batch(ctx, seed=5, n_joins=18):
+    """Independent joins of uneven sizes, similarity functions, thresholds and
+    techniques (self-joins and R-S joins)."""
+    rng = np.random.default_rng(seed)
+    joins, colls = [], []
+    sims = ["jaccard", "cosine", "dice"]
+    for j in range(n_joins):
+        nr = int(rng.integers(300, 6000))
+        mean = float(np.exp(rng.uniform(np.log(8), np.log(120))))
+        spec = dict(n_sets=nr, universe=int(rng.integers(3000, 40000)), zipf_s=float(rng.uniform(0.7, 1.3)),
+                    size_dist=synth.LOGNORMAL, size_a=float(np.log(mean)), size_b=0.5, size_min=2,
+                    size_max=600, dup_frac=0.05, dup_edit_lo=0.0, dup_edit_hi=0.2, seed=1000 + j)
+        R = synth.generate(synth.C2, **spec)
+        cr = ctx.upload(R.tokens, R.sizes, R.starts)
+        colls.append(cr)
+        kw = dict(threshold=float(rng.uniform(0.5, 0.95)), sim=sims[j % 3])
+        if j % 4 == 1:
+            kw.update(technique="bitmap", bitmap=128)
+        elif j % 4 == 2:
+            kw.update(technique="direct") if nr < 1500 else kw.update(technique="fgss", probe_major=True)
+        if j % 2 == 0:
+            joins.append((cr, None, kw))  # self-join
+        else:
+            spec2 = dict(spec, n_sets=int(rng.integers(300, 4000)), seed=2000 + j)
+            S = synth.generate(synth.C2, **spec2)
+            cs = ctx.upload(S.tokens, S.sizes, S.starts)
+            colls.append(cs)
+            joins.append((cr, cs, kw))
+    return joins, colls
+
+
+def test_batch_join_matches_joins_run_one_at_a_time(ctx):
+    joins, colls = _mixed_batch(ctx)
+    single = []
+    for R, S, kw in joins:
+        r = ctx.self_join(R, **kw) if S is None else ctx.rs_join(R, S, **kw)
+        single.append(as_set_checked(r.pairs))
+    assert sum(len(x) for x in single) > 0
+    for attempt in range(2):  # first call captures the batch graph, the second replays it
+        res = ctx.batch_join(joins)
+        for k, (r, exp) in enumerate(zip(res, single)):
+            assert r.count == len(exp), (attempt, k, joins[k][2])
+            assert as_set_checked(r.pairs) == exp, (attempt, k, joins[k][2])
