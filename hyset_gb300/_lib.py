@@ -29,6 +29,8 @@ STATUS_NAMES = {0: "OK", 1: "E_INVALID", 2: "E_CUDA", 3: "E_NOMEM", 4: "E_OVERFL
 SIM = {"jaccard": 0, "cosine": 1, "dice": 2}
 TECH = {"auto": 0, "bitmap": 1, "fgss": 2, "direct": 3}
 TECH_NAMES = {v: k for k, v in TECH.items()}
+SELECTOR_NAMES = {-1: "explicit", 0: "rules", 1: "cost_model", 2: "mlp"}
+N_FEATURES, MLP_PARAMS, COST_TERMS = 12, 5187, 9
 
 
 class JoinOpts(C.Structure):
@@ -88,6 +90,13 @@ PROTOTYPES = {
     "hyset_verifier_flush": (C.c_int, [C.c_void_p]),
     "hyset_verifier_output": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_void_p)]),
     "hyset_verifier_destroy": (None, [C.c_void_p]),
+    "hyset_join_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(JoinOpts),
+                                      C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "hyset_mlp_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "hyset_mlp_grad": (C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_void_p, C.c_void_p]),
+    "hyset_mlp_train": (C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_void_p]),
+    "hyset_selector_set": (C.c_int, [C.c_void_p] * 5),
+    "hyset_result_selector": (C.c_int, [C.c_void_p]),
     "hyset_verify_candidates_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_uint32] + [C.c_void_p] * 3 +
                                         [C.c_uint32, C.c_int, C.c_double, C.c_uint32, C.c_void_p, C.c_uint64,
                                          C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -15,7 +15,8 @@ from typing import Optional, Sequence
 import numpy as np
 
 from . import _lib
-from ._lib import SIM, TECH, TECH_NAMES, JoinDesc, JoinOpts, U32P, check, load
+from ._lib import (COST_TERMS, MLP_PARAMS, N_FEATURES, SELECTOR_NAMES, SIM, TECH, TECH_NAMES, JoinDesc, JoinOpts,
+                   U32P, check, load)
 
 
 @dataclass
@@ -28,6 +29,7 @@ class JoinResult:
     stats: Optional[list] = None
     device_pairs: int = 0  # device address when device_pairs was requested
     launches: int = 0      # kernel launches the join issued
+    selector: str = "explicit"  # which selector chose the technique
 
 
 def make_opts(threshold: float = 0.8, sim: str = "jaccard", technique: str = "auto", bitmap: int = 0,
@@ -57,7 +59,7 @@ def _take_result(lib, r) -> JoinResult:
         return JoinResult(int(n), pairs, TECH_NAMES.get(lib.hyset_result_technique(r), "?"),
                           float(lib.hyset_result_device_ms(r)), float(lib.hyset_result_kernel_ms(r)),
                           [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0),
-                          int(lib.hyset_result_launches(r)))
+                          int(lib.hyset_result_launches(r)), SELECTOR_NAMES.get(lib.hyset_result_selector(r), "?"))
     finally:
         lib.hyset_result_free(r)
 
@@ -84,12 +86,22 @@ class DeviceCollection:
             pass
 
 
+def _fptr(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
 class Context:
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, selector: bool = True):
+        """selector: install the shipped technique selector (learned network
+        and analytic cost model) for technique AUTO, if it is present."""
         self._lib = load()
         h = C.c_void_p()
         check(self._lib.hyset_create(device, C.byref(h)))
         self.handle = h
+        self.selector_info = None
+        if selector:
+            from . import selector as _sel
+            self.selector_info = _sel.install_shipped(self)
 
     def close(self):
         if self.handle:
@@ -145,6 +157,57 @@ class Context:
         check(self._lib.hyset_rs_join(self.handle, indexed.handle, probe.handle, C.byref(o), C.byref(r)),
               self.handle)
         return _take_result(self._lib, r)
+
+    # ---- selector
+    def features(self, indexed: DeviceCollection, probe: Optional[DeviceCollection] = None, **kw):
+        """(features[12], base_stats[8]) of a join, computed on the GPU."""
+        o = make_opts(**kw)
+        f = np.zeros(N_FEATURES, np.float32)
+        b = np.zeros(8, np.float64)
+        check(self._lib.hyset_join_features(self.handle, indexed.handle, probe.handle if probe else None,
+                                            C.byref(o), f.ctypes.data_as(C.POINTER(C.c_float)),
+                                            b.ctypes.data_as(C.POINTER(C.c_double))), self.handle)
+        return f, b
+
+    def mlp_forward(self, params: np.ndarray, x: np.ndarray) -> np.ndarray:
+        params = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, N_FEATURES)
+        y = np.zeros((x.shape[0], 3), np.float32)
+        check(self._lib.hyset_mlp_forward(self.handle, _fptr(params), _fptr(x), x.shape[0], _fptr(y)), self.handle)
+        return y
+
+    def mlp_grad(self, params, x, t, mask):
+        params = np.ascontiguousarray(params, np.float32)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, N_FEATURES)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, 3)
+        mask = np.ascontiguousarray(mask, np.float32).reshape(-1, 3)
+        g = np.zeros(MLP_PARAMS, np.float32)
+        loss = np.zeros(1, np.float32)
+        check(self._lib.hyset_mlp_grad(self.handle, _fptr(params), _fptr(x), _fptr(t), _fptr(mask), x.shape[0],
+                                       _fptr(g), _fptr(loss)), self.handle)
+        return g, float(loss[0])
+
+    def mlp_train(self, params, x, t, mask, steps, lr=1e-3, weight_decay=0.0):
+        p = np.array(params, dtype=np.float32, copy=True)
+        x = np.ascontiguousarray(x, np.float32).reshape(-1, N_FEATURES)
+        t = np.ascontiguousarray(t, np.float32).reshape(-1, 3)
+        mask = np.ascontiguousarray(mask, np.float32).reshape(-1, 3)
+        trace = np.zeros(max(int(steps), 1), np.float32)
+        check(self._lib.hyset_mlp_train(self.handle, _fptr(p), _fptr(x), _fptr(t), _fptr(mask), x.shape[0],
+                                        int(steps), float(lr), float(weight_decay), _fptr(trace)), self.handle)
+        return p, trace[:int(steps)]
+
+    def selector_set(self, params=None, mean=None, scale=None, cost=None):
+        args = []
+        keep = []
+        for a, dt in ((params, np.float32), (mean, np.float32), (scale, np.float32), (cost, np.float64)):
+            if a is None:
+                args.append(None)
+            else:
+                arr = np.ascontiguousarray(a, dt)
+                keep.append(arr)
+                args.append(_fptr(arr))
+        check(self._lib.hyset_selector_set(self.handle, *args), self.handle)
 
     def batch_join(self, joins: Sequence[tuple]) -> list:
         """joins: (indexed, probe_or_None, opts_kwargs) triples."""

@@ -321,11 +321,13 @@ struct Tuned {
     int vmode;
 };
 
-Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o) {
+Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o,
+           hyset_technique selected = HYSET_TECH_AUTO) {
     Tuned t{};
     const double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
     const uint64_t pairs_window = (uint64_t)R->n * (uint64_t)S->n;
     t.tech = o->technique;
+    if (t.tech == HYSET_TECH_AUTO) t.tech = selected;
     if (t.tech == HYSET_TECH_AUTO) t.tech = (pairs_window <= 4000000ull) ? HYSET_TECH_BITMAP : HYSET_TECH_FGSS;
     // explicit FGSS defaults to the token-major kernel; AUTO to probe-major
     t.probe_major = (o->technique == HYSET_TECH_FGSS && !o->probe_major) ? 0 : 1;
@@ -399,13 +401,163 @@ hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const h
     return HYSET_OK;
 }
 
+// ---------------------------------------------------------------- selector
+
+// Length-compatible candidate pairs (the enumeration techniques' work) from the
+// size histograms: per probe size l, the indexed sets of size [minsize(l), upper(l)].
+double window_pairs(const hyset_coll* R, const std::vector<uint64_t>& probe_hist, const Bounds* b, bool self) {
+    std::vector<uint64_t> cum(R->size_hist.size() + 1, 0);
+    for (size_t l = 0; l < R->size_hist.size(); ++l) cum[l + 1] = cum[l] + R->size_hist[l];
+    auto count_le = [&](uint64_t l) -> uint64_t { return cum[std::min<uint64_t>(l + 1, cum.size() - 1)]; };
+    double pairs = 0;
+    for (size_t l = 0; l < probe_hist.size(); ++l) {
+        if (!probe_hist[l]) continue;
+        const uint64_t lo = b->minsize[l];
+        const uint64_t hi = self ? l : b->max_partner[l];
+        if (hi < lo) continue;
+        double w = (double)(count_le(hi) - (lo ? count_le(lo - 1) : 0));
+        if (self) w -= 0.5 * (double)(probe_hist[l] + 1);  // only smaller ids among equal sizes
+        pairs += (double)probe_hist[l] * std::max(0.0, w);
+    }
+    return pairs;
+}
+
+hyset_status compute_features(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, float* f,
+                              double* base) {
+    ST(check_opts(ctx, o));
+    const bool self = R == S;
+    const uint32_t L = std::max(R->max_size, S->max_size);
+    Bounds* b = nullptr;
+    ST(get_bounds(ctx, o->sim, o->threshold, L, self ? 0 : 1, &b));
+    if (o->probe_end > S->n || o->probe_begin > o->probe_end)
+        return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
+    const uint32_t p_lo = o->probe_end ? o->probe_begin : 0, p_hi = o->probe_end ? o->probe_end : S->n;
+    const uint32_t np = p_hi - p_lo;
+    const uint32_t U = std::max(R->universe, S->universe);
+    cudaStream_t s = ctx->stream;
+    CK(ctx->d_moments.ensure(64, s));
+    CK(ctx->d_hist.ensure(((size_t)U + 1) * 4, s));
+    unsigned long long* mom = ctx->d_moments.as<unsigned long long>();
+    CK(cudaMemsetAsync(mom, 0, 64, s));
+    CK(cudaMemsetAsync(ctx->d_hist.p, 0, ((size_t)U + 1) * 4, s));
+    CollView part = S->view();  // the probe partition as a collection of its own
+    part.sizes += p_lo;
+    part.starts += p_lo;
+    part.meta += p_lo;
+    part.n = np;
+    if (np) {
+        CK(moments_u32(S->d_sizes + p_lo, np, mom, s));
+        CK(group_count(part, b->view.probe_prefix, ctx->d_hist.as<uint32_t>(), s));
+        CK(moments_u32(ctx->d_hist.as<uint32_t>(), U, mom + 4, s));
+    }
+    unsigned long long m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    CK(cudaMemcpyAsync(m, mom, 64, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    std::vector<uint64_t> ph(S->max_size + 1, 0);
+    if (np == S->n) ph = S->size_hist;
+    else
+        for (uint32_t i = p_lo; i < p_hi; ++i) ph[S->h_sizes[i]]++;
+    double pre = 0;
+    for (size_t l = 0; l < ph.size(); ++l) pre += (double)ph[l] * b->probe_prefix[l];
+    const double n_d = np ? (double)np : 1.0;
+    const double mean = (double)m[0] / n_d;
+    const double var = std::max(0.0, (double)m[1] / n_d - mean * mean);
+    const double tmean = (double)m[4] / (double)U;
+    const double tvar = std::max(0.0, (double)m[5] / (double)U - tmean * tmean);  // over the whole universe
+    const double index_entries = (double)prefix_entries(R, b->index_prefix);
+    const double pairs = window_pairs(R, ph, b, self);
+    const double v[MLP_IN] = {std::log2(1.0 + np), mean, std::sqrt(var), std::log2(1.0 + (double)m[2]),
+                              std::log2(1.0 + U), o->threshold, (double)o->sim / 2.0, pre / n_d,
+                              std::log2(1.0 + index_entries), std::log2(1.0 + std::sqrt(tvar)),
+                              std::log2(1.0 + (double)m[6]), std::log2(1.0 + pairs)};
+    for (int k = 0; k < MLP_IN; ++k) f[k] = (float)v[k];
+    if (base) {
+        base[0] = std::sqrt(var);
+        base[1] = mean;
+        base[2] = std::sqrt(tvar);
+        base[3] = np;
+        base[4] = U;
+        base[5] = index_entries;
+        base[6] = pairs;
+        base[7] = pre / n_d;
+    }
+    return HYSET_OK;
+}
+
+const hyset_technique kSelectable[3] = {HYSET_TECH_BITMAP, HYSET_TECH_FGSS, HYSET_TECH_DIRECT};
+
+// cost.hpp:28-58 / statistics.hpp:150-160: |c . (1, std, avg, tokfreq, n, n^2, U, index, bitmap)|
+double analytic_cost(const double* c, const double* base, double bitmap_bits) {
+    const double x[9] = {1.0, base[0], base[1], base[2], base[3], base[3] * base[3], base[4], base[5], bitmap_bits};
+    double s = 0;
+    for (int k = 0; k < 9; ++k) s += c[k] * x[k];
+    return std::fabs(s);
+}
+
+// The technique AUTO runs: the learned network's argmin of predicted log-time,
+// else the analytic cost model's argmin, else fixed rules (AUTO passed on).
+// Decided once per (collections, similarity, threshold, probe range) and reused.
+hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o,
+                              hyset_technique* out, int* selector) {
+    *out = HYSET_TECH_AUTO;
+    *selector = 0;
+    if (o->technique != HYSET_TECH_AUTO) {
+        *selector = -1;
+        return HYSET_OK;
+    }
+    if (!ctx->has_mlp && !ctx->has_cost) return HYSET_OK;
+    char key[128];
+    std::snprintf(key, sizeof key, "%p/%p/%d/%.17g/%u/%u", (void*)R, (void*)S, (int)o->sim, o->threshold,
+                  o->probe_begin, o->probe_end);
+    auto it = ctx->select_cache.find(key);
+    if (it != ctx->select_cache.end()) {
+        *out = it->second.first;
+        *selector = it->second.second;
+        return HYSET_OK;
+    }
+    float f[MLP_IN];
+    double base[8];
+    ST(compute_features(ctx, R, S, o, f, base));
+    if (ctx->has_mlp) {
+        float x[MLP_IN], y[MLP_OUT] = {0, 0, 0};
+        for (int k = 0; k < MLP_IN; ++k) x[k] = (f[k] - ctx->feat_mean[k]) / ctx->feat_scale[k];
+        cudaStream_t s = ctx->stream;
+        CK(ctx->d_feat.ensure(256, s));
+        float* dx = ctx->d_feat.as<float>();
+        CK(cudaMemcpyAsync(dx, x, sizeof x, cudaMemcpyHostToDevice, s));
+        CK(mlp_forward(ctx->d_mlp.as<float>(), dx, 1, dx + 32, ctx->sm_count, s));
+        CK(cudaMemcpyAsync(y, dx + 32, sizeof y, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        int best = 0;
+        for (int k = 1; k < MLP_OUT; ++k)
+            if (y[k] < y[best]) best = k;
+        *out = kSelectable[best];
+        *selector = 2;
+    } else {
+        const double avg = base[1];
+        const double bits = avg <= 48.0 ? 128.0 : 256.0;
+        int best = 0;
+        double bc = 0;
+        for (int k = 0; k < 3; ++k) {
+            const double c = analytic_cost(ctx->cost[k], base, k == 0 ? bits : 0.0);
+            if (k == 0 || c < bc) { bc = c; best = k; }
+        }
+        *out = kSelectable[best];
+        *selector = 1;
+    }
+    ctx->select_cache[key] = {*out, *selector};
+    return HYSET_OK;
+}
+
 hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, hyset_result* res) {
     ST(check_opts(ctx, o));
     const bool self = (S == R);
     const uint32_t L = std::max(R->max_size, S->max_size);
     Bounds* b = nullptr;
     ST(get_bounds(ctx, o->sim, o->threshold, L, self ? 0 : 1, &b));
-    const Tuned tn = tune(R, S, o);
+    hyset_technique selected = HYSET_TECH_AUTO;
+    ST(select_technique(ctx, R, S, o, &selected, &res->selector));
+    const Tuned tn = tune(R, S, o, selected);
     const hyset_technique tech = tn.tech;
     const int vmode = tn.vmode;
     res->technique = tech;
@@ -586,7 +738,10 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
             return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
         const uint32_t L = std::max(R->max_size, S->max_size);
         ST(get_bounds(ctx, o->sim, o->threshold, L, bj->self ? 0 : 1, &bj->b));
-        Tuned tn = tune(R, S, o);
+        hyset_technique selected = HYSET_TECH_AUTO;
+        int selector = 0;
+        ST(select_technique(ctx, R, S, o, &selected, &selector));
+        Tuned tn = tune(R, S, o, selected);
         tn.probe_major = 1;  // the batched kernel runs the probe-major form
         bj->tech = tn.tech;
         bj->ktech = tn.tech == HYSET_TECH_FGSS ? TECH_FGSS : (tn.tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
@@ -755,7 +910,8 @@ void hyset_destroy(hyset_ctx* ctx) {
         for (auto& kv : ctx->bounds) kv.second->dev.release(s);
         DevBuf* bufs[] = {&ctx->s_len, &ctx->s_off, &ctx->s_tok, &ctx->s_set, &ctx->s_pos, &ctx->s_order,
                           &ctx->s_altk, &ctx->s_altv, &ctx->s_counts, &ctx->s_scan,
-                          &ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats};
+                          &ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats,
+                          &ctx->d_mlp, &ctx->d_feat, &ctx->d_moments, &ctx->d_hist};
         for (DevBuf* b : bufs) b->release(s);
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
@@ -943,6 +1099,146 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
     }
     return HYSET_OK;
 }
+
+hyset_status hyset_join_features(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                                 const hyset_join_opts* opts, float* features, double* base_stats) {
+    if (!ctx || !indexed || !opts || !features) return fail(ctx, HYSET_E_INVALID, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    hyset_coll* R = const_cast<hyset_coll*>(indexed);
+    hyset_coll* S = const_cast<hyset_coll*>(probe ? probe : indexed);
+    return compute_features(ctx, R, S, opts, features, base_stats);
+}
+
+namespace {
+struct MlpBufs {
+    DevBuf w, x, t, m, y, g, mom, vel, loss;
+};
+hyset_status mlp_upload(hyset_ctx* ctx, MlpBufs& B, const float* params, const float* x, const float* t,
+                        const float* mask, uint32_t n) {
+    cudaStream_t s = ctx->stream;
+    CK(B.w.ensure(MLP_PARAMS * 4, s));
+    CK(B.x.ensure((size_t)n * MLP_IN * 4 + 4, s));
+    CK(B.y.ensure((size_t)n * MLP_OUT * 4 + 4, s));
+    CK(cudaMemcpyAsync(B.w.p, params, MLP_PARAMS * 4, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(B.x.p, x, (size_t)n * MLP_IN * 4, cudaMemcpyHostToDevice, s));
+    if (t) {
+        CK(B.t.ensure((size_t)n * MLP_OUT * 4 + 4, s));
+        CK(B.m.ensure((size_t)n * MLP_OUT * 4 + 4, s));
+        CK(cudaMemcpyAsync(B.t.p, t, (size_t)n * MLP_OUT * 4, cudaMemcpyHostToDevice, s));
+        CK(cudaMemcpyAsync(B.m.p, mask, (size_t)n * MLP_OUT * 4, cudaMemcpyHostToDevice, s));
+    }
+    return HYSET_OK;
+}
+void mlp_release(hyset_ctx* ctx, MlpBufs& B) {
+    DevBuf* bufs[] = {&B.w, &B.x, &B.t, &B.m, &B.y, &B.g, &B.mom, &B.vel, &B.loss};
+    for (DevBuf* d : bufs) d->release(ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+}
+float mask_sum(const float* mask, uint32_t n) {
+    double d = 0;
+    for (size_t i = 0; i < (size_t)n * MLP_OUT; ++i) d += mask[i];
+    return (float)d;
+}
+}  // namespace
+
+hyset_status hyset_mlp_forward(hyset_ctx* ctx, const float* params, const float* x, uint32_t n, float* y) {
+    if (!ctx || !params || (n && (!x || !y))) return fail(ctx, HYSET_E_INVALID, "null argument");
+    if (n == 0) return HYSET_OK;
+    CK(cudaSetDevice(ctx->device));
+    MlpBufs B;
+    hyset_status st = mlp_upload(ctx, B, params, x, nullptr, nullptr, n);
+    if (st == HYSET_OK) {
+        cudaError_t e = mlp_forward(B.w.as<float>(), B.x.as<float>(), (int)n, B.y.as<float>(), ctx->sm_count,
+                                    ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(y, B.y.p, (size_t)n * MLP_OUT * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = fail(ctx, HYSET_E_CUDA, "mlp forward", e);
+    }
+    mlp_release(ctx, B);
+    return st;
+}
+
+hyset_status hyset_mlp_grad(hyset_ctx* ctx, const float* params, const float* x, const float* t, const float* mask,
+                            uint32_t n, float* grad, float* loss) {
+    if (!ctx || !params || !x || !t || !mask || !grad || !loss || n == 0)
+        return fail(ctx, HYSET_E_INVALID, "null argument");
+    const float denom = mask_sum(mask, n);
+    if (!(denom > 0.f)) return fail(ctx, HYSET_E_INVALID, "mask selects no output");
+    CK(cudaSetDevice(ctx->device));
+    MlpBufs B;
+    hyset_status st = mlp_upload(ctx, B, params, x, t, mask, n);
+    cudaError_t e = cudaSuccess;
+    if (st == HYSET_OK) {
+        e = B.g.ensure(MLP_PARAMS * 4, ctx->stream);
+        if (e == cudaSuccess) e = B.loss.ensure(16, ctx->stream);
+        if (e == cudaSuccess)
+            e = mlp_grad(B.w.as<float>(), B.x.as<float>(), B.t.as<float>(), B.m.as<float>(), (int)n, denom,
+                         B.g.as<float>(), B.loss.as<float>(), ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(grad, B.g.p, MLP_PARAMS * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(loss, B.loss.p, 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) st = fail(ctx, HYSET_E_CUDA, "mlp gradient", e);
+    }
+    mlp_release(ctx, B);
+    return st;
+}
+
+hyset_status hyset_mlp_train(hyset_ctx* ctx, float* params, const float* x, const float* t, const float* mask,
+                             uint32_t n, uint32_t steps, float lr, float weight_decay, float* loss_trace) {
+    if (!ctx || !params || !x || !t || !mask || n == 0) return fail(ctx, HYSET_E_INVALID, "null argument");
+    const float denom = mask_sum(mask, n);
+    if (!(denom > 0.f)) return fail(ctx, HYSET_E_INVALID, "mask selects no output");
+    CK(cudaSetDevice(ctx->device));
+    MlpBufs B;
+    hyset_status st = mlp_upload(ctx, B, params, x, t, mask, n);
+    cudaError_t e = cudaSuccess;
+    cudaStream_t s = ctx->stream;
+    if (st == HYSET_OK) {
+        e = B.g.ensure(MLP_PARAMS * 4, s);
+        if (e == cudaSuccess) e = B.mom.ensure(MLP_PARAMS * 4, s);
+        if (e == cudaSuccess) e = B.vel.ensure(MLP_PARAMS * 4, s);
+        if (e == cudaSuccess) e = B.loss.ensure((size_t)steps * 4 + 4, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.mom.p, 0, MLP_PARAMS * 4, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(B.vel.p, 0, MLP_PARAMS * 4, s);
+        if (e == cudaSuccess)
+            e = mlp_train(B.w.as<float>(), B.mom.as<float>(), B.vel.as<float>(), B.g.as<float>(), B.x.as<float>(),
+                          B.t.as<float>(), B.m.as<float>(), (int)n, denom, (int)steps, lr, weight_decay,
+                          B.loss.as<float>(), s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(params, B.w.p, MLP_PARAMS * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess && loss_trace && steps)
+            e = cudaMemcpyAsync(loss_trace, B.loss.p, (size_t)steps * 4, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) st = fail(ctx, HYSET_E_CUDA, "mlp training", e);
+    }
+    mlp_release(ctx, B);
+    return st;
+}
+
+hyset_status hyset_selector_set(hyset_ctx* ctx, const float* params, const float* feature_mean,
+                                const float* feature_scale, const double* cost_coefficients) {
+    if (!ctx) return HYSET_E_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    ctx->select_cache.clear();
+    ctx->has_mlp = false;
+    if (params) {
+        if (!feature_mean || !feature_scale) return fail(ctx, HYSET_E_INVALID, "normalisation missing");
+        for (int k = 0; k < MLP_IN; ++k)
+            if (!(feature_scale[k] > 0.f)) return fail(ctx, HYSET_E_INVALID, "feature scale must be > 0");
+        ctx->mlp_params.assign(params, params + MLP_PARAMS);
+        std::memcpy(ctx->feat_mean, feature_mean, sizeof ctx->feat_mean);
+        std::memcpy(ctx->feat_scale, feature_scale, sizeof ctx->feat_scale);
+        CK(ctx->d_mlp.ensure(MLP_PARAMS * 4, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_mlp.p, ctx->mlp_params.data(), MLP_PARAMS * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        ctx->has_mlp = true;
+    }
+    ctx->has_cost = cost_coefficients != nullptr;
+    if (cost_coefficients) std::memcpy(ctx->cost, cost_coefficients, sizeof ctx->cost);
+    return HYSET_OK;
+}
+
+int hyset_result_selector(const hyset_result* r) { return r ? r->selector : -1; }
 
 uint64_t hyset_result_count(const hyset_result* r) { return r ? r->count : 0; }
 const hyset_pair* hyset_result_pairs(const hyset_result* r) {

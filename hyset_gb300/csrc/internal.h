@@ -110,6 +110,13 @@ struct hyset_ctx {
     hs::DevBuf s_len, s_off, s_tok, s_set, s_pos, s_order, s_altk, s_altv, s_counts, s_scan;
     hs::DevBuf s_pairs, s_count, s_work, s_stats;
     std::unique_ptr<hs::BatchPlan> batch;
+    // technique selector: learned network and/or analytic cost model
+    bool has_mlp = false, has_cost = false;
+    std::vector<float> mlp_params;            // MLP_PARAMS
+    float feat_mean[hs::MLP_IN] = {}, feat_scale[hs::MLP_IN] = {};
+    double cost[3][9] = {};                   // per technique (bitmap, fgss, direct)
+    hs::DevBuf d_mlp, d_feat, d_moments, d_hist;
+    std::map<std::string, std::pair<hyset_technique, int>> select_cache;  // decision, selector
 };
 
 struct hyset_coll {
@@ -141,6 +148,7 @@ struct hyset_result {
     double kernel_ms = 0;
     uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     uint64_t launches = 0;
+    int selector = -1;  // -1 explicit technique, 0 rules, 1 analytic cost model, 2 learned network
 };
 
 struct hyset_handler {

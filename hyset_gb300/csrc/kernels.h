@@ -146,6 +146,27 @@ struct BatchDesc {
 cudaError_t launch_batch_join(const BatchDesc* d_desc, const uint32_t* d_unit_off, uint32_t n_joins,
                               unsigned int* d_work, int sm_count, cudaStream_t s);
 
+// ---- stats.cu --------------------------------------------------------------
+// out4[0] += sum, [1] += sum of squares, [2] = max, [3] += non-zero count (zero out4 first)
+cudaError_t moments_u32(const uint32_t* v, uint64_t n, unsigned long long* out4, cudaStream_t s);
+
+// ---- mlp.cu ----------------------------------------------------------------
+constexpr int MLP_IN = 12, MLP_HIDDEN = 64, MLP_OUT = 3;
+constexpr int MLP_PARAMS = MLP_IN * MLP_HIDDEN + MLP_HIDDEN + MLP_HIDDEN * MLP_HIDDEN + MLP_HIDDEN +
+                           MLP_HIDDEN * MLP_OUT + MLP_OUT;  // 5187
+constexpr int MLP_MAX_BATCH = 128;  // samples held in shared memory at once
+constexpr int MLP_THREADS = 256;
+size_t mlp_smem_bytes();
+// y[n][3] = net(x[n][12])
+cudaError_t mlp_forward(const float* w, const float* x, int n, float* y, int sm_count, cudaStream_t s);
+// g = dLoss/dw, *loss = Loss over the dataset (t, m: [n][3] targets and 0/1 mask; denom = sum of m)
+cudaError_t mlp_grad(const float* w, const float* x, const float* t, const float* m, int n, float denom, float* g,
+                     float* loss, cudaStream_t s);
+// `steps` Adam steps (w, mom, vel, g: MLP_PARAMS floats each; mom/vel zeroed by the caller)
+cudaError_t mlp_train(float* w, float* mom, float* vel, float* g, const float* x, const float* t, const float* m,
+                      int n, float denom, int steps, float lr, float weight_decay, float* loss_trace,
+                      cudaStream_t s);
+
 // Explicit candidate lists (hybrid::device_handler): probes[i] owns candidates
 // [i ? offsets[i-1] : 0, offsets[i]).
 cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const uint32_t* probes,

@@ -194,6 +194,44 @@ hyset_status hyset_verifier_flush(hyset_verifier* v);
 hyset_status hyset_verifier_output(const hyset_verifier* v, uint64_t* count, const hyset_pair** pairs);
 void hyset_verifier_destroy(hyset_verifier* v);
 
+/* ---- technique selector ------------------------------------------ */
+/* statistics::extract (include/hyset/statistics.hpp:163-213) and the analytic
+ * model of cost::run (include/hyset/cost.hpp:28-58) drive the reference's
+ * technique choice.  Here a small FP32 network (12 -> 64 -> 64 -> 3, ReLU,
+ * trained on the GPU by this library's kernels on timings this library
+ * measured) predicts the log-time of the bitmap, prefix-index and
+ * direct-verify techniques for a join; the analytic cost model is its
+ * fallback; without either, fixed rules decide.  The choice never changes a
+ * join's output. */
+#define HYSET_FEATURES 12
+#define HYSET_MLP_PARAMS 5187
+#define HYSET_COST_TERMS 9
+/* features[12]: log2(1+probes), mean size, size std, log2(1+max size),
+ * log2(1+universe), threshold, sim/2, mean probe prefix, log2(1+index entries),
+ * log2(1+token-frequency std), log2(1+max token frequency), log2(1+length-
+ * compatible pairs).  base_stats[8] (may be NULL): the reference's
+ * statistics::base — size std, mean size, token-frequency std, set count,
+ * universe, index entries — then length-compatible pairs and mean prefix. */
+hyset_status hyset_join_features(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                                 const hyset_join_opts* opts, float* features, double* base_stats);
+/* Host arrays: x[n][12], y/t/mask[n][3], params[HYSET_MLP_PARAMS]. */
+hyset_status hyset_mlp_forward(hyset_ctx* ctx, const float* params, const float* x, uint32_t n, float* y);
+hyset_status hyset_mlp_grad(hyset_ctx* ctx, const float* params, const float* x, const float* t, const float* mask,
+                            uint32_t n, float* grad, float* loss);
+/* Full-dataset Adam on the GPU; params is updated in place; loss_trace[steps] may be NULL. */
+hyset_status hyset_mlp_train(hyset_ctx* ctx, float* params, const float* x, const float* t, const float* mask,
+                             uint32_t n, uint32_t steps, float lr, float weight_decay, float* loss_trace);
+/* Installs the selector AUTO uses: params (NULL: none) with the features'
+ * normalisation x' = (x - mean) / scale, and the analytic model's coefficients
+ * per technique (bitmap, fgss, direct) x HYSET_COST_TERMS in the reference's
+ * form |c0 + c1 std + c2 avg + c3 tokfreq + c4 n + c5 n^2 + c6 universe +
+ * c7 index + c8 bitmap| (NULL: none). */
+hyset_status hyset_selector_set(hyset_ctx* ctx, const float* params, const float* feature_mean,
+                                const float* feature_scale, const double* cost_coefficients);
+/* Which selector chose the result's technique: -1 explicit, 0 rules,
+ * 1 analytic cost model, 2 learned network. */
+int hyset_result_selector(const hyset_result* r);
+
 /* ---- verification without allocation ------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they verify: a host engine that owns all GPU memory through its

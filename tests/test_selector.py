@@ -1,0 +1,120 @@
+"""Technique selector: the network's GPU kernels against the float64 numpy
+restatement, the analytic cost model, and AUTO's output neutrality."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _data(n=40, seed=0):
+    rng = np.random.default_rng(seed)
+    x = rng.normal(size=(n, 12)).astype(np.float32)
+    t = rng.normal(size=(n, 3)).astype(np.float32)
+    m = (rng.random((n, 3)) > 0.2).astype(np.float32)
+    return x, t, m
+
+
+def test_numpy_reference_gradient_matches_finite_differences():
+    from oracle import mlp
+    from hyset_gb300.selector import init_params
+    p = init_params(3).astype(np.float64)
+    x, t, m = _data(10, 1)
+    _, g = mlp.loss_grad(p, x, t, m)
+    rng = np.random.default_rng(2)
+    for i in rng.choice(p.size, 40, replace=False):
+        e = np.zeros_like(p)
+        e[i] = 1e-6
+        num = (mlp.loss_grad(p + e, x, t, m)[0] - mlp.loss_grad(p - e, x, t, m)[0]) / 2e-6
+        assert abs(num - g[i]) <= 1e-5 + 1e-4 * abs(g[i])
+
+
+def test_cost_model_fit_recovers_a_linear_cost():
+    from hyset_gb300.selector import cost_predict, fit_cost_model
+    rng = np.random.default_rng(0)
+    true = np.array([5.0, 0.1, 0.2, 0.01, 1e-5, 0.0, 1e-6, 2e-6, 0.0])
+    rows = []
+    for _ in range(60):
+        base = [rng.uniform(1, 50), rng.uniform(5, 200), rng.uniform(1, 30), rng.uniform(1e4, 1e6),
+                rng.uniform(1e4, 1e6), rng.uniform(1e5, 1e7), 0, 0]
+        x = np.array([1.0, base[0], base[1], base[2], base[3], base[3] ** 2, base[4], base[5], 0.0])
+        rows.append({"base": base, "ms": [float(true @ x)] * 3})
+    coefs = fit_cost_model(rows)
+    for r in rows[:10]:
+        assert abs(cost_predict(coefs, r["base"])[1] - r["ms"][1]) <= 0.02 * r["ms"][1]
+
+
+def test_shipped_selector_report_shows_the_network_gains():
+    path = os.path.join(ROOT, "hyset_gb300", "selector_weights.json")
+    if not os.path.exists(path):
+        pytest.skip("no trained selector shipped yet")
+    with open(path) as f:
+        w = json.load(f)
+    assert len(w["params"]) == 5187 and len(w["mean"]) == 12 and len(w["cost"]) == 27
+    rep = w["report"]["held_out"]
+    # held-out collections: the learned choice is at least as good as the
+    # method without it (fixed rules) and as the analytic cost model
+    assert rep["mlp"]["mean_regret"] <= rep["rules"]["mean_regret"] + 1e-9
+    assert rep["mlp"]["mean_regret"] <= rep["cost_model"]["mean_regret"] + 1e-9
+
+
+@pytest.mark.gpu
+def test_gpu_forward_and_gradient_match_numpy(ctx):
+    from oracle import mlp
+    from hyset_gb300.selector import init_params
+    for n in (5, 128, 300):  # one chunk, exactly one, several
+        p = init_params(n)
+        x, t, m = _data(n, n)
+        y = ctx.mlp_forward(p, x)
+        y64, _ = mlp.forward(p, x)
+        np.testing.assert_allclose(y, y64, rtol=1e-4, atol=1e-4)
+        g, loss = ctx.mlp_grad(p, x, t, m)
+        l64, g64 = mlp.loss_grad(p, x, t, m)
+        assert abs(loss - l64) <= 1e-4 * max(1.0, abs(l64))
+        np.testing.assert_allclose(g, g64, rtol=2e-3, atol=2e-5)
+
+
+@pytest.mark.gpu
+def test_gpu_training_reduces_loss(ctx):
+    from hyset_gb300.selector import init_params
+    rng = np.random.default_rng(5)
+    x = rng.normal(size=(150, 12)).astype(np.float32)
+    t = np.stack([x[:, 0] * 2 - x[:, 1], np.sin(x[:, 2]), x[:, 3] ** 2], 1).astype(np.float32)
+    m = np.ones_like(t)
+    p, trace = ctx.mlp_train(init_params(1), x, t, m, steps=400, lr=3e-3)
+    assert trace[-1] < 0.2 * trace[0]
+    from oracle import mlp
+    assert abs(mlp.loss_grad(p, x, t, m)[0] - trace[-1]) < 0.05 * max(trace[-1], 1e-3) + 1e-3
+
+
+@pytest.mark.gpu
+def test_auto_with_selector_is_output_neutral(ctx):
+    import hyset_gb300 as hs
+    import oracle
+    from hyset_gb300 import synth
+    from hyset_gb300.selector import init_params
+    c = synth.generate(synth.C2, n_sets=20000, seed=4)
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.7))
+    mean, scale = np.zeros(12, np.float32), np.ones(12, np.float32)
+    for bias in range(3):  # force each technique through the network's bias
+        p = init_params(0)
+        p[-3:] = [5.0, 5.0, 5.0]
+        p[-3 + bias] = -5.0
+        p[:-3] *= 0.0
+        with hs.Context(0, selector=False) as c2:
+            c2.selector_set(p, mean, scale, None)
+            coll2 = c2.upload(c.tokens, c.sizes, c.starts)
+            r = c2.self_join(coll2, threshold=0.7)
+            assert r.selector == "mlp" and r.technique == ["bitmap", "fgss", "direct"][bias]
+            assert oracle.as_set(r.pairs) == exp
+    cost = np.zeros((3, 9))
+    cost[:, 0] = [3.0, 1.0, 2.0]  # constant costs: fgss is cheapest
+    with hs.Context(0, selector=False) as c3:
+        c3.selector_set(None, None, None, cost)
+        coll3 = c3.upload(c.tokens, c.sizes, c.starts)
+        r = c3.self_join(coll3, threshold=0.7)
+        assert r.selector == "cost_model" and r.technique == "fgss"
+        assert oracle.as_set(r.pairs) == exp
