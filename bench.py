@@ -312,6 +312,84 @@ def run_ours(args, ws, rank, local):
     return out
 
 
+def batch_workload(n_joins=256, seed=0x5E7B):
+    """R-S joins of uneven sizes: |R|, |S| log-uniform in [1e3, 2e5], Zipf s in
+    [0.7, 1.3], mean set size log-uniform in [8, 300], universe 5e4..5e5,
+    threshold in [0.5, 0.95], similarity Jaccard / cosine / dice in turn.  R and
+    S of a join are a random split of one generated collection, so near-duplicate
+    sets fall on both sides."""
+    import math
+    import numpy as np
+    from hyset_gb300 import synth
+    rng = np.random.default_rng(seed)
+    sims = ["jaccard", "cosine", "dice"]
+    out = []
+    for j in range(n_joins):
+        nr = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
+        ns = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
+        mean = math.exp(rng.uniform(math.log(8), math.log(300)))
+        c = synth.generate(synth.C2, n_sets=nr + ns, universe=int(rng.uniform(5e4, 5e5)),
+                           zipf_s=float(rng.uniform(0.7, 1.3)), size_dist=synth.LOGNORMAL,
+                           size_a=math.log(mean) - 0.125, size_b=0.5, size_min=2,
+                           size_max=min(2000, max(16, int(mean * 6))), dup_frac=0.05, dup_edit_lo=0.02,
+                           dup_edit_hi=0.12, seed=int(rng.integers(1, 2**31)))
+        side = rng.random(c.n) < nr / (nr + ns)
+        parts = []
+        for mask in (side, ~side):
+            ids = np.nonzero(mask)[0]
+            sizes = c.sizes[ids]
+            starts = np.zeros(len(ids), np.uint32)
+            if len(ids):
+                starts[1:] = np.cumsum(sizes[:-1])
+            sz64 = sizes.astype(np.int64)
+            src = np.repeat(c.starts[ids].astype(np.int64) - starts.astype(np.int64), sz64) + np.arange(sz64.sum())
+            parts.append((c.tokens[src], starts, sizes))
+        out.append((parts[0], parts[1], dict(threshold=float(rng.uniform(0.5, 0.95)), sim=sims[j % 3])))
+    return out
+
+
+def run_batch(args):
+    import torch
+    import hyset_gb300 as hs
+    t0 = time.time()
+    work = batch_workload(args.joins)
+    gen_s = time.time() - t0
+    ctx = hs.Context(0)
+    joins, colls = [], []
+    for (rt, rs, rz), (st, ss, sz), kw in work:
+        R = ctx.upload(rt, rz, rs)
+        S = ctx.upload(st, sz, ss)
+        colls += [R, S]
+        joins.append((R, S, dict(kw, device_pairs=True)))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        res = ctx.batch_join(joins)
+    batch_ms, seq_ms = [], []
+    for _ in range(args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        res = ctx.batch_join(joins)
+        batch_ms.append(res[0].device_ms)
+    total = sum(r.count for r in res)
+    # the same joins one launch sequence at a time (each through its own self/rs call)
+    for _ in range(max(1, args.steps // 2)):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t = 0.0
+        for R, S, kw in joins:
+            t += ctx.rs_join(R, S, **kw).device_ms
+        seq_ms.append(t)
+    bm, sm = statistics.mean(batch_ms), statistics.mean(seq_ms)
+    print(json.dumps({"metric": "batched R-S joins: result pairs/s (one persistent launch in a CUDA graph)",
+                      "value": total / (bm / 1000.0), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
+                      "warmup": args.warmup, "ms_per_step": bm, "higher_is_better": True,
+                      "config": {"workload": f"{args.joins} R-S joins, |R|,|S| log-uniform [1e3, 2e5], mean size "
+                                             "log-uniform [8, 300], mixed similarity, threshold U[0.5, 0.95]",
+                                 "result_pairs": total, "sets": int(sum(c.n for c in colls)),
+                                 "one_at_a_time_ms": sm, "speedup_vs_one_at_a_time": sm / bm,
+                                 "generation_s": gen_s}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -326,8 +404,14 @@ def main():
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
     ap.add_argument("--vmode", type=int, default=0, help="verification: 0 auto, 1 lane, 2 warp per candidate")
+    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch"],
+                    help="batch: the batched R-S workload (a separate measurement, not the headline)")
+    ap.add_argument("--joins", type=int, default=256)
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.workload == "batch":
+        run_batch(args)
+        return
     if args.impl == "reference":
         run_reference(args, ws, rank)
     else:

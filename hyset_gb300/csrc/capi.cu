@@ -549,6 +549,80 @@ hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
     return HYSET_OK;
 }
 
+// Autotuner for the prefix-index join's signature width: on the first AUTO join
+// of a (collections, similarity, threshold), the probe-major kernel runs on
+// three probe samples spread over the probe range with no signatures and with
+// 128- and 256-bit signatures, and the fastest width is kept for that join.
+// Measured on GB300: 256 bits wins on long sets, 128 on short ones, none at
+// high thresholds on some collections.
+constexpr uint32_t TUNE_MIN_PROBES = 20000, TUNE_SAMPLE = 2048;
+
+hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
+                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits) {
+    char key[128];
+    std::snprintf(key, sizeof key, "%p/%p/%d/%.17g/%u/%u", (void*)R, (void*)S, (int)o->sim, o->threshold, p_lo, p_hi);
+    auto it = ctx->bits_cache.find(key);
+    if (it != ctx->bits_cache.end()) {
+        *bits = it->second;
+        return HYSET_OK;
+    }
+    cudaStream_t s = ctx->stream;
+    ST(build_sorted_index(ctx, R, b, self ? 0 : 1, R->index));
+    JoinParams P{};
+    P.R = R->view();
+    P.S = S->view();
+    P.B = b->view;
+    P.first_ge = R->first_ge.as<uint32_t>();
+    P.R_L = R->max_size;
+    P.self = self ? 1 : 0;
+    P.r_lo = 0;
+    P.r_hi = R->n;
+    P.grab = 4;
+    P.X = R->index.view();
+    CK(ctx->s_count.ensure(16, s));
+    CK(ctx->s_work.ensure(16, s));
+    P.out = Sink{nullptr, ctx->s_count.as<unsigned long long>(), 0, 1};
+    P.work = ctx->s_work.as<unsigned int>();
+    const uint32_t cand[3] = {0, 128, 256};
+    float best_ms = 0;
+    uint32_t best = 256;
+    for (int k = 0; k < 3; ++k) {
+        const int words = (int)(cand[k] / 64);
+        P.words = words;
+        P.bits_R = P.bits_S = nullptr;
+        if (words) {
+            const uint64_t *br = nullptr, *bs = nullptr;
+            ST(get_bitmaps(ctx, R, words, &br));
+            if (self) bs = br;
+            else ST(get_bitmaps(ctx, S, words, &bs));
+            P.bits_R = br;
+            P.bits_S = bs;
+        }
+        float total = 0;
+        for (int c = 0; c < 3; ++c) {  // samples at the start, middle and end of the probe range
+            const uint32_t span = p_hi - p_lo, len = std::min(TUNE_SAMPLE, span / 3);
+            P.p_lo = p_lo + (uint32_t)((uint64_t)(span - len) * c / 2);
+            P.p_hi = P.p_lo + len;
+            CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+            CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
+            CK(cudaEventRecord(ctx->ek0, s));
+            CK(launch_join(P, TECH_FGSS, 1, ctx->sm_count, s));
+            CK(cudaEventRecord(ctx->ek1, s));
+            CK(cudaEventSynchronize(ctx->ek1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ctx->ek0, ctx->ek1));
+            total += ms;
+        }
+        if (k == 0 || total < best_ms) {
+            best_ms = total;
+            best = cand[k];
+        }
+    }
+    ctx->bits_cache[key] = best;
+    *bits = best;
+    return HYSET_OK;
+}
+
 hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, hyset_result* res) {
     ST(check_opts(ctx, o));
     const bool self = (S == R);
@@ -557,10 +631,16 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     ST(get_bounds(ctx, o->sim, o->threshold, L, self ? 0 : 1, &b));
     hyset_technique selected = HYSET_TECH_AUTO;
     ST(select_technique(ctx, R, S, o, &selected, &res->selector));
-    const Tuned tn = tune(R, S, o, selected);
+    Tuned tn = tune(R, S, o, selected);
     const hyset_technique tech = tn.tech;
     const int vmode = tn.vmode;
     res->technique = tech;
+    {
+        const uint32_t a_lo = o->probe_end ? o->probe_begin : 0, a_hi = o->probe_end ? o->probe_end : S->n;
+        if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && tech == HYSET_TECH_FGSS && tn.probe_major &&
+            a_hi - a_lo >= TUNE_MIN_PROBES)
+            ST(autotune_bits(ctx, R, S, o, b, self, a_lo, a_hi, &tn.bits));
+    }
     if (o->probe_end > S->n || o->probe_begin > o->probe_end)
         return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
     const unsigned long long launches0 = launches();

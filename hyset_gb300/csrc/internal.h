@@ -117,6 +117,7 @@ struct hyset_ctx {
     double cost[3][9] = {};                   // per technique (bitmap, fgss, direct)
     hs::DevBuf d_mlp, d_feat, d_moments, d_hist;
     std::map<std::string, std::pair<hyset_technique, int>> select_cache;  // decision, selector
+    std::map<std::string, uint32_t> bits_cache;  // autotuned signature width per join
 };
 
 struct hyset_coll {

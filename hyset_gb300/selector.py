@@ -62,12 +62,12 @@ def install_shipped(ctx, path: str = WEIGHTS):
 
 # ------------------------------------------------------------------ training data
 
-def grid(n_collections: int, seed: int = 2024):
+def grid(n_collections: int, seed: int = 2024, n_lo: int = 50_000, n_hi: int = 1_000_000):
     """Seeded grid configurations (ordered; the last ones are held out)."""
     rng = np.random.default_rng(seed)
     out = []
     while len(out) < n_collections:
-        n = int(math.exp(rng.uniform(math.log(50_000), math.log(1_000_000))))
+        n = int(math.exp(rng.uniform(math.log(n_lo), math.log(n_hi))))
         mean = math.exp(rng.uniform(math.log(10), math.log(300)))
         if n * mean > 8e7:  # keep every collection within a few hundred MB
             continue
@@ -218,24 +218,37 @@ def main(argv=None):
     ap.add_argument("--collections", type=int, default=80)
     ap.add_argument("--train", type=int, default=64)
     ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--small", type=int, default=40,
+                    help="extra collections with 1k-50k sets (the batched R-S joins' range)")
+    ap.add_argument("--small-train", type=int, default=32)
     args = ap.parse_args(argv)
     from .api import Context
     ctx = Context(0, selector=False)
     cfgs = grid(args.collections)
-    rows = collect(ctx, cfgs)
-    tr = [r for r in rows if r["collection"] < args.train]
-    te = [r for r in rows if r["collection"] >= args.train]
+    small = grid(args.small, seed=4048, n_lo=1_000, n_hi=50_000)
+    rows = collect(ctx, cfgs + small)
+    big_ids = set(range(args.collections))
+    is_train = lambda r: (r["collection"] < args.train if r["collection"] in big_ids
+                          else r["collection"] - args.collections < args.small_train)
+    tr = [r for r in rows if is_train(r)]
+    te = [r for r in rows if not is_train(r)]
     params, mean, scale, trace = train(ctx, tr, steps=args.steps)
     coefs = fit_cost_model(tr)
-    report = {"held_out": evaluate(ctx, params, mean, scale, coefs, [r for r in te if r["part"] == "all"]),
+    whole = lambda rs: [r for r in rs if r["part"] == "all"]
+    report = {"held_out": evaluate(ctx, params, mean, scale, coefs, whole(te)),
+              "held_out_grid_50k_1m": evaluate(ctx, params, mean, scale, coefs,
+                                               [r for r in whole(te) if r["collection"] in big_ids]),
+              "held_out_small_1k_50k": evaluate(ctx, params, mean, scale, coefs,
+                                                [r for r in whole(te) if r["collection"] not in big_ids]),
               "held_out_partitions": evaluate(ctx, params, mean, scale, coefs, te),
-              "train": evaluate(ctx, params, mean, scale, coefs, [r for r in tr if r["part"] == "all"]),
+              "train": evaluate(ctx, params, mean, scale, coefs, whole(tr)),
               "final_loss": float(trace[-1]) if len(trace) else None, "first_loss": float(trace[0])}
     os.makedirs(args.out, exist_ok=True)
     with open(os.path.join(args.out, "selector_weights.json"), "w") as f:
         json.dump({"params": params.tolist(), "mean": mean.tolist(), "scale": scale.tolist(),
                    "cost": coefs.ravel().tolist(), "techniques": TECHNIQUES,
-                   "trained_on": args.train, "held_out": args.collections - args.train, "report": report}, f)
+                   "trained_on": args.train + args.small_train,
+                   "held_out": args.collections - args.train + args.small - args.small_train, "report": report}, f)
     with open(os.path.join(args.out, "selector_samples.json"), "w") as f:
         json.dump(rows, f)
     print(json.dumps(report, indent=1))
