@@ -118,3 +118,38 @@ def test_auto_with_selector_is_output_neutral(ctx):
         r = c3.self_join(coll3, threshold=0.7)
         assert r.selector == "cost_model" and r.technique == "fgss"
         assert oracle.as_set(r.pairs) == exp
+
+
+def test_shipped_report_recomputes_from_samples():
+    """The held-out regrets stored with the weights follow from the shipped
+    timing samples and the network (recomputed here in float64)."""
+    wpath = os.path.join(ROOT, "hyset_gb300", "selector_weights.json")
+    spath = os.path.join(ROOT, "hyset_gb300", "selector_samples.json")
+    if not (os.path.exists(wpath) and os.path.exists(spath)):
+        pytest.skip("no trained selector shipped yet")
+    from oracle import mlp
+    from hyset_gb300.selector import rules_choice
+    with open(wpath) as f:
+        w = json.load(f)
+    with open(spath) as f:
+        rows = json.load(f)
+    p = np.array(w["params"])
+    mean, scale = np.array(w["mean"]), np.array(w["scale"])
+    n_big, n_small = 80, 40
+    train_big, train_small = 64, 32
+    held = [r for r in rows if r["part"] == "all" and
+            ((r["collection"] < n_big and r["collection"] >= train_big) or
+             (r["collection"] >= n_big and r["collection"] - n_big >= train_small))]
+    assert len(held) == w["held_out"]
+    x = (np.array([r["features"] for r in held]) - mean) / scale
+    y, _ = mlp.forward(p, x)
+    reg_mlp, reg_rules = [], []
+    for r, yy in zip(held, y):
+        ms = np.array(r["ms"])
+        best = ms.min()
+        reg_mlp.append(ms[int(np.argmin(yy))] / best - 1)
+        reg_rules.append(ms[rules_choice(r)] / best - 1)
+    rep = w["report"]["held_out"]
+    assert abs(np.mean(reg_rules) - rep["rules"]["mean_regret"]) < 1e-3
+    assert abs(np.mean(reg_mlp) - rep["mlp"]["mean_regret"]) < 0.02  # float32 GPU vs float64 argmin ties
+    assert np.mean(reg_mlp) < np.mean(reg_rules)
