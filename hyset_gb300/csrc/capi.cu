@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <string>
 
 #include "internal.h"
 
@@ -484,6 +485,28 @@ hyset_status compute_features(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
     return HYSET_OK;
 }
 
+// Content signature of a collection for the selector and autotuner caches: the
+// decisions depend only on the collection's statistics, so a re-uploaded copy
+// of the same data reuses them.
+std::string coll_signature(const hyset_coll* c) {
+    uint64_t h = 1469598103934665603ull;  // FNV-1a over the size histogram
+    for (uint64_t v : c->size_hist) {
+        h ^= v;
+        h *= 1099511628211ull;
+    }
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "%u:%llu:%u:%u:%016llx", c->n, (unsigned long long)c->n_tokens, c->universe,
+                  c->max_size, (unsigned long long)h);
+    return buf;
+}
+
+std::string join_key(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o) {
+    char buf[96];
+    std::snprintf(buf, sizeof buf, "|%d|%.17g|%u|%u|%d", (int)o->sim, o->threshold, o->probe_begin, o->probe_end,
+                  R == S ? 1 : 0);
+    return coll_signature(R) + "/" + coll_signature(S) + buf;
+}
+
 const hyset_technique kSelectable[3] = {HYSET_TECH_BITMAP, HYSET_TECH_FGSS, HYSET_TECH_DIRECT};
 
 // cost.hpp:28-58 / statistics.hpp:150-160: |c . (1, std, avg, tokfreq, n, n^2, U, index, bitmap)|
@@ -506,9 +529,7 @@ hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
         return HYSET_OK;
     }
     if (!ctx->has_mlp && !ctx->has_cost) return HYSET_OK;
-    char key[128];
-    std::snprintf(key, sizeof key, "%p/%p/%d/%.17g/%u/%u", (void*)R, (void*)S, (int)o->sim, o->threshold,
-                  o->probe_begin, o->probe_end);
+    const std::string key = join_key(R, S, o);
     auto it = ctx->select_cache.find(key);
     if (it != ctx->select_cache.end()) {
         *out = it->second.first;
@@ -559,8 +580,7 @@ constexpr uint32_t TUNE_MIN_PROBES = 20000, TUNE_SAMPLE = 2048;
 
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
                            bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits) {
-    char key[128];
-    std::snprintf(key, sizeof key, "%p/%p/%d/%.17g/%u/%u", (void*)R, (void*)S, (int)o->sim, o->threshold, p_lo, p_hi);
+    const std::string key = join_key(R, S, o);
     auto it = ctx->bits_cache.find(key);
     if (it != ctx->bits_cache.end()) {
         *bits = it->second;
