@@ -201,25 +201,25 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     const uint64_t E = prefix_entries(c, b->index_prefix);
     if (E >= (1ull << 32)) return fail(ctx, HYSET_E_UNSUPPORTED, "more than 2^32 prefix entries");
     const uint64_t E1 = E ? E : 1;
-    CK(ctx->s_len.ensure((size_t)n * 4 + 4, s));
-    CK(ctx->s_off.ensure((size_t)n * 4 + 4, s));
-    CK(ctx->s_tok.ensure(E1 * 4, s));
-    CK(ctx->s_set.ensure(E1 * 4, s));
-    CK(ctx->s_pos.ensure(E1 * 4, s));
-    CK(ctx->s_order.ensure(E1 * 4, s));
-    CK(ctx->s_altk.ensure(E1 * 4, s));
-    CK(ctx->s_altv.ensure(E1 * 4, s));
-    CK(ctx->s_counts.ensure(((size_t)U + 1) * 4, s));
+    CK(ctx->sc->len.ensure((size_t)n * 4 + 4, s));
+    CK(ctx->sc->off.ensure((size_t)n * 4 + 4, s));
+    CK(ctx->sc->tok.ensure(E1 * 4, s));
+    CK(ctx->sc->set.ensure(E1 * 4, s));
+    CK(ctx->sc->pos.ensure(E1 * 4, s));
+    CK(ctx->sc->order.ensure(E1 * 4, s));
+    CK(ctx->sc->altk.ensure(E1 * 4, s));
+    CK(ctx->sc->altv.ensure(E1 * 4, s));
+    CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
     size_t scan_words = std::max(std::max(scan_scratch_words(n), scan_scratch_words((uint64_t)U + 1)),
                                  radix_scratch_words(E1));
-    CK(ctx->s_scan.ensure(scan_words * 4, s));
+    CK(ctx->sc->scan.ensure(scan_words * 4, s));
     CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
     CK(ix.set.ensure(E1 * 4, s));
     CK(ix.pos.ensure(E1 * 4, s));
     CollView v = c->view();
-    uint32_t* len = ctx->s_len.as<uint32_t>();
-    uint32_t* off = ctx->s_off.as<uint32_t>();
-    uint32_t* scr = ctx->s_scan.as<uint32_t>();
+    uint32_t* len = ctx->sc->len.as<uint32_t>();
+    uint32_t* off = ctx->sc->off.as<uint32_t>();
+    uint32_t* scr = ctx->sc->scan.as<uint32_t>();
     CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
     CK(scan_exclusive(len, off, n, scr, s));
     // Packed entries (set << pb | position) when set ids up to n and positions
@@ -229,12 +229,12 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         if (c->size_hist[l]) max_pre = std::max(max_pre, pre_len(b, (uint32_t)l));
     const uint32_t pb = bits_for(max_pre), sb = bits_for(n);
     if (pb + sb <= 32) {
-        uint32_t* counts = ctx->s_counts.as<uint32_t>();
+        uint32_t* counts = ctx->sc->counts.as<uint32_t>();
         CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
-        CK(emit_packed_entries(v, off, len, pb, ctx->s_tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
+        CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
         CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
-        CK(radix_sort_pairs(ctx->s_tok.as<uint32_t>(), ix.set.as<uint32_t>(), ctx->s_altk.as<uint32_t>(),
-                            ctx->s_altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
+        CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
+                            ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
         ix.sim = b->sim;
         ix.tau = b->tau;
         ix.kind = kind;
@@ -243,16 +243,16 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         ix.pos_bits = pb;
         return HYSET_OK;
     }
-    CK(emit_prefix_entries(v, 0, n, off, len, ctx->s_tok.as<uint32_t>(), ctx->s_set.as<uint32_t>(),
-                           ctx->s_pos.as<uint32_t>(), s));
-    uint32_t* counts = ctx->s_counts.as<uint32_t>();
+    CK(emit_prefix_entries(v, 0, n, off, len, ctx->sc->tok.as<uint32_t>(), ctx->sc->set.as<uint32_t>(),
+                           ctx->sc->pos.as<uint32_t>(), s));
+    uint32_t* counts = ctx->sc->counts.as<uint32_t>();
     CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
-    CK(token_histogram(ctx->s_tok.as<uint32_t>(), E, counts, s));
+    CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, s));
     CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
-    CK(iota_u32(ctx->s_order.as<uint32_t>(), E, s));
-    CK(radix_sort_pairs(ctx->s_tok.as<uint32_t>(), ctx->s_order.as<uint32_t>(), ctx->s_altk.as<uint32_t>(),
-                        ctx->s_altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
-    CK(gather_entries(ctx->s_order.as<uint32_t>(), E, ctx->s_set.as<uint32_t>(), ctx->s_pos.as<uint32_t>(),
+    CK(iota_u32(ctx->sc->order.as<uint32_t>(), E, s));
+    CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ctx->sc->order.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
+                        ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
+    CK(gather_entries(ctx->sc->order.as<uint32_t>(), E, ctx->sc->set.as<uint32_t>(), ctx->sc->pos.as<uint32_t>(),
                       ix.set.as<uint32_t>(), ix.pos.as<uint32_t>(), s));
     ix.sim = b->sim;
     ix.tau = b->tau;
@@ -274,11 +274,11 @@ hyset_status build_groups(hyset_ctx* ctx, hyset_coll* c, const uint32_t* d_pre, 
     CK(c->g_cursor.ensure(((size_t)U + 1) * 4, s));
     CK(c->g_set.ensure((E ? E : 1) * 4, s));
     CK(c->g_ps.ensure((E ? E : 1) * 4, s));
-    CK(ctx->s_scan.ensure(scan_scratch_words((uint64_t)U + 1) * 4, s));
+    CK(ctx->sc->scan.ensure(scan_scratch_words((uint64_t)U + 1) * 4, s));
     uint32_t* cnt = c->g_cursor.as<uint32_t>();
     CK(cudaMemsetAsync(cnt, 0, ((size_t)U + 1) * 4, s));
     CK(group_count(c->view(), d_pre, cnt, s));
-    CK(scan_exclusive(cnt, c->g_off.as<uint32_t>(), (uint64_t)U + 1, ctx->s_scan.as<uint32_t>(), s));
+    CK(scan_exclusive(cnt, c->g_off.as<uint32_t>(), (uint64_t)U + 1, ctx->sc->scan.as<uint32_t>(), s));
     CK(cudaMemcpyAsync(cnt, c->g_off.p, ((size_t)U + 1) * 4, cudaMemcpyDeviceToDevice, s));
     CK(group_scatter(c->view(), d_pre, cnt, c->g_set.as<uint32_t>(), c->g_ps.as<uint32_t>(), s));
     *entries = E;
@@ -341,6 +341,23 @@ Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o,
     return t;
 }
 
+// Orders n result pairs by (probe id, indexed id) on the device, in place.
+hyset_status sort_device_pairs(hyset_ctx* ctx, uint2* pairs, uint64_t n, uint32_t n_probe, uint32_t n_indexed) {
+    if (n <= 1) return HYSET_OK;
+    cudaStream_t s = ctx->stream;
+    Scratch& sc = ctx->own;
+    const size_t b = (size_t)n * 4;
+    CK(sc.tok.ensure(b, s));
+    CK(sc.set.ensure(b, s));
+    CK(sc.altk.ensure(b, s));
+    CK(sc.altv.ensure(b, s));
+    CK(sc.scan.ensure(radix_scratch_words(n) * 4, s));
+    CK(sort_pair_list(pairs, n, (int)bits_for(n_probe), (int)bits_for(n_indexed), sc.tok.as<uint32_t>(),
+                      sc.set.as<uint32_t>(), sc.altk.as<uint32_t>(), sc.altv.as<uint32_t>(), sc.scan.as<uint32_t>(),
+                      s));
+    return HYSET_OK;
+}
+
 // Runs one configured join launch into the context's pair buffer, growing the
 // buffer and re-running when the first pass overflowed.
 hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const hyset_join_opts* o,
@@ -389,7 +406,9 @@ hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const h
         cap = count + count / 8 + 1024;  // overflow: retry once with room for everything
         if (attempt == 1) return fail(ctx, HYSET_E_OVERFLOW, "pair buffer overflow after resize");
     }
+    if (!count_only && o->sort_pairs) ST(sort_device_pairs(ctx, ctx->s_pairs.as<uint2>(), res->count, P.S.n, P.R.n));
     if (!count_only && o->device_pairs) {
+        if (o->sort_pairs) CK(cudaStreamSynchronize(s));  // device pairs are final when the call returns
         res->device_pairs = ctx->s_pairs.p;
     } else if (!count_only) {
         res->pairs.resize(res->count);
@@ -732,10 +751,6 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
         res->stats[3] = R->index.entries;
     }
     res->launches = launches() - launches0;
-    if (o->sort_pairs && res->has_pairs)
-        std::sort(res->pairs.begin(), res->pairs.end(), [](const hyset_pair& x, const hyset_pair& y) {
-            return x.first != y.first ? x.first < y.first : x.second < y.second;
-        });
     return HYSET_OK;
 }
 
@@ -787,6 +802,7 @@ void batch_release(hyset_ctx* ctx) {
     }
     DevBuf* bufs[] = {&bp.desc, &bp.unit_off, &bp.counts, &bp.work};
     for (DevBuf* d : bufs) d->release(s);
+    bp.sc.release(s);
     cudaStreamSynchronize(s);
     ctx->batch.reset();
 }
@@ -818,6 +834,13 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
     batch_release(ctx);
     auto plan = std::make_unique<BatchPlan>();
     plan->sig = sig;
+    // index builds of the batch use the plan's own scratch, so later joins that
+    // grow the context's scratch cannot free memory the graph still addresses
+    struct ScratchSwitch {
+        hyset_ctx* c;
+        ~ScratchSwitch() { c->sc = &c->own; }
+    } sw{ctx};
+    ctx->sc = &plan->sc;
     cudaStream_t s = ctx->stream;
     std::vector<BatchDesc> desc(n);
     std::vector<double> cost(n);
@@ -896,19 +919,19 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         plan->joins.push_back(std::move(bj));
     }
     // scratch for the largest index build, sized before capture
-    CK(ctx->s_len.ensure((size_t)maxN * 4 + 4, s));
-    CK(ctx->s_off.ensure((size_t)maxN * 4 + 4, s));
+    CK(ctx->sc->len.ensure((size_t)maxN * 4 + 4, s));
+    CK(ctx->sc->off.ensure((size_t)maxN * 4 + 4, s));
     const size_t e4 = (size_t)maxE * 4;
-    CK(ctx->s_tok.ensure(e4, s));
-    CK(ctx->s_set.ensure(e4, s));
-    CK(ctx->s_pos.ensure(e4, s));
-    CK(ctx->s_order.ensure(e4, s));
-    CK(ctx->s_altk.ensure(e4, s));
-    CK(ctx->s_altv.ensure(e4, s));
-    CK(ctx->s_counts.ensure((size_t)maxU * 4, s));
+    CK(ctx->sc->tok.ensure(e4, s));
+    CK(ctx->sc->set.ensure(e4, s));
+    CK(ctx->sc->pos.ensure(e4, s));
+    CK(ctx->sc->order.ensure(e4, s));
+    CK(ctx->sc->altk.ensure(e4, s));
+    CK(ctx->sc->altv.ensure(e4, s));
+    CK(ctx->sc->counts.ensure((size_t)maxU * 4, s));
     const size_t scan_words = std::max(std::max(scan_scratch_words(maxN), scan_scratch_words(maxU)),
                                        radix_scratch_words(maxE));
-    CK(ctx->s_scan.ensure(scan_words * 4, s));
+    CK(ctx->sc->scan.ensure(scan_words * 4, s));
     // heaviest joins first, so the tail of the launch is light
     plan->order.resize(n);
     for (uint32_t j = 0; j < n; ++j) plan->order[j] = j;
@@ -1008,9 +1031,8 @@ void hyset_destroy(hyset_ctx* ctx) {
         cudaStream_t s = ctx->stream;
         batch_release(ctx);
         for (auto& kv : ctx->bounds) kv.second->dev.release(s);
-        DevBuf* bufs[] = {&ctx->s_len, &ctx->s_off, &ctx->s_tok, &ctx->s_set, &ctx->s_pos, &ctx->s_order,
-                          &ctx->s_altk, &ctx->s_altv, &ctx->s_counts, &ctx->s_scan,
-                          &ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats,
+        ctx->own.release(s);
+        DevBuf* bufs[] = {&ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats,
                           &ctx->d_mlp, &ctx->d_feat, &ctx->d_moments, &ctx->d_hist};
         for (DevBuf* b : bufs) b->release(s);
         cudaStreamSynchronize(s);
@@ -1095,6 +1117,14 @@ hyset_status hyset_collection_from_device(hyset_ctx* ctx, const uint32_t* d_toke
 
 void hyset_collection_free(hyset_ctx* ctx, hyset_coll* c) {
     if (!c) return;
+    hyset_ctx* owner = ctx ? ctx : c->ctx;
+    if (owner && owner->batch) {  // a captured batch that reads this collection is dropped with it
+        for (const auto& bj : owner->batch->joins)
+            if (bj->R == c || bj->S == c) {
+                batch_release(owner);
+                break;
+            }
+    }
     cudaStream_t s = ctx ? ctx->stream : c->ctx->stream;
     c->tokens.release(s);
     c->starts.release(s);
@@ -1175,6 +1205,10 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
             continue;
         }
         if (bj.o.count_only) continue;
+        if (bj.o.sort_pairs) {
+            st = sort_device_pairs(ctx, bj.pairs.as<uint2>(), counts[j], bj.S->n, bj.R->n);
+            if (st != HYSET_OK) break;
+        }
         if (bj.o.device_pairs) {
             r->device_pairs = bj.pairs.p;
             continue;
@@ -1189,14 +1223,7 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
     }
     if (st == HYSET_OK) CK(cudaStreamSynchronize(s));
     if (st != HYSET_OK) return st;
-    for (uint32_t j = 0; j < n_joins; ++j) {
-        hyset_result* r = out[j].get();
-        if (bp.joins[j]->o.sort_pairs && r->has_pairs)
-            std::sort(r->pairs.begin(), r->pairs.end(), [](const hyset_pair& x, const hyset_pair& y) {
-                return x.first != y.first ? x.first < y.first : x.second < y.second;
-            });
-        results[j] = out[j].release();
-    }
+    for (uint32_t j = 0; j < n_joins; ++j) results[j] = out[j].release();
     return HYSET_OK;
 }
 

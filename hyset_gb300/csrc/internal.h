@@ -88,8 +88,19 @@ struct BatchJoin {
 
 // A captured batch: signature (collections and options), per-join buffers,
 // device descriptors, and the instantiated graph of its device work.
+// Scratch of an index build (prefix lengths and offsets, entries, radix sort
+// ping-pong buffers, token counts, scan/sort scratch).
+struct Scratch {
+    DevBuf len, off, tok, set, pos, order, altk, altv, counts, scan;
+    void release(cudaStream_t s) {
+        DevBuf* all[] = {&len, &off, &tok, &set, &pos, &order, &altk, &altv, &counts, &scan};
+        for (DevBuf* d : all) d->release(s);
+    }
+};
+
 struct BatchPlan {
     std::vector<std::string> sig;
+    Scratch sc;  // owned by the plan: its graph holds these addresses
     std::vector<std::unique_ptr<BatchJoin>> joins;
     std::vector<uint32_t> order;  // joins[order[k]] is descriptor k (heaviest first)
     DevBuf desc, unit_off, counts, work;
@@ -106,8 +117,9 @@ struct hyset_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ek0 = nullptr, ek1 = nullptr;
     std::string err;
     std::map<std::tuple<int, double, uint32_t, int>, std::unique_ptr<hs::Bounds>> bounds;
-    // scratch reused across joins
-    hs::DevBuf s_len, s_off, s_tok, s_set, s_pos, s_order, s_altk, s_altv, s_counts, s_scan;
+    // scratch reused across joins; a batch being prepared points sc at its own
+    hs::Scratch own;
+    hs::Scratch* sc = &own;
     hs::DevBuf s_pairs, s_count, s_work, s_stats;
     std::unique_ptr<hs::BatchPlan> batch;
     // technique selector: learned network and/or analytic cost model

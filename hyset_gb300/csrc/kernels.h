@@ -54,6 +54,14 @@ cudaError_t gather_entries(const uint32_t* order, uint64_t n, const uint32_t* e_
 
 cudaError_t iota_u32(uint32_t* out, uint64_t n, cudaStream_t s);
 
+// Sorts n result pairs in place by (first, second) on the device: two stable
+// LSD radix sorts (by second, then by first carrying second), so a result's
+// order no longer depends on the order warps appended it.  first < 2^first_bits,
+// second < 2^second_bits; a, b, c, d hold n words each, scratch
+// radix_scratch_words(n) words.
+cudaError_t sort_pair_list(uint2* pairs, uint64_t n, int first_bits, int second_bits, uint32_t* a, uint32_t* b,
+                           uint32_t* c, uint32_t* d, uint32_t* scratch, cudaStream_t s);
+
 // Input contract check of an uploaded collection.  flags[0] gets bit 1 for an
 // empty set, 2 for a set whose tokens are not strictly ascending, 4 for a size
 // smaller than the previous set's, 8 for a set reaching past n_tokens;

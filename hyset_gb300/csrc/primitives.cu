@@ -454,6 +454,44 @@ cudaError_t iota_u32(uint32_t* out, uint64_t n, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+namespace {
+
+__global__ void k_split_pairs(const uint2* __restrict__ pairs, uint64_t n, uint32_t* __restrict__ first,
+                              uint32_t* __restrict__ second) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint2 p = pairs[i];
+        first[i] = p.x;
+        second[i] = p.y;
+    }
+}
+
+__global__ void k_zip_pairs(const uint32_t* __restrict__ first, const uint32_t* __restrict__ second, uint64_t n,
+                            uint2* __restrict__ pairs) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        pairs[i] = make_uint2(first[i], second[i]);
+}
+
+}  // namespace
+
+cudaError_t sort_pair_list(uint2* pairs, uint64_t n, int first_bits, int second_bits, uint32_t* a, uint32_t* b,
+                           uint32_t* c, uint32_t* d, uint32_t* scratch, cudaStream_t s) {
+    if (n <= 1) return cudaSuccess;
+    note_launches();
+    k_split_pairs<<<grid_for(n, 256), 256, 0, s>>>(pairs, n, a, b);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // keys = second, values = first; then keys = first, values = second (stable)
+    e = radix_sort_pairs(b, a, c, d, n, second_bits < 1 ? 1 : second_bits, scratch, s);
+    if (e != cudaSuccess) return e;
+    e = radix_sort_pairs(a, b, c, d, n, first_bits < 1 ? 1 : first_bits, scratch, s);
+    if (e != cudaSuccess) return e;
+    note_launches();
+    k_zip_pairs<<<grid_for(n, 256), 256, 0, s>>>(a, b, n, pairs);
+    return cudaGetLastError();
+}
+
 cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s) {
     if (c.n == 0) return cudaSuccess;
     note_launches();
