@@ -38,7 +38,7 @@ class JoinOpts(C.Structure):
                 ("count_only", C.c_uint32), ("verify_mode", C.c_uint32), ("sort_pairs", C.c_uint32),
                 ("pair_capacity", C.c_uint64), ("device_pairs", C.c_uint32), ("collect_stats", C.c_uint32),
                 ("probe_begin", C.c_uint32), ("probe_end", C.c_uint32), ("probe_major", C.c_uint32),
-                ("fgss_batch", C.c_uint32)]
+                ("fgss_batch", C.c_uint32), ("orientation", C.c_uint32)]
 
 
 class Block(C.Structure):

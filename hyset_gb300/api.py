@@ -32,18 +32,26 @@ class JoinResult:
     selector: str = "explicit"  # which selector chose the technique
 
 
+# R-S joins: which collection is indexed (hyset_join_opts.orientation)
+ORIENTATION = {"auto": 0, "as_given": 1, "swapped": 2}
+
+
 def make_opts(threshold: float = 0.8, sim: str = "jaccard", technique: str = "auto", bitmap: int = 0,
               count_only: bool = False, verify_mode: int = 0, sort_pairs: bool = False,
               pair_capacity: int = 0, device_pairs: bool = False, collect_stats: bool = False,
-              probe_range=None, probe_major: bool = False, fgss_batch: int = 0) -> JoinOpts:
+              probe_range=None, probe_major: bool = False, fgss_batch: int = 0,
+              orientation: str = "auto") -> JoinOpts:
     if sim not in SIM:
         raise ValueError(f"unknown similarity {sim!r}")
     if technique not in TECH:
         raise ValueError(f"unknown technique {technique!r}")
+    if orientation not in ORIENTATION:
+        raise ValueError(f"unknown orientation {orientation!r}")
     return JoinOpts(SIM[sim], float(threshold), TECH[technique], int(bitmap), int(bool(count_only)),
                     int(verify_mode), int(bool(sort_pairs)), int(pair_capacity), int(bool(device_pairs)),
                     int(bool(collect_stats)), int(probe_range[0]) if probe_range else 0,
-                    int(probe_range[1]) if probe_range else 0, int(bool(probe_major)), int(fgss_batch))
+                    int(probe_range[1]) if probe_range else 0, int(bool(probe_major)), int(fgss_batch),
+                    ORIENTATION[orientation])
 
 
 def _take_result(lib, r) -> JoinResult:

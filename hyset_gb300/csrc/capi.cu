@@ -151,11 +151,18 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
 
 // Per-collection size metadata, built once at upload: sets per size and
 // first_ge[l] = first id with size >= l (l in [0, max_size + 1]).
+// Host size statistics from the host copy of the sizes: the per-size histogram
+// and first_ge[l] = first set id with size >= l (sizes are non-decreasing),
+// whose device copy is enqueued on the stream (the host array is a member, so
+// no synchronisation is needed here).
 hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c) {
-    const uint32_t L = c->max_size;
+    uint32_t L = 0;
+    for (uint32_t v : c->h_sizes) L = std::max(L, v);
+    c->max_size = L;
     c->size_hist.assign((size_t)L + 1, 0);
     for (uint32_t v : c->h_sizes) c->size_hist[v]++;
-    std::vector<uint32_t> f((size_t)L + 2);
+    std::vector<uint32_t>& f = c->h_first_ge;
+    f.resize((size_t)L + 2);
     uint64_t run = 0;
     for (uint32_t l = 0; l <= L + 1; ++l) {
         f[l] = (uint32_t)run;
@@ -163,7 +170,6 @@ hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c) {
     }
     CK(c->first_ge.ensure(f.size() * 4, ctx->stream));
     CK(cudaMemcpyAsync(c->first_ge.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));  // f goes out of scope
     return HYSET_OK;
 }
 
@@ -304,6 +310,7 @@ hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
         o->bitmap_bits != 512)
         return fail(ctx, HYSET_E_INVALID, "bitmap_bits must be 0, 64, 128, 256 or 512");
     if (o->verify_mode > 2) return fail(ctx, HYSET_E_INVALID, "verify_mode must be 0, 1 or 2");
+    if (o->orientation > 2) return fail(ctx, HYSET_E_INVALID, "orientation must be 0, 1 or 2");
     return HYSET_OK;
 }
 
@@ -358,6 +365,19 @@ hyset_status sort_device_pairs(hyset_ctx* ctx, uint2* pairs, uint64_t n, uint32_
     return HYSET_OK;
 }
 
+// R-S joins are symmetric in the two collections (the bounds take the larger
+// and smaller size of a pair, both sides keep maxprefix tokens), so the
+// collections' roles may be exchanged: the indexed side is the smaller one
+// (a cheaper index build) and the probe side the larger one (more work units
+// for the persistent launch).  Output pairs are written back in the caller's
+// (probe, indexed) order.  Probe ranges shard the caller's probe side and keep
+// the given orientation.
+bool swap_sides(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o) {
+    if (R == S || o->probe_end) return false;
+    if (o->orientation == 2) return true;
+    return o->orientation == 0 && S->n < R->n;
+}
+
 // Runs one configured join launch into the context's pair buffer, growing the
 // buffer and re-running when the first pass overflowed.
 hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const hyset_join_opts* o,
@@ -406,7 +426,9 @@ hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const h
         cap = count + count / 8 + 1024;  // overflow: retry once with room for everything
         if (attempt == 1) return fail(ctx, HYSET_E_OVERFLOW, "pair buffer overflow after resize");
     }
-    if (!count_only && o->sort_pairs) ST(sort_device_pairs(ctx, ctx->s_pairs.as<uint2>(), res->count, P.S.n, P.R.n));
+    if (!count_only && o->sort_pairs)
+        ST(sort_device_pairs(ctx, ctx->s_pairs.as<uint2>(), res->count, P.out.swap ? P.R.n : P.S.n,
+                             P.out.swap ? P.S.n : P.R.n));
     if (!count_only && o->device_pairs) {
         if (o->sort_pairs) CK(cudaStreamSynchronize(s));  // device pairs are final when the call returns
         res->device_pairs = ctx->s_pairs.p;
@@ -664,6 +686,8 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
 
 hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, hyset_result* res) {
     ST(check_opts(ctx, o));
+    const bool swapped = swap_sides(R, S, o);
+    if (swapped) std::swap(R, S);
     const bool self = (S == R);
     const uint32_t L = std::max(R->max_size, S->max_size);
     Bounds* b = nullptr;
@@ -696,6 +720,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     P.p_hi = o->probe_end ? o->probe_end : S->n;
     P.r_lo = 0;
     P.r_hi = R->n;
+    P.out.swap = swapped ? 1 : 0;
     const bool token_major = tech == HYSET_TECH_FGSS && L < 65536 && !tn.probe_major;
     uint64_t group_entries = 0;
     TokenJoinParams T{};
@@ -754,31 +779,34 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     return HYSET_OK;
 }
 
+// Validates an uploaded collection and derives its metadata.  The device
+// check (one pass over the tokens, which also writes the meta pairs) is
+// enqueued behind the caller's copies; with host sizes the histogram work runs
+// on the host while the copies are in flight, and one synchronisation ends it.
 hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
     cudaStream_t s = ctx->stream;
     c->h_sizes.resize(c->n);
-    if (c->n) {
-        if (h_sizes_or_null) std::memcpy(c->h_sizes.data(), h_sizes_or_null, (size_t)c->n * 4);
-        else CK(cudaMemcpyAsync(c->h_sizes.data(), c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
-    }
-    DevBuf flags;
-    CK(flags.ensure(16, s));
-    CK(cudaMemsetAsync(flags.p, 0, 16, s));
+    if (c->n && !h_sizes_or_null)
+        CK(cudaMemcpyAsync(c->h_sizes.data(), c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
+    CK(ctx->s_flags.ensure(16, s));
+    CK(cudaMemsetAsync(ctx->s_flags.p, 0, 16, s));
     CK(c->meta.ensure((size_t)c->n * sizeof(uint2) + 8, s));
-    CK(validate_collection(c->view(), c->n_tokens, flags.as<uint32_t>(), s));
+    CK(validate_collection(c->view(), c->n_tokens, ctx->s_flags.as<uint32_t>(), c->meta.as<uint2>(), s));
     uint32_t f[2] = {0, 0};
-    CK(cudaMemcpyAsync(f, flags.p, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+    if (c->n && h_sizes_or_null) {
+        std::memcpy(c->h_sizes.data(), h_sizes_or_null, (size_t)c->n * 4);
+        ST(build_size_meta(ctx, c));
+    }
     CK(cudaStreamSynchronize(s));
-    flags.release(s);
     if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
     if (f[0] & 1) return fail(ctx, HYSET_E_INVALID, "empty set in collection");
     if (f[0] & 2) return fail(ctx, HYSET_E_INVALID, "set tokens must be strictly ascending");
     if (f[0] & 4) return fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size");
     if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
     c->universe = c->n ? f[1] + 1 : 1;
-    c->max_size = c->n ? c->h_sizes.back() : 0;
-    CK(build_meta(c->view(), c->meta.as<uint2>(), s));
-    return build_size_meta(ctx, c);
+    if (!h_sizes_or_null || !c->n) ST(build_size_meta(ctx, c));
+    return HYSET_OK;
 }
 
 // ---------------------------------------------------------------- batches
@@ -854,6 +882,8 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         bj->self = bj->S == bj->R;
         bj->o = d.opts;
         ST(check_opts(ctx, &bj->o));
+        bj->swapped = swap_sides(bj->R, bj->S, &bj->o);
+        if (bj->swapped) std::swap(bj->R, bj->S);
         const hyset_join_opts* o = &bj->o;
         hyset_coll* R = bj->R;
         hyset_coll* S = bj->S;
@@ -866,6 +896,12 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         ST(select_technique(ctx, R, S, o, &selected, &selector));
         Tuned tn = tune(R, S, o, selected);
         tn.probe_major = 1;  // the batched kernel runs the probe-major form
+        {
+            const uint32_t a_lo = o->probe_end ? o->probe_begin : 0, a_hi = o->probe_end ? o->probe_end : S->n;
+            if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && tn.tech == HYSET_TECH_FGSS &&
+                a_hi - a_lo >= TUNE_MIN_PROBES)
+                ST(autotune_bits(ctx, R, S, o, bj->b, bj->self, a_lo, a_hi, &tn.bits));
+        }
         bj->tech = tn.tech;
         bj->ktech = tn.tech == HYSET_TECH_FGSS ? TECH_FGSS : (tn.tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
         bj->words = (int)(tn.bits / 64);
@@ -945,7 +981,8 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         ordered[k] = desc[j];
         BatchJoin& bj = *plan->joins[j];
         ordered[k].P.out = Sink{bj.o.count_only ? nullptr : bj.pairs.as<uint2>(),
-                                plan->counts.as<unsigned long long>() + j, bj.cap, bj.o.count_only ? 1 : 0};
+                                plan->counts.as<unsigned long long>() + j, bj.cap, bj.o.count_only ? 1 : 0,
+                                bj.swapped ? 1 : 0};
         unit_off[k + 1] = unit_off[k] + bj.units;
     }
     CK(plan->desc.ensure(n * sizeof(BatchDesc), s));
@@ -1032,7 +1069,7 @@ void hyset_destroy(hyset_ctx* ctx) {
         batch_release(ctx);
         for (auto& kv : ctx->bounds) kv.second->dev.release(s);
         ctx->own.release(s);
-        DevBuf* bufs[] = {&ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats,
+        DevBuf* bufs[] = {&ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats, &ctx->s_flags,
                           &ctx->d_mlp, &ctx->d_feat, &ctx->d_moments, &ctx->d_hist};
         for (DevBuf* b : bufs) b->release(s);
         cudaStreamSynchronize(s);
@@ -1201,12 +1238,13 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
             // the join's buffer overflowed: run it alone with room for every pair
             hyset_join_opts o2 = bj.o;
             o2.pair_capacity = counts[j] + 1024;
-            st = do_join(ctx, bj.R, bj.S, &o2, r);
+            st = do_join(ctx, bj.swapped ? bj.S : bj.R, bj.swapped ? bj.R : bj.S, &o2, r);
             continue;
         }
         if (bj.o.count_only) continue;
         if (bj.o.sort_pairs) {
-            st = sort_device_pairs(ctx, bj.pairs.as<uint2>(), counts[j], bj.S->n, bj.R->n);
+            st = sort_device_pairs(ctx, bj.pairs.as<uint2>(), counts[j], bj.swapped ? bj.R->n : bj.S->n,
+                                   bj.swapped ? bj.S->n : bj.R->n);
             if (st != HYSET_OK) break;
         }
         if (bj.o.device_pairs) {

@@ -77,6 +77,7 @@ struct Sink {
     unsigned long long* count;
     unsigned long long cap;
     int count_only;
+    int swap;  // store (second, first): an R-S join run with the collections' roles exchanged
 };
 
 // Warp-aggregated append; every lane of the warp must call it.
@@ -89,7 +90,7 @@ __device__ __forceinline__ void emit(const Sink& out, bool want, uint32_t first,
     base = __shfl_sync(FULL, base, leader);
     if (want && !out.count_only) {
         unsigned long long pos = base + __popc(m & lanemask_lt(lane));
-        if (pos < out.cap) out.pairs[pos] = make_uint2(first, second);
+        if (pos < out.cap) out.pairs[pos] = out.swap ? make_uint2(second, first) : make_uint2(first, second);
     }
 }
 

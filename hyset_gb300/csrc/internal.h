@@ -75,6 +75,7 @@ struct BatchJoin {
     hyset_coll* R = nullptr;
     hyset_coll* S = nullptr;
     bool self = false;
+    bool swapped = false;  // R-S join run with the roles exchanged (R, S are the kernel's roles)
     hyset_join_opts o{};
     Bounds* b = nullptr;
     Index ix;
@@ -86,8 +87,6 @@ struct BatchJoin {
     uint32_t units = 0;
 };
 
-// A captured batch: signature (collections and options), per-join buffers,
-// device descriptors, and the instantiated graph of its device work.
 // Scratch of an index build (prefix lengths and offsets, entries, radix sort
 // ping-pong buffers, token counts, scan/sort scratch).
 struct Scratch {
@@ -98,6 +97,8 @@ struct Scratch {
     }
 };
 
+// A captured batch: signature (collections and options), per-join buffers,
+// device descriptors, and the instantiated graph of its device work.
 struct BatchPlan {
     std::vector<std::string> sig;
     Scratch sc;  // owned by the plan: its graph holds these addresses
@@ -120,7 +121,7 @@ struct hyset_ctx {
     // scratch reused across joins; a batch being prepared points sc at its own
     hs::Scratch own;
     hs::Scratch* sc = &own;
-    hs::DevBuf s_pairs, s_count, s_work, s_stats;
+    hs::DevBuf s_pairs, s_count, s_work, s_stats, s_flags;
     std::unique_ptr<hs::BatchPlan> batch;
     // technique selector: learned network and/or analytic cost model
     bool has_mlp = false, has_cost = false;
@@ -145,6 +146,7 @@ struct hyset_coll {
     std::vector<uint32_t> h_sizes;
     std::vector<uint64_t> size_hist;  // sets per size, [max_size+1]
     hs::DevBuf first_ge;              // [max_size+2] first id with size >= l
+    std::vector<uint32_t> h_first_ge; // host copy (source of the device copy)
     hs::Index index;
     hs::DevBuf g_off, g_set, g_ps, g_cursor;  // token groups of the prefix entries (token-major join)
     std::map<int, hs::DevBuf> bitmaps;  // by words

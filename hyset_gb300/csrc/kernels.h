@@ -66,10 +66,8 @@ cudaError_t sort_pair_list(uint2* pairs, uint64_t n, int first_bits, int second_
 // empty set, 2 for a set whose tokens are not strictly ascending, 4 for a size
 // smaller than the previous set's, 8 for a set reaching past n_tokens;
 // flags[1] gets the largest token (atomicMax).  flags must be zeroed first.
-cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s);
-
-// meta[i] = (starts[i], sizes[i]).
-cudaError_t build_meta(CollView c, uint2* meta, cudaStream_t s);
+// The same pass writes meta[i] = (starts[i], sizes[i]).
+cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, cudaStream_t s);
 
 // XOR bitmap signatures, bit (token mod bits) per token
 // (include/hyset/device_algorithms.hpp:58-74), words = bits / 64 in {1,2,4,8}.

@@ -294,28 +294,33 @@ __global__ void k_bitmaps(CollView c, uint64_t* out) {
     }
 }
 
-__global__ void k_validate(CollView c, uint64_t n_tokens, uint32_t* flags) {
+// One warp per set: checks the input contract and writes the set's (start,
+// size) pair.  The largest token is kept per lane and reduced once per warp, so
+// the kernel makes one atomic per warp, not one per set.
+__global__ void k_validate(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta) {
     const int lane = threadIdx.x & 31;
-    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t f = 0, mx = 0;
     for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < c.n; s += warps) {
-        uint32_t l = c.sizes[s], st = c.starts[s];
-        uint32_t f = 0;
+        const uint32_t l = c.sizes[s], st = c.starts[s];
+        if (lane == 0) meta[s] = make_uint2(st, l);
         if (l == 0) f |= 1;
         if (s > 0 && c.sizes[s - 1] > l) f |= 4;
-        if ((uint64_t)st + l > n_tokens) f |= 8;
-        if (!(f & 8) && l > 0) {
+        if ((uint64_t)st + l > n_tokens) {
+            f |= 8;
+        } else if (l > 0) {
             const uint32_t* t = c.tokens + st;
             for (uint32_t i = lane; i + 1 < l; i += 32)
                 if (t[i] >= t[i + 1]) f |= 2;
-            if (lane == 0) atomicMax(&flags[1], t[l - 1]);
+            if (lane == 0) mx = max(mx, t[l - 1]);
         }
-        if (f) atomicOr(&flags[0], f);
     }
-}
-
-__global__ void k_meta(CollView c, uint2* meta) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < c.n; i += gridDim.x * blockDim.x)
-        meta[i] = make_uint2(c.starts[i], c.sizes[i]);
+    f = __reduce_or_sync(FULL, f);
+    mx = __reduce_max_sync(FULL, mx);
+    if (lane == 0) {
+        if (f) atomicOr(&flags[0], f);
+        atomicMax(&flags[1], mx);
+    }
 }
 
 unsigned grid_for(uint64_t n, unsigned threads, unsigned cap = 152u * 32u) {
@@ -492,17 +497,10 @@ cudaError_t sort_pair_list(uint2* pairs, uint64_t n, int first_bits, int second_
     return cudaGetLastError();
 }
 
-cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, cudaStream_t s) {
+cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, cudaStream_t s) {
     if (c.n == 0) return cudaSuccess;
     note_launches();
-    k_validate<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, n_tokens, flags);
-    return cudaGetLastError();
-}
-
-cudaError_t build_meta(CollView c, uint2* meta, cudaStream_t s) {
-    if (c.n == 0) return cudaSuccess;
-    note_launches();
-    k_meta<<<grid_for(c.n, 256), 256, 0, s>>>(c, meta);
+    k_validate<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, n_tokens, flags, meta);
     return cudaGetLastError();
 }
 

@@ -1,12 +1,15 @@
 """Technique selector: a small FP32 network trained on timings this library measures.
 
-    python -m hyset_gb300.selector train [--out DIR] [--collections 80] [--train 64]
+    python -m hyset_gb300.selector train [--out DIR] [--collections 80] [--train 64] [--rs 80]
 
 The reference chooses a GPU technique per partition pair with an analytic linear
 cost model whose coefficients it does not ship (include/hyset/cost.hpp:28-58,
 src/cost_model.cu:296-323).  Here:
   1. a seeded grid of collections (Zipf s in [0.6, 1.4], mean set size in
-     [10, 300], n in [50k, 1M], threshold in [0.5, 0.95]) is generated;
+     [10, 300], n in [50k, 1M] and [1k, 50k], threshold in [0.5, 0.95], Jaccard,
+     cosine or dice) is generated for self-joins, and a grid of R-S joins
+     (one collection split in two, |R|/|S| in [1/50, 1], 2k-400k sets in
+     all) in the orientation the library runs them (the smaller side indexed);
   2. each join is timed on the GPU with each technique (bitmap, fgss,
      direct-verify), on evenly spread probe ranges, extrapolated to the whole
      probe set, plus the technique's full-size preparation (index build,
@@ -62,8 +65,13 @@ def install_shipped(ctx, path: str = WEIGHTS):
 
 # ------------------------------------------------------------------ training data
 
-def grid(n_collections: int, seed: int = 2024, n_lo: int = 50_000, n_hi: int = 1_000_000):
-    """Seeded grid configurations (ordered; the last ones are held out)."""
+SIMS = ["jaccard", "cosine", "dice"]
+
+
+def grid(n_collections: int, seed: int = 2024, n_lo: int = 50_000, n_hi: int = 1_000_000, rs: bool = False):
+    """Seeded grid configurations (ordered; the last ones are held out).  With
+    rs=True each configuration is an R-S join: n_sets in all, split so that the
+    smaller side holds r_frac of them."""
     rng = np.random.default_rng(seed)
     out = []
     while len(out) < n_collections:
@@ -71,10 +79,14 @@ def grid(n_collections: int, seed: int = 2024, n_lo: int = 50_000, n_hi: int = 1
         mean = math.exp(rng.uniform(math.log(10), math.log(300)))
         if n * mean > 8e7:  # keep every collection within a few hundred MB
             continue
-        out.append(dict(n_sets=n, mean=mean, zipf=float(rng.uniform(0.6, 1.4)),
-                        tau=round(float(rng.uniform(0.5, 0.95)), 3),
-                        universe=int(math.exp(rng.uniform(math.log(50_000), math.log(1_000_000)))),
-                        seed=int(rng.integers(1, 2**31))))
+        cfg = dict(n_sets=n, mean=mean, zipf=float(rng.uniform(0.6, 1.4)),
+                   tau=round(float(rng.uniform(0.5, 0.95)), 3),
+                   universe=int(math.exp(rng.uniform(math.log(50_000), math.log(1_000_000)))),
+                   seed=int(rng.integers(1, 2**31)), sim=SIMS[int(rng.integers(0, 3))])
+        if rs:
+            ratio = math.exp(rng.uniform(math.log(1 / 50), 0.0))  # |R| / |S|
+            cfg["r_frac"] = ratio / (1.0 + ratio)
+        out.append(cfg)
     return out
 
 
@@ -87,6 +99,23 @@ def make_collection(cfg):
     return synth.generate(synth.C2, **spec)
 
 
+def split_collection(c, frac, seed):
+    """(R, S) host triples (tokens, starts, sizes): each set of c goes to R with
+    probability frac, so near-duplicates land on both sides."""
+    side = np.random.default_rng(seed).random(c.n) < frac
+    out = []
+    for mask in (side, ~side):
+        ids = np.nonzero(mask)[0]
+        sizes = c.sizes[ids]
+        starts = np.zeros(len(ids), np.uint32)
+        if len(ids):
+            starts[1:] = np.cumsum(sizes[:-1])
+        sz = sizes.astype(np.int64)
+        src = np.repeat(c.starts[ids].astype(np.int64) - starts.astype(np.int64), sz) + np.arange(int(sz.sum()))
+        out.append((c.tokens[src], starts, sizes))
+    return out
+
+
 def _chunks(n, k, per):
     """k evenly spread probe ranges of `per` probes."""
     per = max(1, min(per, n // k if n >= k else n))
@@ -94,28 +123,29 @@ def _chunks(n, k, per):
     return [(int(s), int(s) + per) for s in starts]
 
 
-def time_techniques(ctx, coll, n, tau, window_pairs, sample_probes=48_000, k=8, pair_budget=2e7):
+def time_techniques(join, n, window_pairs, sample_probes=48_000, k=8, pair_budget=2e7):
     """Estimated whole-join milliseconds per technique, for the whole probe
-    range and for its two halves: {part: [bitmap, fgss, direct]}.  The
-    enumeration techniques sample fewer probes where length windows are long
-    (about pair_budget length-compatible pairs per chunk)."""
+    range and for its two halves: {part: [bitmap, fgss, direct]}.  `join(probe_range,
+    **kw)` runs the join over a probe range of its n probes.  The enumeration
+    techniques sample fewer probes where length windows are long (about
+    pair_budget length-compatible pairs per chunk)."""
     half = n // 2
     est = {"all": [], "low": [], "high": []}
     per_probe = max(1.0, window_pairs / max(n, 1))
     for tech in TECHNIQUES:
         per = sample_probes // k if tech == "fgss" else int(max(1, min(sample_probes // k, pair_budget / per_probe)))
         chunks = _chunks(n, k, per)
-        kw = dict(threshold=tau, technique=tech, device_pairs=True, count_only=False)
+        kw = dict(technique=tech, device_pairs=True, count_only=False)
         if tech == "fgss":
             kw.update(probe_major=True)
         # preparation of the whole collection (index build / signatures) from a one-probe call
-        r0 = ctx.self_join(coll, probe_range=(n - 1, n), **kw)
+        r0 = join((n - 1, n), **kw)
         prep = max(0.0, r0.device_ms - r0.kernel_ms)
         ks = []
         for lo, hi in chunks:
             best = None
             for _ in range(2):
-                r = ctx.self_join(coll, probe_range=(lo, hi), **kw)
+                r = join((lo, hi), **kw)
                 best = r.kernel_ms if best is None else min(best, r.kernel_ms)
             ks.append((lo, hi, best))
         for part, (plo, phi) in (("all", (0, n)), ("low", (0, half)), ("high", (half, n))):
@@ -127,23 +157,41 @@ def time_techniques(ctx, coll, n, tau, window_pairs, sample_probes=48_000, k=8, 
     return est
 
 
-def collect(ctx, cfgs, log=print):
+def collect(ctx, cfgs, log=print, first_id=0):
+    """Features and per-technique times of every configuration: a self-join,
+    or (cfg with r_frac) an R-S join with the smaller side indexed."""
     rows = []
     for i, cfg in enumerate(cfgs):
         t0 = time.time()
         c = make_collection(cfg)
-        coll = ctx.upload(c.tokens, c.sizes, c.starts)
-        n = c.n
+        sim, tau = cfg.get("sim", "jaccard"), cfg["tau"]
+        if "r_frac" in cfg:
+            (rt, rs_, rz), (st, ss, sz) = split_collection(c, cfg["r_frac"], cfg["seed"] + 1)
+            R, S = ctx.upload(rt, rz, rs_), ctx.upload(st, sz, ss)
+            n = S.n
+
+            def join(pr, **kw):
+                return ctx.rs_join(R, S, threshold=tau, sim=sim, probe_range=pr, orientation="as_given", **kw)
+            colls = [R, S]
+        else:
+            R = S = ctx.upload(c.tokens, c.sizes, c.starts)
+            n = c.n
+
+            def join(pr, **kw):
+                return ctx.self_join(R, threshold=tau, sim=sim, probe_range=pr, **kw)
+            colls = [R]
         feats = {}
         for part, rng_ in (("all", None), ("low", (0, n // 2)), ("high", (n // 2, n))):
-            f, base = ctx.features(coll, threshold=cfg["tau"], probe_range=rng_)
+            f, base = ctx.features(R, None if S is R else S, threshold=tau, sim=sim, probe_range=rng_)
             feats[part] = (f.tolist(), base.tolist())
-        times = time_techniques(ctx, coll, n, cfg["tau"], feats["all"][1][6])
+        times = time_techniques(join, n, feats["all"][1][6])
         for part in ("all", "low", "high"):
-            rows.append(dict(collection=i, part=part, cfg=cfg, features=feats[part][0], base=feats[part][1],
-                             ms=times[part]))
-        coll.free()
-        log(f"[{i + 1}/{len(cfgs)}] n={n} mean={cfg['mean']:.0f} zipf={cfg['zipf']:.2f} tau={cfg['tau']} "
+            rows.append(dict(collection=first_id + i, part=part, cfg=cfg, features=feats[part][0],
+                             base=feats[part][1], ms=times[part]))
+        for x in colls:
+            x.free()
+        kind = f"R-S {R.n}x{S.n}" if "r_frac" in cfg else f"self n={n}"
+        log(f"[{i + 1}/{len(cfgs)}] {kind} mean={cfg['mean']:.0f} zipf={cfg['zipf']:.2f} {sim} tau={tau} "
             f"ms(bitmap,fgss,direct)={[round(x, 3) for x in times['all']]} ({time.time() - t0:.1f}s)")
     return rows
 
@@ -221,34 +269,42 @@ def main(argv=None):
     ap.add_argument("--small", type=int, default=40,
                     help="extra collections with 1k-50k sets (the batched R-S joins' range)")
     ap.add_argument("--small-train", type=int, default=32)
+    ap.add_argument("--rs", type=int, default=80, help="R-S joins (2k-400k sets split in two)")
+    ap.add_argument("--rs-train", type=int, default=56)
     args = ap.parse_args(argv)
     from .api import Context
     ctx = Context(0, selector=False)
     cfgs = grid(args.collections)
     small = grid(args.small, seed=4048, n_lo=1_000, n_hi=50_000)
-    rows = collect(ctx, cfgs + small)
-    big_ids = set(range(args.collections))
-    is_train = lambda r: (r["collection"] < args.train if r["collection"] in big_ids
-                          else r["collection"] - args.collections < args.small_train)
-    tr = [r for r in rows if is_train(r)]
-    te = [r for r in rows if not is_train(r)]
+    rs = grid(args.rs, seed=6072, n_lo=2_000, n_hi=400_000, rs=True)
+    rows = collect(ctx, cfgs + small + rs)
+    nb, ns = args.collections, args.small
+    family = lambda r: "grid" if r["collection"] < nb else ("small" if r["collection"] < nb + ns else "rs")
+    is_train = lambda r: {"grid": r["collection"] < args.train,
+                          "small": r["collection"] - nb < args.small_train,
+                          "rs": r["collection"] - nb - ns < args.rs_train}[family(r)]
+    for r in rows:
+        r["family"], r["train"] = family(r), bool(is_train(r))
+    tr = [r for r in rows if r["train"]]
+    te = [r for r in rows if not r["train"]]
     params, mean, scale, trace = train(ctx, tr, steps=args.steps)
     coefs = fit_cost_model(tr)
-    whole = lambda rs: [r for r in rs if r["part"] == "all"]
-    report = {"held_out": evaluate(ctx, params, mean, scale, coefs, whole(te)),
-              "held_out_grid_50k_1m": evaluate(ctx, params, mean, scale, coefs,
-                                               [r for r in whole(te) if r["collection"] in big_ids]),
-              "held_out_small_1k_50k": evaluate(ctx, params, mean, scale, coefs,
-                                                [r for r in whole(te) if r["collection"] not in big_ids]),
-              "held_out_partitions": evaluate(ctx, params, mean, scale, coefs, te),
+    whole = lambda rs_: [r for r in rs_ if r["part"] == "all"]
+    ev = lambda sel: evaluate(ctx, params, mean, scale, coefs, sel)
+    report = {"held_out": ev(whole(te)),
+              "held_out_grid_50k_1m": ev([r for r in whole(te) if family(r) == "grid"]),
+              "held_out_small_1k_50k": ev([r for r in whole(te) if family(r) == "small"]),
+              "held_out_rs": ev([r for r in whole(te) if family(r) == "rs"]),
+              "held_out_partitions": ev(te),
               "train": evaluate(ctx, params, mean, scale, coefs, whole(tr)),
               "final_loss": float(trace[-1]) if len(trace) else None, "first_loss": float(trace[0])}
     os.makedirs(args.out, exist_ok=True)
     with open(os.path.join(args.out, "selector_weights.json"), "w") as f:
         json.dump({"params": params.tolist(), "mean": mean.tolist(), "scale": scale.tolist(),
                    "cost": coefs.ravel().tolist(), "techniques": TECHNIQUES,
-                   "trained_on": args.train + args.small_train,
-                   "held_out": args.collections - args.train + args.small - args.small_train, "report": report}, f)
+                   "trained_on": args.train + args.small_train + args.rs_train,
+                   "held_out": nb - args.train + ns - args.small_train + args.rs - args.rs_train,
+                   "report": report}, f)
     with open(os.path.join(args.out, "selector_samples.json"), "w") as f:
         json.dump(rows, f)
     print(json.dumps(report, indent=1))

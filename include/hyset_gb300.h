@@ -79,6 +79,10 @@ typedef struct {
                                   per probe batch), 0 = token-major kernel (token groups in shared
                                   memory).  AUTO always uses probe-major; probe ranges need it */
     uint32_t fgss_batch;       /* probe-major FGSS: probes per warp batch (1..32); 0 = tuned default */
+    uint32_t orientation;      /* R-S joins: 0 = automatic (index the smaller collection, probe the
+                                  larger), 1 = as given, 2 = swapped.  The result is the same pair
+                                  set in every orientation, pairs always (probe id, indexed id) of
+                                  the caller's collections; probe ranges keep the given orientation */
 } hyset_join_opts;
 
 typedef struct hyset_ctx hyset_ctx;

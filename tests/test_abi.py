@@ -55,4 +55,4 @@ def test_synth_header_and_library_agree():
 def test_struct_layouts_match_header():
     import hyset_gb300._lib as L
     assert ctypes.sizeof(L.Block) == 32
-    assert ctypes.sizeof(L.JoinOpts) == 72
+    assert ctypes.sizeof(L.JoinOpts) == 80

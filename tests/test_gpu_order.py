@@ -45,20 +45,33 @@ def test_sorted_pairs_are_the_oracle_pairs_in_order(ctx, kw):
     exp = want[np.lexsort((want[:, 1], want[:, 0]))]
     r1 = ctx.self_join(coll, threshold=0.6, sort_pairs=True, **kw)
     r2 = ctx.self_join(coll, threshold=0.6, sort_pairs=True, **kw)
-    assert r1.count == len(exp) > 1000
+    assert r1.count == len(exp) > 100
     assert _lexsorted(r1.pairs)
     np.testing.assert_array_equal(r1.pairs, exp)
     np.testing.assert_array_equal(r2.pairs, exp)
 
 
+def _split(c, frac, seed):
+    """Two collections from one (near-duplicates land on both sides)."""
+    side = np.random.default_rng(seed).random(c.n) < frac
+    out = []
+    for mask in (side, ~side):
+        ids = np.nonzero(mask)[0]
+        sizes = c.sizes[ids]
+        starts = np.zeros(len(ids), np.uint32)
+        starts[1:] = np.cumsum(sizes[:-1])
+        tokens = np.concatenate([c.tokens[c.starts[i]:c.starts[i] + c.sizes[i]] for i in ids])
+        out.append((tokens, starts, sizes))
+    return out
+
+
 def test_sorted_device_pairs_rs_join(ctx):
-    R = synth.generate(synth.C2, n_sets=9000, seed=42)
-    S = synth.generate(synth.C2, n_sets=7000, seed=43)
-    cr = ctx.upload(R.tokens, R.sizes, R.starts)
-    cs = ctx.upload(S.tokens, S.sizes, S.starts)
+    R, S = _split(synth.generate(synth.C2, n_sets=16000, seed=42), 0.55, 43)
+    cr = ctx.upload(R[0], R[2], R[1])
+    cs = ctx.upload(S[0], S[2], S[1])
     r = ctx.rs_join(cr, cs, threshold=0.5, sort_pairs=True, device_pairs=True)
     got = _read_device_pairs(r)
-    exp = oracle.brute_rs((R.tokens, R.starts, R.sizes), (S.tokens, S.starts, S.sizes), 0.5)
+    exp = oracle.brute_rs(R, S, 0.5)
     assert r.count == len(exp) > 0
     assert _lexsorted(got)
     assert oracle.as_set(got) == oracle.as_set(exp)
@@ -100,3 +113,21 @@ def test_freeing_a_collection_drops_its_captured_batch(ctx):
     ub = ctx.upload(b.tokens, b.sizes, b.starts)  # may reuse the freed handle's address
     res = ctx.batch_join([(ub, None, dict(threshold=0.6))])
     assert oracle.as_set(res[0].pairs) == oracle.as_set(oracle.join(b.tokens, b.starts, b.sizes, 0.6))
+
+
+@pytest.mark.parametrize("frac", [0.85, 0.15])
+@pytest.mark.parametrize("sim,tau", [("jaccard", 0.6), ("cosine", 0.7), ("dice", 0.65)])
+def test_rs_orientation_gives_the_same_pairs(ctx, frac, sim, tau):
+    """Indexing either collection of an R-S join yields the same (probe, indexed)
+    pairs; `auto` indexes the smaller one."""
+    R, S = _split(synth.generate(synth.C2, n_sets=16000, seed=44), frac, 45)
+    cr = ctx.upload(R[0], R[2], R[1])
+    cs = ctx.upload(S[0], S[2], S[1])
+    exp = oracle.brute_rs(R, S, tau, sim=sim)
+    exp = exp[np.lexsort((exp[:, 1], exp[:, 0]))]
+    assert len(exp) > 0
+    for orient in ("auto", "as_given", "swapped"):
+        for kw in (dict(technique="fgss", probe_major=True), dict(technique="bitmap", bitmap=128),
+                   dict(technique="fgss")):
+            r = ctx.rs_join(cr, cs, threshold=tau, sim=sim, orientation=orient, sort_pairs=True, **kw)
+            np.testing.assert_array_equal(r.pairs, exp, err_msg=f"{orient} {kw}")

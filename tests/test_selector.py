@@ -135,11 +135,7 @@ def test_shipped_report_recomputes_from_samples():
         rows = json.load(f)
     p = np.array(w["params"])
     mean, scale = np.array(w["mean"]), np.array(w["scale"])
-    n_big, n_small = 80, 40
-    train_big, train_small = 64, 32
-    held = [r for r in rows if r["part"] == "all" and
-            ((r["collection"] < n_big and r["collection"] >= train_big) or
-             (r["collection"] >= n_big and r["collection"] - n_big >= train_small))]
+    held = [r for r in rows if r["part"] == "all" and not r["train"]]
     assert len(held) == w["held_out"]
     x = (np.array([r["features"] for r in held]) - mean) / scale
     y, _ = mlp.forward(p, x)
