@@ -89,10 +89,12 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
     b->probe_prefix.resize(L + 1);
     b->index_prefix.resize(L + 1);
     b->max_partner.resize(L + 1);
+    b->mid_prefix.resize(L + 1);
     for (uint32_t l = 0; l <= L; ++l) {
         b->minsize[l] = minsize_of(sim, l, tau);
         b->probe_prefix[l] = l ? maxprefix_of(sim, l, tau) : 0;
-        b->index_prefix[l] = l ? (index_maxprefix ? maxprefix_of(sim, l, tau) : midprefix_of(sim, l, tau)) : 0;
+        b->mid_prefix[l] = l ? midprefix_of(sim, l, tau) : 0;
+        b->index_prefix[l] = l ? (index_maxprefix ? b->probe_prefix[l] : b->mid_prefix[l]) : 0;
         if (b->minsize[l] > l) return fail(ctx, HYSET_E_INVALID, "threshold yields minsize > set size");
     }
     uint32_t q = 0;
@@ -115,14 +117,28 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
             for (uint32_t small = b->minsize[big]; small <= big; ++small)
                 b->mo_tab[b->mo_row[big] + (small - b->minsize[big])] = sim_minoverlap(sim, big, small, tau);
         b->mo_sum.assign(1, 0);
+        // non-decreasing along rows (small) and along columns (big)
+        b->mo_monotone = true;
+        for (uint32_t big = 1; big <= L && b->mo_monotone; ++big)
+            for (uint32_t small = b->minsize[big]; small <= big; ++small) {
+                const uint32_t v = b->mo_tab[b->mo_row[big] + (small - b->minsize[big])];
+                if (small > b->minsize[big] && b->mo_tab[b->mo_row[big] + (small - 1 - b->minsize[big])] > v)
+                    b->mo_monotone = false;
+                if (big > 1 && small >= b->minsize[big - 1] && small <= big - 1 &&
+                    b->mo_tab[b->mo_row[big - 1] + (small - b->minsize[big - 1])] > v)
+                    b->mo_monotone = false;
+            }
     } else {
         b->mo_sum.resize(2 * (size_t)L + 1);
         for (uint32_t s = 0; s <= 2 * L; ++s) b->mo_sum[s] = sim_minoverlap(sim, s, 0, tau);
         b->mo_row.assign(1, 0);
         b->mo_tab.assign(1, 0);
+        b->mo_monotone = true;
+        for (uint32_t s = 1; s <= 2 * L; ++s)
+            if (b->mo_sum[s] < b->mo_sum[s - 1]) b->mo_monotone = false;
     }
     // one device allocation holding all tables
-    size_t n32 = 4 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size();
+    size_t n32 = 5 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size();
     size_t bytes = b->mo_row.size() * 8 + n32 * 4;
     CK(b->dev.ensure(bytes, ctx->stream));
     uint8_t* base = b->dev.as<uint8_t>();
@@ -134,23 +150,22 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
         dst = d;
         return cudaMemcpyAsync(d, v.data(), v.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
     };
-    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_sum, *d_tab;
+    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_mid, *d_sum, *d_tab;
     CK(cudaMemcpyAsync(d_row, b->mo_row.data(), b->mo_row.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(put(b->minsize, d_minsize));
     CK(put(b->probe_prefix, d_pp));
     CK(put(b->index_prefix, d_ip));
     CK(put(b->max_partner, d_mp));
+    CK(put(b->mid_prefix, d_mid));
     CK(put(b->mo_sum, d_sum));
     CK(put(b->mo_tab, d_tab));
     CK(cudaStreamSynchronize(ctx->stream));
-    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_sum, d_row, d_tab, L, sim};
+    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_mid, d_sum, d_row, d_tab, L, sim};
     *out = b.get();
     ctx->bounds.emplace(key, std::move(b));
     return HYSET_OK;
 }
 
-// Per-collection size metadata, built once at upload: sets per size and
-// first_ge[l] = first id with size >= l (l in [0, max_size + 1]).
 // Host size statistics from the host copy of the sizes: the per-size histogram
 // and first_ge[l] = first set id with size >= l (sizes are non-decreasing),
 // whose device copy is enqueued on the stream (the host array is a member, so
@@ -198,13 +213,22 @@ int key_bits_for(uint32_t universe) {
 // Global inverted index over the prefix entries of every set, lists ordered by
 // set id: histogram + scan give the list offsets, a stable radix sort by token
 // of the entries (emitted in set order) gives the order inside each list.
-hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, int kind, Index& ix) {
+// pre / d_pre: the prefix length table (default: the bounds' index prefix);
+// force_pb >= 0 fixes the layout (0 = unpacked, > 0 = packed with that many
+// position bits) so that two indexes of one join share it.
+hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, int kind, Index& ix,
+                                const std::vector<uint32_t>* pre = nullptr, const uint32_t* d_pre = nullptr,
+                                int force_pb = -1) {
     // Rebuilt on every join (buffers are reused): a join's timed device work
     // always includes its own index build.  Only asynchronous stream work once
     // the buffers are large enough, so a batch can capture it into a graph.
+    if (!pre) {
+        pre = &b->index_prefix;
+        d_pre = b->view.index_prefix;
+    }
     cudaStream_t s = ctx->stream;
     const uint32_t n = c->n, U = c->universe;
-    const uint64_t E = prefix_entries(c, b->index_prefix);
+    const uint64_t E = prefix_entries(c, *pre);
     if (E >= (1ull << 32)) return fail(ctx, HYSET_E_UNSUPPORTED, "more than 2^32 prefix entries");
     const uint64_t E1 = E ? E : 1;
     CK(ctx->sc->len.ensure((size_t)n * 4 + 4, s));
@@ -226,15 +250,15 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     uint32_t* len = ctx->sc->len.as<uint32_t>();
     uint32_t* off = ctx->sc->off.as<uint32_t>();
     uint32_t* scr = ctx->sc->scan.as<uint32_t>();
-    CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
+    CK(set_prefix_lengths(v, d_pre, 0, n, len, s));
     CK(scan_exclusive(len, off, n, scr, s));
     // Packed entries (set << pb | position) when set ids up to n and positions
     // below the longest prefix fit 32 bits: the sorted values are the index.
     uint32_t max_pre = 1;
     for (size_t l = 0; l < c->size_hist.size(); ++l)
-        if (c->size_hist[l]) max_pre = std::max(max_pre, pre_len(b, (uint32_t)l));
-    const uint32_t pb = bits_for(max_pre), sb = bits_for(n);
-    if (pb + sb <= 32) {
+        if (c->size_hist[l]) max_pre = std::max(max_pre, (*pre)[l]);
+    const uint32_t pb = force_pb > 0 ? (uint32_t)force_pb : bits_for(max_pre), sb = bits_for(n);
+    if (force_pb != 0 && pb + sb <= 32) {
         uint32_t* counts = ctx->sc->counts.as<uint32_t>();
         CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
         CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
@@ -266,6 +290,28 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     ix.universe = U;
     ix.entries = E;
     ix.pos_bits = 0;
+    return HYSET_OK;
+}
+
+// R-S prefix-index joins split each probe's length window in two bands:
+// candidates at least as long as the probe need only the probe's midprefix
+// tokens (against R's maxprefix index), shorter candidates need only their
+// own midprefix entries (a second, midprefix index of R, against the probe's
+// maxprefix tokens).  Both hold because minoverlap does not decrease when
+// either length grows, which get_bounds checks on the bound tables.
+bool use_bands(const Bounds* b, bool self) { return !self && b->mo_monotone; }
+
+// The prefix index (and for banded R-S joins the midprefix index) of R, and
+// their views in P.
+hyset_status build_fgss_indexes(hyset_ctx* ctx, hyset_coll* R, const Bounds* b, bool self, Index& ix,
+                                 Index& ix_mid, JoinParams& P) {
+    ST(build_sorted_index(ctx, R, b, self ? 0 : 1, ix));
+    P.X = ix.view();
+    P.X2 = IndexView{};
+    if (use_bands(b, self)) {
+        ST(build_sorted_index(ctx, R, b, 2, ix_mid, &b->mid_prefix, b->view.mid_prefix, (int)ix.pos_bits));
+        P.X2 = ix_mid.view();
+    }
     return HYSET_OK;
 }
 
@@ -614,9 +660,9 @@ hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
 // Autotuner for the prefix-index join's signature width: on the first AUTO join
 // of a (collections, similarity, threshold), the probe-major kernel runs on
 // three probe samples spread over the probe range with no signatures and with
-// 128- and 256-bit signatures, and the fastest width is kept for that join.
-// Measured on GB300: 256 bits wins on long sets, 128 on short ones, none at
-// high thresholds on some collections.
+// 128-, 256- and 512-bit signatures, and the fastest width is kept for that
+// join.  Measured on GB300: 256 bits wins on long sets at high thresholds, 512
+// on long sets at low thresholds, 128 on short ones, none on some collections.
 constexpr uint32_t TUNE_MIN_PROBES = 20000, TUNE_SAMPLE = 2048;
 
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
@@ -628,8 +674,8 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
         return HYSET_OK;
     }
     cudaStream_t s = ctx->stream;
-    ST(build_sorted_index(ctx, R, b, self ? 0 : 1, R->index));
     JoinParams P{};
+    ST(build_fgss_indexes(ctx, R, b, self, R->index, R->index_mid, P));
     P.R = R->view();
     P.S = S->view();
     P.B = b->view;
@@ -639,15 +685,14 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     P.r_lo = 0;
     P.r_hi = R->n;
     P.grab = 4;
-    P.X = R->index.view();
     CK(ctx->s_count.ensure(16, s));
     CK(ctx->s_work.ensure(16, s));
     P.out = Sink{nullptr, ctx->s_count.as<unsigned long long>(), 0, 1};
     P.work = ctx->s_work.as<unsigned int>();
-    const uint32_t cand[3] = {0, 128, 256};
+    const uint32_t cand[4] = {0, 128, 256, 512};
     float best_ms = 0;
     uint32_t best = 256;
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
         const int words = (int)(cand[k] / 64);
         P.words = words;
         P.bits_R = P.bits_S = nullptr;
@@ -747,8 +792,8 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
         T.self = self ? 1 : 0;
         T.grab = 16;
     } else if (tech == HYSET_TECH_FGSS) {
-        ST(build_sorted_index(ctx, R, b, self ? 0 : 1, R->index));
-        P.X = R->index.view();
+        ST(build_fgss_indexes(ctx, R, b, self, R->index, R->index_mid, P));
+        if (P.X2.set) P.grab = std::min<uint32_t>(P.grab, 16);  // two bands per probe share a warp batch
     }
     const int words = (int)(tn.bits / 64);
     if (words) {
@@ -825,7 +870,8 @@ void batch_release(hyset_ctx* ctx) {
     if (bp.exec) cudaGraphExecDestroy(bp.exec);
     if (bp.graph) cudaGraphDestroy(bp.graph);
     for (auto& bj : bp.joins) {
-        DevBuf* bufs[] = {&bj->ix.list_off, &bj->ix.set, &bj->ix.pos, &bj->bits_r, &bj->bits_s, &bj->pairs};
+        DevBuf* bufs[] = {&bj->ix.list_off, &bj->ix.set, &bj->ix.pos, &bj->ix_mid.list_off, &bj->ix_mid.set,
+                          &bj->ix_mid.pos, &bj->bits_r, &bj->bits_s, &bj->pairs};
         for (DevBuf* d : bufs) d->release(s);
     }
     DevBuf* bufs[] = {&bp.desc, &bp.unit_off, &bp.counts, &bp.work};
@@ -844,7 +890,12 @@ hyset_status batch_record(hyset_ctx* ctx, BatchPlan& bp) {
     CK(cudaMemsetAsync(bp.work.p, 0, 16, s));
     for (auto& bjp : bp.joins) {
         BatchJoin& bj = *bjp;
-        if (bj.ktech == TECH_FGSS) ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix));
+        if (bj.ktech == TECH_FGSS) {
+            ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix));
+            if (use_bands(bj.b, bj.self))
+                ST(build_sorted_index(ctx, bj.R, bj.b, 2, bj.ix_mid, &bj.b->mid_prefix, bj.b->view.mid_prefix,
+                                      (int)bj.ix.pos_bits));
+        }
         if (bj.words) {
             CK(generate_bitmaps(bj.R->view(), bj.words, bj.bits_r.as<uint64_t>(), s));
             if (!bj.self) CK(generate_bitmaps(bj.S->view(), bj.words, bj.bits_s.as<uint64_t>(), s));
@@ -935,6 +986,15 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
             bj->ix.universe = R->universe;
             bj->ix.pos_bits = pb + sb <= 32 ? pb : 0;
             P.X = bj->ix.view();
+            if (use_bands(bj->b, bj->self)) {  // the midprefix index, same layout
+                const uint64_t E2 = prefix_entries(R, bj->b->mid_prefix);
+                CK(bj->ix_mid.list_off.ensure(((size_t)R->universe + 1) * 4, s));
+                CK(bj->ix_mid.set.ensure((E2 ? E2 : 1) * 4, s));
+                CK(bj->ix_mid.pos.ensure((E2 ? E2 : 1) * 4, s));
+                bj->ix_mid.universe = R->universe;
+                bj->ix_mid.pos_bits = bj->ix.pos_bits;
+                P.X2 = bj->ix_mid.view();
+            }
         }
         if (bj->words) {
             CK(bj->bits_r.ensure((size_t)R->n * bj->words * 8 + 8, s));
@@ -947,7 +1007,7 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         if (!o->count_only) CK(bj->pairs.ensure(std::max<uint64_t>(bj->cap, 1) * sizeof(uint2), s));
         desc[j].tech = (uint32_t)bj->ktech;
         desc[j].words = (uint32_t)bj->words;
-        desc[j].unit_probes = bj->ktech == TECH_FGSS ? std::min<uint32_t>(tn.batch, 32) : 1;
+        desc[j].unit_probes = bj->ktech == TECH_FGSS ? std::min<uint32_t>(tn.batch, P.X2.set ? 16 : 32) : 1;
         const uint32_t np = P.p_hi - P.p_lo;
         bj->units = (np + desc[j].unit_probes - 1) / desc[j].unit_probes;
         cost[j] = (double)np * (double)(R->n_tokens / std::max<uint32_t>(R->n, 1) + 1) *
@@ -1170,6 +1230,9 @@ void hyset_collection_free(hyset_ctx* ctx, hyset_coll* c) {
     c->index.list_off.release(s);
     c->index.set.release(s);
     c->index.pos.release(s);
+    c->index_mid.list_off.release(s);
+    c->index_mid.set.release(s);
+    c->index_mid.pos.release(s);
     c->first_ge.release(s);
     c->g_off.release(s);
     c->g_set.release(s);

@@ -32,6 +32,7 @@ struct BoundsView {
     const uint32_t* __restrict__ probe_prefix;  // [L+1]  maxprefix
     const uint32_t* __restrict__ index_prefix;  // [L+1]  midprefix (self-join) or maxprefix (R-S)
     const uint32_t* __restrict__ max_partner;   // [L+1]  largest l with minsize(l) <= len
+    const uint32_t* __restrict__ mid_prefix;    // [L+1]  midprefix
     const uint32_t* __restrict__ mo_sum;        // [2L+1] raw minoverlap by l1+l2 (jaccard, dice)
     const uint64_t* __restrict__ mo_row;        // [L+2]  cosine: row offsets by larger length
     const uint32_t* __restrict__ mo_tab;        // cosine: raw minoverlap at (big, small)

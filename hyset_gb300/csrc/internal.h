@@ -42,7 +42,8 @@ struct Bounds {
     double tau = 0;
     uint32_t L = 0;
     int index_maxprefix = 0;  // 0: index midprefix (self-join), 1: maxprefix (R-S)
-    std::vector<uint32_t> minsize, probe_prefix, index_prefix, max_partner, mo_sum, mo_tab;
+    std::vector<uint32_t> minsize, probe_prefix, index_prefix, max_partner, mid_prefix, mo_sum, mo_tab;
+    bool mo_monotone = false;  // minoverlap non-decreasing in each length (R-S bands are valid)
     std::vector<uint64_t> mo_row;
     DevBuf dev;
     BoundsView view{};
@@ -78,7 +79,7 @@ struct BatchJoin {
     bool swapped = false;  // R-S join run with the roles exchanged (R, S are the kernel's roles)
     hyset_join_opts o{};
     Bounds* b = nullptr;
-    Index ix;
+    Index ix, ix_mid;
     DevBuf bits_r, bits_s, pairs;
     uint64_t cap = 0;
     int words = 0;
@@ -148,6 +149,7 @@ struct hyset_coll {
     hs::DevBuf first_ge;              // [max_size+2] first id with size >= l
     std::vector<uint32_t> h_first_ge; // host copy (source of the device copy)
     hs::Index index;
+    hs::Index index_mid;  // R-S bands: midprefix entries, same layout as index
     hs::DevBuf g_off, g_set, g_ps, g_cursor;  // token groups of the prefix entries (token-major join)
     std::map<int, hs::DevBuf> bitmaps;  // by words
     hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, meta.as<uint2>(), n}; }

@@ -132,12 +132,20 @@ __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
 // (probe, position) are flattened across lanes, then the index entries their
 // inverted lists contribute; every round trip to memory is shared by the whole
 // batch, so a warp keeps several probes' loads in flight at once.
+//
+// Banded R-S joins (P.X2.set != nullptr, k <= 16): lane t < k takes the
+// candidates of probe t at least as long as the probe (its midprefix tokens
+// against the maxprefix index X), lane k + t the shorter ones (its maxprefix
+// tokens against the midprefix index X2).
 template <int VMODE, int W>
 __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
     // lane t < k: probe t of the batch (largest sets first)
-    uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0;
-    if ((uint32_t)lane < k) {
-        p = P.p_hi - 1 - (i0 + (uint32_t)lane);
+    uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
+    const bool banded = P.X2.set != nullptr;
+    const uint32_t t_probe = banded && (uint32_t)lane >= k ? (uint32_t)lane - k : (uint32_t)lane;
+    if (t_probe < k && (banded || (uint32_t)lane < k)) {
+        band = (uint32_t)lane >= k ? 1u : 0u;
+        p = P.p_hi - 1 - (i0 + t_probe);
         const uint2 pm = P.S.meta[p];
         lp = pm.y;
         pst = pm.x;
@@ -145,7 +153,12 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             const Window w = candidate_window(P, p, lp);
             lo = w.lo;
             hi = w.hi;
-            if (lo < hi) mp = P.B.probe_prefix[lp];
+            if (banded) {
+                const uint32_t mid = P.first_ge[min(lp, P.R_L + 1)];  // first candidate with size >= lp
+                if (band == 0) lo = max(lo, mid);
+                else hi = min(hi, mid);
+            }
+            if (lo < hi) mp = banded && band == 0 ? P.B.mid_prefix[lp] : P.B.probe_prefix[lp];
         }
     }
     count_stat(P, 4, mp, lane);  // prefix tokens read by the filter
@@ -160,11 +173,14 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
         const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp);
         const uint32_t t_pst = __shfl_sync(FULL, pst, t);
         const uint32_t t_lo = __shfl_sync(FULL, lo, t), t_hi = __shfl_sync(FULL, hi, t);
+        const uint32_t t_band = __shfl_sync(FULL, band, t);
+        const uint32_t* __restrict__ x_off = t_band ? P.X2.list_off : P.X.list_off;
+        const uint32_t* __restrict__ x_set = t_band ? P.X2.set : P.X.set;
         uint32_t first = 0, cnt = 0;
         if (sv) {
             const uint32_t tok = __ldg(P.S.tokens + t_pst + j);
             if (tok < P.X.universe) {
-                uint32_t b0 = P.X.list_off[tok], b1 = P.X.list_off[tok + 1];
+                uint32_t b0 = x_off[tok], b1 = x_off[tok + 1];
                 if (P.X.sorted) {
                     const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
                     const uint32_t len = b1 - b0;
@@ -173,7 +189,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                         uint32_t v[SHORT_LIST];
 #pragma unroll
                         for (int q = 0; q < (int)SHORT_LIST; ++q)
-                            v[q] = (uint32_t)q < len ? __ldg(P.X.set + b0 + q) : 0xFFFFFFFFu;
+                            v[q] = (uint32_t)q < len ? __ldg(x_set + b0 + q) : 0xFFFFFFFFu;
                         uint32_t nlo = 0, nhi = 0;
 #pragma unroll
                         for (int q = 0; q < (int)SHORT_LIST; ++q) {
@@ -183,8 +199,8 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                         b1 = b0 + nhi;
                         b0 = b0 + nlo;
                     } else {
-                        b0 = lower_bound_u32(P.X.set, b0, b1, klo);
-                        b1 = lower_bound_u32(P.X.set, b0, b1, khi);
+                        b0 = lower_bound_u32(x_set, b0, b1, klo);
+                        b1 = lower_bound_u32(x_set, b0, b1, khi);
                     }
                 }
                 first = b0;
@@ -207,23 +223,27 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             const uint32_t ilp = __shfl_sync(FULL, lp, it);
             const uint32_t ipst = __shfl_sync(FULL, pst, it);
             const uint32_t ilo = __shfl_sync(FULL, lo, it), ihi = __shfl_sync(FULL, hi, it);
+            const uint32_t iband = __shfl_sync(FULL, band, it);
             const uint32_t e = f_jj + ((keep ? q : 0) - (i_jj - c_jj));
             uint32_t c = 0, pc = 0, lc = 0, mo = 0, cstart = 0, pop = 0;
             if (keep) {
-                const uint32_t v = P.X.set[e];
+                const uint32_t v = (iband ? P.X2.set : P.X.set)[e];
                 if (P.X.pos) {
                     c = v;
-                    pc = P.X.pos[e];
+                    pc = (iband ? P.X2.pos : P.X.pos)[e];
                 } else {
                     c = v >> P.X.pos_bits;
                     pc = v & ((1u << P.X.pos_bits) - 1u);
                 }
                 if (!P.X.sorted) keep = c >= ilo && c < ihi;
             }
+            // Signatures up to 256 bits are loaded with the candidate's meta (one
+            // round trip); wider ones only for items that pass the positional
+            // bound (their reads outweigh the extra round trip).
+            constexpr bool early_sig = W > 0 && W <= 4;
             if (keep) {
-                // the candidate's (start, size) and signature depend only on c: issue together
                 const uint2 cm = P.R.meta[c];
-                if constexpr (W > 0) {
+                if constexpr (early_sig) {
                     const uint64_t* bs = P.bits_S + (uint64_t)ip * W;
                     const uint64_t* bc = P.bits_R + (uint64_t)c * W;
 #pragma unroll
@@ -237,6 +257,14 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             }
             count_stat(P, 0, q < total ? 1u : 0u, lane);
             count_stat(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
+            if constexpr (W > 4) {
+                if (keep) {
+                    const uint64_t* bs = P.bits_S + (uint64_t)ip * W;
+                    const uint64_t* bc = P.bits_R + (uint64_t)c * W;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) pop += __popcll(__ldg(bs + w) ^ __ldg(bc + w));
+                }
+            }
             if constexpr (W > 0) keep = keep && ilp + lc - pop >= 2u * mo;
             count_stat(P, 1, keep ? 1u : 0u, lane);
             count_stat(P, 2, keep ? lc : 0u, lane);

@@ -93,6 +93,7 @@ struct JoinParams {
     uint32_t p_lo, p_hi;        // probe ids [p_lo, p_hi)
     uint32_t r_lo, r_hi;        // candidate ids restricted to [r_lo, r_hi)
     IndexView X;                // FGSS only
+    IndexView X2;               // R-S FGSS, banded: midprefix index of R (set == nullptr: no bands)
     const uint64_t* __restrict__ bits_R;    // signatures (nullptr = no bitmap filter)
     const uint64_t* __restrict__ bits_S;
     int words;
