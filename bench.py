@@ -390,6 +390,82 @@ def run_batch(args):
                                  "generation_s": gen_s}}), flush=True)
 
 
+def run_parse(args):
+    """The collection reader (the step before the join): the workload's text
+    form parsed on the GPU, from device memory (`value`) and from pinned host
+    memory (`e2e`, copy included), against the reference reader's restatement
+    on one host core over a bounded sample."""
+    import numpy as np
+    import torch
+    import hyset_gb300 as hs
+    import oracle
+    from hyset_gb300 import synth
+    c = make_workload(args.sets or None)
+    n_bytes = int(hs_text_bytes(c))
+    pinned = torch.empty(n_bytes, dtype=torch.uint8).pin_memory()
+    text = synth.format_text(c.tokens, c.starts, c.sizes, out=pinned.numpy())
+    assert text.size == n_bytes
+    ctx = hs.Context(0)
+    d_text = torch.empty(n_bytes, dtype=torch.uint8, device="cuda")
+    d_text.copy_(pinned)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    dev_s, e2e_s = [], []
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        coll = ctx.parse((d_text.data_ptr(), n_bytes))
+        dt = time.perf_counter() - t0
+        if i == 0:
+            tk, _, sz = coll.download()
+            assert np.array_equal(tk, c.tokens) and np.array_equal(sz, c.sizes), "parse differs from the generator"
+        coll.free()
+        if i >= args.warmup:
+            dev_s.append(dt)
+    for i in range(args.warmup + args.steps):
+        flush.fill_(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        coll = ctx.parse(text)
+        dt = time.perf_counter() - t0
+        coll.free()
+        if i >= args.warmup:
+            e2e_s.append(dt)
+    dev, e2e = statistics.median(dev_s), statistics.median(e2e_s)
+    # CPU: the reference reader's restatement on a bounded sample (first lines up to 128 MB)
+    cut = int(text[:min(n_bytes, 128 << 20)].tobytes().rfind(b"\n")) + 1
+    sample = text[:cut].tobytes()
+    t0 = time.perf_counter()
+    ct, cz, _ = oracle.read_text(sample)
+    cpu_s = time.perf_counter() - t0
+    assert np.array_equal(cz, c.sizes[:cz.size])
+    peak, peak_kind = measured_peaks()
+    alg = 2 * n_bytes + 4 * c.tokens.size + 12 * c.sizes.size  # two passes over the text, tokens, starts/sizes/meta
+    print(json.dumps({
+        "metric": "collection text parsed: bytes/s (read_collection on the GPU)", "value": n_bytes / dev / 1e9,
+        "unit": "GB/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev * 1000,
+        "higher_is_better": True, "dtype": "u8", "data": "synthetic (seeded generator, reference text format)",
+        "config": {"workload": WORKLOAD.split(":")[0] + " as text", "text_bytes": n_bytes,
+                   "tokens": int(c.tokens.size), "sets": int(c.sizes.size),
+                   "timing": "host wall clock of the whole call (two launches, two synchronisations, validation)"},
+        "roofline": {"bound": "hbm", "achieved": alg / dev / 1e9, "peak": peak, "unit": "GB/s",
+                     "frac": alg / dev / 1e9 / peak, "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_call": alg},
+        "cpu_baseline": {"value": len(sample) / cpu_s / 1e9, "unit": "GB/s", "cores": 1, "kind": "port",
+                         "sample": f"first {len(sample) >> 20} MB of the text, oracle_read_text (getline/split/atoi)"},
+        "e2e": {"value": n_bytes / e2e / 1e9, "unit": "GB/s", "h2d_bytes_per_step": n_bytes,
+                "d2h_bytes_per_step": 32, "ms_per_step": e2e * 1000}}), flush=True)
+
+
+def hs_text_bytes(c):
+    from hyset_gb300 import synth
+    lib = synth._load()
+    import ctypes as C
+    U32 = C.POINTER(C.c_uint32)
+    return lib.hyset_format_text(c.tokens.ctypes.data_as(U32), c.starts.ctypes.data_as(U32),
+                                 c.sizes.ctypes.data_as(U32), c.sizes.size, None, 0)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -404,13 +480,17 @@ def main():
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
     ap.add_argument("--vmode", type=int, default=0, help="verification: 0 auto, 1 lane, 2 warp per candidate")
-    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch"],
-                    help="batch: the batched R-S workload (a separate measurement, not the headline)")
+    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse"],
+                    help="batch: the batched R-S workload; parse: the collection text reader "
+                         "(separate measurements, not the headline)")
     ap.add_argument("--joins", type=int, default=256)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     if args.workload == "batch":
         run_batch(args)
+        return
+    if args.workload == "parse":
+        run_parse(args)
         return
     if args.impl == "reference":
         run_reference(args, ws, rank)

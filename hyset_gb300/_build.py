@@ -22,7 +22,7 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhyset_gb300.so")
 SYNTH = os.path.join(PKG, "libhyset_synth.so")
 
-CUDA_SOURCES = ["primitives.cu", "join.cu", "join_tm.cu", "batch.cu", "mlp.cu", "stats.cu", "capi.cu", "noalloc.cu"]
+CUDA_SOURCES = ["primitives.cu", "join.cu", "join_tm.cu", "batch.cu", "mlp.cu", "stats.cu", "capi.cu", "noalloc.cu", "parse.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17",

@@ -62,8 +62,11 @@ PROTOTYPES = {
                                           C.POINTER(C.c_void_p)]),
     "hyset_collection_from_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                C.c_uint32, C.POINTER(C.c_void_p)]),
+    "hyset_collection_parse": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
     "hyset_collection_free": (None, [C.c_void_p, C.c_void_p]),
     "hyset_collection_num_sets": (C.c_uint32, [C.c_void_p]),
+    "hyset_collection_num_tokens": (C.c_uint64, [C.c_void_p]),
+    "hyset_collection_download": (C.c_int, [C.c_void_p, C.c_void_p, U32P, U32P, U32P]),
     "hyset_self_join": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(JoinOpts), C.POINTER(C.c_void_p)]),
     "hyset_rs_join": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(JoinOpts), C.POINTER(C.c_void_p)]),
     "hyset_batch_join": (C.c_int, [C.c_void_p, C.POINTER(JoinDesc), C.c_uint32, C.POINTER(C.c_void_p)]),

@@ -86,6 +86,20 @@ class DeviceCollection:
             load().hyset_collection_free(self._ctx.handle, self.handle)
             self.handle = None
 
+    @property
+    def num_tokens(self) -> int:
+        return int(load().hyset_collection_num_tokens(self.handle))
+
+    def download(self):
+        """(tokens, starts, sizes) copied to host numpy arrays."""
+        lib = load()
+        tok = np.empty(self.num_tokens, np.uint32)
+        st = np.empty(self.n, np.uint32)
+        sz = np.empty(self.n, np.uint32)
+        check(lib.hyset_collection_download(self._ctx.handle, self.handle, tok.ctypes.data_as(U32P),
+                                            st.ctypes.data_as(U32P), sz.ctypes.data_as(U32P)), self._ctx.handle)
+        return tok, st, sz
+
     def __del__(self):
         try:
             if self._ctx.handle:
@@ -141,6 +155,24 @@ class Context:
             self.handle, tok.ctypes.data_as(U32P), tok.size, None if st is None else st.ctypes.data_as(U32P),
             sz.ctypes.data_as(U32P), sz.size, C.byref(h)), self.handle)
         return DeviceCollection(self, h, int(sz.size))
+
+    def parse(self, text) -> DeviceCollection:
+        """Parses the reference's text format on the GPU (read_collection,
+        include/hyset/collection.hpp:93-177).  text: bytes, a path, or an
+        object exposing a device pointer (int address, n_bytes) pair."""
+        if isinstance(text, tuple):
+            ptr, n = int(text[0]), int(text[1])
+            keep = None
+        else:
+            if isinstance(text, str):
+                with open(text, "rb") as f:
+                    text = f.read()
+            buf = np.frombuffer(text, dtype=np.uint8)
+            ptr, n, keep = buf.ctypes.data, buf.size, buf
+        h = C.c_void_p()
+        check(self._lib.hyset_collection_parse(self.handle, C.c_void_p(ptr), n, C.byref(h)), self.handle)
+        del keep
+        return DeviceCollection(self, h, int(self._lib.hyset_collection_num_sets(h)))
 
     def from_device(self, d_tokens: int, n_tokens: int, d_starts: int, d_sizes: int, n_sets: int,
                     keep=None) -> DeviceCollection:

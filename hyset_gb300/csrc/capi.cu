@@ -171,11 +171,14 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
 // whose device copy is enqueued on the stream (the host array is a member, so
 // no synchronisation is needed here).
 hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c) {
-    uint32_t L = 0;
-    for (uint32_t v : c->h_sizes) L = std::max(L, v);
+    std::vector<uint64_t>& hist = c->size_hist;  // one pass; grows with the largest size seen
+    hist.assign(c->n ? (size_t)c->h_sizes.back() + 1 : 1, 0);
+    for (uint32_t v : c->h_sizes) {
+        if (v >= hist.size()) hist.resize((size_t)v + 1, 0);
+        hist[v]++;
+    }
+    const uint32_t L = (uint32_t)hist.size() - 1;
     c->max_size = L;
-    c->size_hist.assign((size_t)L + 1, 0);
-    for (uint32_t v : c->h_sizes) c->size_hist[v]++;
     std::vector<uint32_t>& f = c->h_first_ge;
     f.resize((size_t)L + 2);
     uint64_t run = 0;
@@ -830,19 +833,20 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
 // on the host while the copies are in flight, and one synchronisation ends it.
 hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
     cudaStream_t s = ctx->stream;
-    c->h_sizes.resize(c->n);
+    if (h_sizes_or_null) c->h_sizes.assign(h_sizes_or_null, h_sizes_or_null + c->n);
+    else c->h_sizes.resize(c->n);
     if (c->n && !h_sizes_or_null)
         CK(cudaMemcpyAsync(c->h_sizes.data(), c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
     CK(ctx->s_flags.ensure(16, s));
     CK(cudaMemsetAsync(ctx->s_flags.p, 0, 16, s));
     CK(c->meta.ensure((size_t)c->n * sizeof(uint2) + 8, s));
     CK(validate_collection(c->view(), c->n_tokens, ctx->s_flags.as<uint32_t>(), c->meta.as<uint2>(), s));
-    uint32_t f[2] = {0, 0};
+    // host work while the copies and the check run; the flags come back
+    // through pinned memory, so nothing here waits for the device early
+    if (c->n && h_sizes_or_null) ST(build_size_meta(ctx, c));
+    uint32_t* f = ctx->h_flags;
+    f[0] = f[1] = 0;
     CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
-    if (c->n && h_sizes_or_null) {
-        std::memcpy(c->h_sizes.data(), h_sizes_or_null, (size_t)c->n * 4);
-        ST(build_size_meta(ctx, c));
-    }
     CK(cudaStreamSynchronize(s));
     if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
     if (f[0] & 1) return fail(ctx, HYSET_E_INVALID, "empty set in collection");
@@ -1106,6 +1110,7 @@ hyset_status hyset_create(int device, hyset_ctx** out) {
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ek0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ek1);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&ctx->h_flags, 64);
     if (e == cudaSuccess) {
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
@@ -1139,6 +1144,7 @@ void hyset_destroy(hyset_ctx* ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ek0) cudaEventDestroy(ctx->ek0);
     if (ctx->ek1) cudaEventDestroy(ctx->ek1);
+    if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
     delete ctx;
 }
 
@@ -1209,6 +1215,112 @@ hyset_status hyset_collection_from_device(hyset_ctx* ctx, const uint32_t* d_toke
         return stt;
     }
     *out = c.release();
+    return HYSET_OK;
+}
+
+hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n_bytes, hyset_coll** out) {
+    if (!ctx || !out || (n_bytes && !text)) return fail(ctx, HYSET_E_INVALID, "null argument");
+    if (n_bytes >= (1ull << 33)) return fail(ctx, HYSET_E_UNSUPPORTED, "text of 2^33 bytes or more");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    // the text: used in place when it is device memory, else copied
+    const uint8_t* d_text = reinterpret_cast<const uint8_t*>(text);
+    DevBuf staged, counts, err;
+    struct Release {  // scratch goes back to the pool on every return path
+        DevBuf* b[3];
+        cudaStream_t s;
+        ~Release() {
+            for (DevBuf* d : b) d->release(s);
+        }
+    } rel{{&staged, &counts, &err}, s};
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, text) != cudaSuccess) cudaGetLastError();
+    if (n_bytes && attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) {
+        CK(staged.ensure(n_bytes + 16, s));
+        CK(cudaMemcpyAsync(staged.p, text, n_bytes, cudaMemcpyHostToDevice, s));
+        d_text = staged.as<uint8_t>();
+    }
+    if (n_bytes && (reinterpret_cast<uintptr_t>(d_text) & 15u)) {  // tiles load 16-byte words
+        DevBuf aligned;
+        CK(aligned.ensure(n_bytes + 16, s));
+        CK(cudaMemcpyAsync(aligned.p, d_text, n_bytes, cudaMemcpyDeviceToDevice, s));
+        staged.release(s);
+        staged = aligned;
+        aligned.p = nullptr;
+        d_text = staged.as<uint8_t>();
+    }
+    const uint64_t tiles = parse_tiles(n_bytes);
+    CK(counts.ensure((2 * tiles + 2) * 4, s));
+    CK(err.ensure(16, s));
+    uint32_t* tile_toks = counts.as<uint32_t>();
+    uint32_t* tile_lines = tile_toks + tiles + 1;
+    uint32_t* flags = err.as<uint32_t>();
+    unsigned long long* first_bad = reinterpret_cast<unsigned long long*>(err.as<uint8_t>() + 8);
+    CK(cudaMemsetAsync(flags, 0, 8, s));
+    CK(cudaMemsetAsync(first_bad, 0xFF, 8, s));
+    CK(cudaMemsetAsync(tile_toks, 0, (2 * tiles + 2) * 4, s));
+    CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s));
+    CK(ctx->sc->scan.ensure(scan_scratch_words(tiles + 1) * 4, s));
+    CK(scan_exclusive(tile_toks, tile_toks, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+    CK(scan_exclusive(tile_lines, tile_lines, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+    uint32_t* h = ctx->h_flags;  // [0] flags, [2..3] first bad offset, [4] tokens, [5] lines
+    CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 4, tile_toks + tiles, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(h + 5, tile_lines + tiles, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    auto parse_error = [&](uint32_t f, unsigned long long at) {
+        char msg[160];
+        const char* what = (f & PARSE_E_CHAR) ? "unexpected byte"
+                           : (f & PARSE_E_EMPTY_ITEM) ? "empty item (two spaces, a leading space or a space before CR)"
+                           : (f & PARSE_E_LINE_END) ? "CR not ending a line, or a line of only CR"
+                                                    : "number of more than 10 digits or >= 2^32";
+        std::snprintf(msg, sizeof msg, "parse error at byte %llu: %s", at, what);
+        return fail(ctx, HYSET_E_INVALID, msg);
+    };
+    if (h[0]) return parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+    const uint32_t n_tokens = h[4], n_lines = h[5];
+    auto c = std::make_unique<hyset_coll>();
+    c->ctx = ctx;
+    c->n = n_lines;
+    c->n_tokens = n_tokens;
+    CK(c->tokens.ensure((size_t)n_tokens * 4 + 4, s));
+    CK(c->starts.ensure((size_t)n_lines * 4 + 4, s));
+    CK(c->sizes.ensure((size_t)n_lines * 4 + 4, s));
+    CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(), flags,
+                  first_bad, s));
+    CK(parse_line_sizes(c->starts.as<uint32_t>(), n_lines, n_tokens, c->starts.as<uint32_t>(),
+                        c->sizes.as<uint32_t>(), s));
+    CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h[0]) {
+        hyset_status st = parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        hyset_collection_free(ctx, c.release());
+        return st;
+    }
+    c->d_tokens = c->tokens.as<uint32_t>();
+    c->d_starts = c->starts.as<uint32_t>();
+    c->d_sizes = c->sizes.as<uint32_t>();
+    hyset_status stt = make_collection(ctx, c.get(), nullptr);
+    if (stt != HYSET_OK) {
+        hyset_collection_free(ctx, c.release());
+        return stt;
+    }
+    *out = c.release();
+    return HYSET_OK;
+}
+
+uint64_t hyset_collection_num_tokens(const hyset_coll* c) { return c ? c->n_tokens : 0; }
+
+hyset_status hyset_collection_download(hyset_ctx* ctx, const hyset_coll* c, uint32_t* tokens, uint32_t* starts,
+                                       uint32_t* sizes) {
+    if (!ctx || !c) return fail(ctx, HYSET_E_INVALID, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    if (tokens && c->n_tokens) CK(cudaMemcpyAsync(tokens, c->d_tokens, c->n_tokens * 4, cudaMemcpyDeviceToHost, s));
+    if (starts && c->n) CK(cudaMemcpyAsync(starts, c->d_starts, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
+    if (sizes && c->n) CK(cudaMemcpyAsync(sizes, c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
     return HYSET_OK;
 }
 

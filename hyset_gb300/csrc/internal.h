@@ -123,6 +123,7 @@ struct hyset_ctx {
     hs::Scratch own;
     hs::Scratch* sc = &own;
     hs::DevBuf s_pairs, s_count, s_work, s_stats, s_flags;
+    uint32_t* h_flags = nullptr;  // pinned host words for small device-to-host reads
     std::unique_ptr<hs::BatchPlan> batch;
     // technique selector: learned network and/or analytic cost model
     bool has_mlp = false, has_cost = false;

@@ -2,6 +2,7 @@
 // Everything here is asynchronous on the given stream and returns the first
 // CUDA error it sees.
 #pragma once
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -12,6 +13,27 @@ namespace hs {
 // Kernel launches issued by this library since load (bench bookkeeping).
 unsigned long long launches();
 void note_launches(unsigned n = 1);
+
+// ---- parse.cu ------------------------------------------------------------
+// The reference's text format on the device (one set per line, tokens split by
+// single spaces).  Error bits of flags[0]:
+constexpr uint32_t PARSE_E_CHAR = 1;        // a byte other than digit, ' ', '\r', '\n'
+constexpr uint32_t PARSE_E_EMPTY_ITEM = 2;  // two spaces, a leading space, or a space before '\r'
+constexpr uint32_t PARSE_E_LINE_END = 4;    // '\r' not followed by '\n', or a line of only "\r"
+constexpr uint32_t PARSE_E_RANGE = 8;       // a number of more than 10 digits or >= 2^32
+uint64_t parse_tiles(uint64_t n_bytes);
+// Per 4 KiB tile: token starts and line starts; flags / first_bad (byte offset,
+// atomicMin) record errors.
+cudaError_t parse_count(const uint8_t* text, uint64_t n_bytes, uint32_t* tile_toks, uint32_t* tile_lines,
+                        uint32_t* flags, unsigned long long* first_bad, cudaStream_t s);
+// tile_tok0 / tile_line0: exclusive scans of the tile counts.  Writes every
+// token and line_tok0[line] = index of the line's first token.
+cudaError_t parse_emit(const uint8_t* text, uint64_t n_bytes, const uint32_t* tile_tok0, const uint32_t* tile_line0,
+                       uint32_t* tokens, uint32_t* line_tok0, uint32_t* flags, unsigned long long* first_bad,
+                       cudaStream_t s);
+// starts[i] = line_tok0[i], sizes[i] = next line's first token - line_tok0[i].
+cudaError_t parse_line_sizes(const uint32_t* line_tok0, uint32_t n_lines, uint32_t n_tokens, uint32_t* starts,
+                             uint32_t* sizes, cudaStream_t s);
 
 // ---- primitives.cu -------------------------------------------------------
 // Exclusive prefix sum of n uint32 values (in may equal out).  `scratch` must

@@ -254,4 +254,40 @@ extern "C" int hyset_synth_write_text(const hyset_synth* s, const char* path) {
     return std::fclose(f) == 0 ? 0 : 1;
 }
 
+namespace {
+inline uint32_t decimal_digits(uint32_t v) {
+    uint32_t d = 1;
+    while (v >= 10) {
+        v /= 10;
+        ++d;
+    }
+    return d;
+}
+}  // namespace
+
+extern "C" uint64_t hyset_format_text(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes,
+                                      uint32_t n_sets, char* buf, uint64_t cap) {
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < n_sets; ++i) {
+        for (uint32_t k = 0; k < sizes[i]; ++k) total += decimal_digits(tokens[(uint64_t)starts[i] + k]) + 1;
+        if (!sizes[i]) total += 1;
+    }
+    if (!buf || cap < total) return total;
+    char* o = buf;
+    for (uint32_t i = 0; i < n_sets; ++i) {
+        for (uint32_t k = 0; k < sizes[i]; ++k) {
+            uint32_t v = tokens[(uint64_t)starts[i] + k];
+            const uint32_t d = decimal_digits(v);
+            for (uint32_t j = d; j-- > 0;) {
+                o[j] = (char)('0' + v % 10);
+                v /= 10;
+            }
+            o += d;
+            *o++ = k + 1 < sizes[i] ? ' ' : '\n';
+        }
+        if (!sizes[i]) *o++ = '\n';
+    }
+    return total;
+}
+
 extern "C" void hyset_synth_free(hyset_synth* s) { delete s; }

@@ -89,8 +89,26 @@ def _load():
             fn.restype = C.POINTER(C.c_uint32)
         lib.hyset_synth_free.argtypes = [C.c_void_p]
         lib.hyset_synth_free.restype = None
+        U32 = C.POINTER(C.c_uint32)
+        lib.hyset_format_text.argtypes = [U32, U32, U32, C.c_uint32, C.c_void_p, C.c_uint64]
+        lib.hyset_format_text.restype = C.c_uint64
         _lib = lib
     return _lib
+
+
+def format_text(tokens, starts, sizes, out=None) -> np.ndarray:
+    """The reference's text format of a collection as a uint8 array (written
+    into `out`, e.g. pinned memory, when it is large enough)."""
+    lib = _load()
+    U32 = C.POINTER(C.c_uint32)
+    t = np.ascontiguousarray(tokens, np.uint32)
+    st = np.ascontiguousarray(starts, np.uint32)
+    sz = np.ascontiguousarray(sizes, np.uint32)
+    args = (t.ctypes.data_as(U32), st.ctypes.data_as(U32), sz.ctypes.data_as(U32), sz.size)
+    n = int(lib.hyset_format_text(*args, None, 0))
+    buf = out[:n] if out is not None and out.size >= n else np.empty(n, np.uint8)
+    lib.hyset_format_text(*args, buf.ctypes.data_as(C.c_void_p), n)
+    return buf
 
 
 def generate(spec: SynthSpec, threads: int = 0, **overrides) -> Collection:

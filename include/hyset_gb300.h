@@ -113,8 +113,24 @@ hyset_status hyset_collection_upload(hyset_ctx* ctx, const uint32_t* tokens, uin
 hyset_status hyset_collection_from_device(hyset_ctx* ctx, const uint32_t* d_tokens, uint64_t n_tokens,
                                           const uint32_t* d_starts, const uint32_t* d_sizes,
                                           uint32_t n_sets, hyset_coll** out);
+/* hyset::collection::read_collection (include/hyset/collection.hpp:93-177, split at :16-24)
+ * on the GPU: parses the reference's text format (one set per line, tokens as
+ * decimal numbers split by single spaces, '\n' or "\r\n" line ends, empty
+ * lines skipped, one trailing space per line allowed) from `text` (host or
+ * device memory, n_bytes long) into a device collection, validated as
+ * hyset_collection_upload validates.  Items the reference would turn into
+ * token 0 through atoi of an empty or non-numeric field (two spaces, a leading
+ * space, a space before '\r', a line of only "\r"), other bytes, and numbers
+ * of 2^32 or more return HYSET_E_INVALID; hyset_last_error names the first
+ * bad byte offset.  n_bytes must be below 2^33. */
+hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n_bytes, hyset_coll** out);
 void hyset_collection_free(hyset_ctx* ctx, hyset_coll* coll);
 uint32_t hyset_collection_num_sets(const hyset_coll* coll);
+/* Copies the collection's CSR arrays to host memory (each may be NULL to skip):
+ * tokens[num_tokens], starts[num_sets], sizes[num_sets]. */
+uint64_t hyset_collection_num_tokens(const hyset_coll* coll);
+hyset_status hyset_collection_download(hyset_ctx* ctx, const hyset_coll* coll, uint32_t* tokens,
+                                       uint32_t* starts, uint32_t* sizes);
 
 /* ---- whole joins ----------------------------------------------------- */
 /* Self-join R ⋈ R: what src/bitmap.cu:112-121 and src/fgss.cu:108-116 compute

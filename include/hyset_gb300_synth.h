@@ -52,6 +52,11 @@ const uint32_t* hyset_synth_sizes(const hyset_synth* s);   /* length num_sets */
 const uint32_t* hyset_synth_starts(const hyset_synth* s);  /* length num_sets */
 /* Writes the reference's text format; returns 0 on success. */
 int hyset_synth_write_text(const hyset_synth* s, const char* path);
+/* Formats CSR arrays in the reference's text format (one set per line, tokens
+ * split by one space, '\n' line ends) into buf; returns the byte count.  With
+ * buf == NULL or cap too small nothing is written (the count is still returned). */
+uint64_t hyset_format_text(const uint32_t* tokens, const uint32_t* starts, const uint32_t* sizes, uint32_t n_sets,
+                           char* buf, uint64_t cap);
 void hyset_synth_free(hyset_synth* s);
 
 #ifdef __cplusplus

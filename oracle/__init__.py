@@ -169,3 +169,19 @@ def ref_join(path: str, threshold: float, algorithm="allpairs", mode="whole", bl
 
 def as_set(pairs: np.ndarray) -> set:
     return set(map(tuple, np.asarray(pairs).reshape(-1, 2).tolist()))
+
+
+def read_text(text: bytes):
+    """(tokens, sizes, empty_items) as the reference's reader reads the text
+    (C restatement, oracle_read_text)."""
+    lib = _load()
+    fn = lib.oracle_read_text
+    fn.restype = C.c_uint64
+    fn.argtypes = [C.c_char_p, C.c_uint64, U32P, C.c_uint64, U32P, C.c_uint64, C.POINTER(C.c_uint64),
+                   C.POINTER(C.c_uint64)]
+    cap = len(text) // 2 + 2
+    tok = np.empty(cap, np.uint32)
+    siz = np.empty(cap, np.uint32)
+    nt, ne = C.c_uint64(), C.c_uint64()
+    ns = fn(text, len(text), tok.ctypes.data_as(U32P), cap, siz.ctypes.data_as(U32P), cap, C.byref(nt), C.byref(ne))
+    return tok[:nt.value].copy(), siz[:ns].copy(), int(ne.value)

@@ -440,3 +440,57 @@ oracle_pairs* oracle_brute_rs(const uint32_t* r_tokens, const uint32_t* r_starts
     }
     return out;
 }
+
+/* ---- the reference's text reader ----------------------------------------- */
+
+static int is_space_c(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; }
+
+/* atoi of item [a, b); *digits = whether any digit was read */
+static uint32_t atoi_item(const char* a, const char* b, int* digits) {
+    while (a < b && is_space_c(*a)) ++a;
+    int neg = 0;
+    if (a < b && (*a == '+' || *a == '-')) {
+        neg = *a == '-';
+        ++a;
+    }
+    uint32_t v = 0;
+    *digits = 0;
+    while (a < b && *a >= '0' && *a <= '9') {
+        v = v * 10u + (uint32_t)(*a - '0');
+        ++a;
+        *digits = 1;
+    }
+    return neg ? (uint32_t)(0u - v) : v;
+}
+
+uint64_t oracle_read_text(const char* text, uint64_t n, uint32_t* tokens, uint64_t tok_cap, uint32_t* sizes,
+                          uint64_t size_cap, uint64_t* n_tokens, uint64_t* empty_items) {
+    uint64_t sets = 0, toks = 0, empty = 0, i = 0;
+    while (i < n) {
+        uint64_t e = i;
+        while (e < n && text[e] != '\n') ++e;
+        if (e > i) { /* a non-empty line [i, e) */
+            uint32_t count = 0;
+            uint64_t a = i;
+            for (uint64_t k = i; k <= e; ++k) {
+                const int end = k == e;
+                if (end && k == a) break; /* nothing after the last ' ' */
+                if (end || text[k] == ' ') {
+                    int digits = 0;
+                    const uint32_t v = atoi_item(text + a, text + k, &digits);
+                    if (!digits) ++empty;
+                    if (toks < tok_cap) tokens[toks] = v;
+                    ++toks;
+                    ++count;
+                    a = k + 1;
+                }
+            }
+            if (sets < size_cap) sizes[sets] = count;
+            ++sets;
+        }
+        i = e + 1;
+    }
+    *n_tokens = toks;
+    *empty_items = empty;
+    return sets;
+}

@@ -71,6 +71,16 @@ oracle_pairs* oracle_brute_rs(const uint32_t* r_tokens, const uint32_t* r_starts
                               uint32_t r_n, const uint32_t* s_tokens, const uint32_t* s_starts,
                               const uint32_t* s_sizes, uint32_t s_n, int sim, double t);
 
+/* hyset::collection::read_collection's text reading (include/hyset/collection.hpp:93-177)
+ * and split (collection.hpp:16-24): lines by '\n' (the text after the last
+ * '\n' too), empty lines skipped, items split at every ' ' (a space at the end
+ * of a line ends the last item), each item atoi'ed (leading white space, a
+ * sign, digits).  Writes up to tok_cap tokens and size_cap sizes; returns the
+ * number of sets, *n_tokens the number of tokens and *empty_items the items
+ * with no digits (atoi gives 0). */
+uint64_t oracle_read_text(const char* text, uint64_t n, uint32_t* tokens, uint64_t tok_cap, uint32_t* sizes,
+                          uint64_t size_cap, uint64_t* n_tokens, uint64_t* empty_items);
+
 uint64_t oracle_pairs_count(const oracle_pairs* p);
 const uint32_t* oracle_pairs_data(const oracle_pairs* p); /* 2*count: (first, second) */
 void oracle_pairs_free(oracle_pairs* p);
