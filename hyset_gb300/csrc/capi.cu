@@ -166,16 +166,24 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
     return HYSET_OK;
 }
 
-// Host size statistics from the host copy of the sizes: the per-size histogram
-// and first_ge[l] = first set id with size >= l (sizes are non-decreasing),
-// whose device copy is enqueued on the stream (the host array is a member, so
-// no synchronisation is needed here).
-hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c) {
-    std::vector<uint64_t>& hist = c->size_hist;  // one pass; grows with the largest size seen
-    hist.assign(c->n ? (size_t)c->h_sizes.back() + 1 : 1, 0);
-    for (uint32_t v : c->h_sizes) {
+// Host size statistics from host-resident sizes (the caller's array, or the
+// pinned copy of device sizes): the per-size histogram and first_ge[l] = first
+// set id with size >= l (sizes are non-decreasing), whose device copy is
+// enqueued on the stream (the host array is a member, so no synchronisation is
+// needed here).  The collection keeps no per-set host array: sizes of single
+// sets and of id ranges come from first_ge.
+hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c, const uint32_t* sizes) {
+    // run lengths: sorted sizes repeat, so the count stays in a register
+    std::vector<uint64_t>& hist = c->size_hist;
+    hist.assign(c->n ? (size_t)sizes[c->n - 1] + 1 : 1, 0);
+    uint32_t i = 0;
+    while (i < c->n) {
+        const uint32_t v = sizes[i];
+        uint32_t j = i + 1;
+        while (j < c->n && sizes[j] == v) ++j;
         if (v >= hist.size()) hist.resize((size_t)v + 1, 0);
-        hist[v]++;
+        hist[v] += j - i;
+        i = j;
     }
     const uint32_t L = (uint32_t)hist.size() - 1;
     c->max_size = L;
@@ -189,6 +197,23 @@ hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c) {
     CK(c->first_ge.ensure(f.size() * 4, ctx->stream));
     CK(cudaMemcpyAsync(c->first_ge.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     return HYSET_OK;
+}
+
+// Size of set i (sizes are non-decreasing: the last l with first_ge[l] <= i).
+uint32_t size_at(const hyset_coll* c, uint32_t i) {
+    const auto& f = c->h_first_ge;
+    return (uint32_t)(std::upper_bound(f.begin(), f.end(), i) - f.begin()) - 1;
+}
+
+// Sets per size among ids [lo, hi).
+std::vector<uint64_t> range_hist(const hyset_coll* c, uint32_t lo, uint32_t hi) {
+    std::vector<uint64_t> ph((size_t)c->max_size + 1, 0);
+    const auto& f = c->h_first_ge;
+    for (uint32_t l = 0; l <= c->max_size; ++l) {
+        const uint32_t a = std::max(lo, f[l]), b = std::min(hi, f[l + 1]);
+        if (b > a) ph[l] = b - a;
+    }
+    return ph;
 }
 
 // Prefix entries of sets [lo, hi) (all sets when hi == n) from the size histogram.
@@ -544,10 +569,7 @@ hyset_status compute_features(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
     unsigned long long m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     CK(cudaMemcpyAsync(m, mom, 64, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    std::vector<uint64_t> ph(S->max_size + 1, 0);
-    if (np == S->n) ph = S->size_hist;
-    else
-        for (uint32_t i = p_lo; i < p_hi; ++i) ph[S->h_sizes[i]]++;
+    const std::vector<uint64_t> ph = np == S->n ? S->size_hist : range_hist(S, p_lo, p_hi);
     double pre = 0;
     for (size_t l = 0; l < ph.size(); ++l) pre += (double)ph[l] * b->probe_prefix[l];
     const double n_d = np ? (double)np : 1.0;
@@ -831,31 +853,62 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
 // check (one pass over the tokens, which also writes the meta pairs) is
 // enqueued behind the caller's copies; with host sizes the histogram work runs
 // on the host while the copies are in flight, and one synchronisation ends it.
-hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
+// Pinned host memory of at least `bytes`, kept by the context for
+// device-to-host reads that must not wait on a pageable copy.
+hyset_status host_stage(hyset_ctx* ctx, size_t bytes, void** out) {
+    if (bytes > ctx->h_stage_bytes) {
+        const size_t want = std::max(bytes, 2 * ctx->h_stage_bytes);
+        if (ctx->h_stage) CK(cudaFreeHost(ctx->h_stage));
+        ctx->h_stage = nullptr;
+        ctx->h_stage_bytes = 0;
+        CK(cudaMallocHost(&ctx->h_stage, want));
+        ctx->h_stage_bytes = want;
+    }
+    *out = ctx->h_stage;
+    return HYSET_OK;
+}
+
+// Enqueues the checks of a new collection (one pass over the tokens, which also
+// writes the meta pairs) and the read-back of their flags (and of the sizes,
+// when they are only on the device).  With host sizes the histogram work runs
+// on the host while the copies and the check are in flight.
+hyset_status enqueue_collection_checks(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
     cudaStream_t s = ctx->stream;
-    if (h_sizes_or_null) c->h_sizes.assign(h_sizes_or_null, h_sizes_or_null + c->n);
-    else c->h_sizes.resize(c->n);
-    if (c->n && !h_sizes_or_null)
-        CK(cudaMemcpyAsync(c->h_sizes.data(), c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
+    if (!h_sizes_or_null && c->n) {
+        void* stage = nullptr;
+        ST(host_stage(ctx, (size_t)c->n * 4, &stage));
+        CK(cudaMemcpyAsync(stage, c->d_sizes, (size_t)c->n * 4, cudaMemcpyDeviceToHost, s));
+    }
     CK(ctx->s_flags.ensure(16, s));
     CK(cudaMemsetAsync(ctx->s_flags.p, 0, 16, s));
     CK(c->meta.ensure((size_t)c->n * sizeof(uint2) + 8, s));
     CK(validate_collection(c->view(), c->n_tokens, ctx->s_flags.as<uint32_t>(), c->meta.as<uint2>(), s));
-    // host work while the copies and the check run; the flags come back
-    // through pinned memory, so nothing here waits for the device early
-    if (c->n && h_sizes_or_null) ST(build_size_meta(ctx, c));
+    if (c->n && h_sizes_or_null) ST(build_size_meta(ctx, c, h_sizes_or_null));
     uint32_t* f = ctx->h_flags;
     f[0] = f[1] = 0;
     CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
+    return HYSET_OK;
+}
+
+// After the stream has synchronised: the verdict of the checks, then the host
+// size statistics of a collection whose sizes came from the device.
+hyset_status finish_collection_checks(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
+    const uint32_t* f = ctx->h_flags;
     if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
     if (f[0] & 1) return fail(ctx, HYSET_E_INVALID, "empty set in collection");
     if (f[0] & 2) return fail(ctx, HYSET_E_INVALID, "set tokens must be strictly ascending");
     if (f[0] & 4) return fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size");
     if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
     c->universe = c->n ? f[1] + 1 : 1;
-    if (!h_sizes_or_null || !c->n) ST(build_size_meta(ctx, c));
+    if (!h_sizes_or_null || !c->n)
+        ST(build_size_meta(ctx, c, c->n ? static_cast<const uint32_t*>(ctx->h_stage) : nullptr));
     return HYSET_OK;
+}
+
+hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_sizes_or_null) {
+    ST(enqueue_collection_checks(ctx, c, h_sizes_or_null));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return finish_collection_checks(ctx, c, h_sizes_or_null);
 }
 
 // ---------------------------------------------------------------- batches
@@ -1145,6 +1198,7 @@ void hyset_destroy(hyset_ctx* ctx) {
     if (ctx->ek0) cudaEventDestroy(ctx->ek0);
     if (ctx->ek1) cudaEventDestroy(ctx->ek1);
     if (ctx->h_flags) cudaFreeHost(ctx->h_flags);
+    if (ctx->h_stage) cudaFreeHost(ctx->h_stage);
     delete ctx;
 }
 
@@ -1264,7 +1318,7 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
     CK(ctx->sc->scan.ensure(scan_scratch_words(tiles + 1) * 4, s));
     CK(scan_exclusive(tile_toks, tile_toks, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
     CK(scan_exclusive(tile_lines, tile_lines, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
-    uint32_t* h = ctx->h_flags;  // [0] flags, [2..3] first bad offset, [4] tokens, [5] lines
+    uint32_t* h = ctx->h_flags + 8;  // [0] flags, [2..3] first bad offset, [4] tokens, [5] lines
     CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h + 4, tile_toks + tiles, 4, cudaMemcpyDeviceToHost, s));
     CK(cudaMemcpyAsync(h + 5, tile_lines + tiles, 4, cudaMemcpyDeviceToHost, s));
@@ -1292,16 +1346,16 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
     CK(parse_line_sizes(c->starts.as<uint32_t>(), n_lines, n_tokens, c->starts.as<uint32_t>(),
                         c->sizes.as<uint32_t>(), s));
     CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    if (h[0]) {
-        hyset_status st = parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
-        hyset_collection_free(ctx, c.release());
-        return st;
-    }
     c->d_tokens = c->tokens.as<uint32_t>();
     c->d_starts = c->starts.as<uint32_t>();
     c->d_sizes = c->sizes.as<uint32_t>();
-    hyset_status stt = make_collection(ctx, c.get(), nullptr);
+    // the collection checks go behind the parse on the stream: one synchronisation
+    hyset_status stt = enqueue_collection_checks(ctx, c.get(), nullptr);
+    if (stt == HYSET_OK) {
+        CK(cudaStreamSynchronize(s));
+        if (h[0]) stt = parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        else stt = finish_collection_checks(ctx, c.get(), nullptr);
+    }
     if (stt != HYSET_OK) {
         hyset_collection_free(ctx, c.release());
         return stt;
@@ -1654,7 +1708,8 @@ hyset_status build_block_index(hyset_handler* h, const hyset_block& blk) {
     const hyset_coll* c = h->coll;
     const uint32_t lo = blk.start_id, hi = blk.end_id + 1, nb = hi - lo, U = c->universe;
     uint64_t E = 0;  // the block's prefix entries (block.entries in the reference)
-    for (uint32_t i = lo; i < hi; ++i) E += h->bounds->index_prefix[c->h_sizes[i]];
+    const std::vector<uint64_t> bh = range_hist(c, lo, hi);
+    for (size_t l = 0; l < bh.size(); ++l) E += bh[l] * h->bounds->index_prefix[l];
     const uint64_t E1 = E ? E : 1;
     CK(h->counts.ensure(((size_t)U + 1) * 4, s));
     CK(h->list_off.ensure(((size_t)U + 1) * 4, s));
@@ -1764,8 +1819,8 @@ hyset_status hyset_handler_join_partitions(hyset_handler* h, const hyset_block* 
         for (uint32_t k = 0; k < n_second; ++k) {
             ST(check_block(h->ctx, h->coll, &second[k]));
             if (second[k].id < first[i].id) continue;
-            uint32_t last_indexed = h->coll->h_sizes[first[i].end_id];
-            uint32_t first_probe = h->coll->h_sizes[second[k].start_id];
+            uint32_t last_indexed = size_at(h->coll, first[i].end_id);
+            uint32_t first_probe = size_at(h->coll, second[k].start_id);
             if (last_indexed >= h->bounds->minsize[first_probe]) ST(hyset_handler_join_blocks(h, &first[i], &second[k]));
         }
     }

@@ -124,6 +124,8 @@ struct hyset_ctx {
     hs::Scratch* sc = &own;
     hs::DevBuf s_pairs, s_count, s_work, s_stats, s_flags;
     uint32_t* h_flags = nullptr;  // pinned host words for small device-to-host reads
+    void* h_stage = nullptr;      // pinned staging for larger reads (grows)
+    size_t h_stage_bytes = 0;
     std::unique_ptr<hs::BatchPlan> batch;
     // technique selector: learned network and/or analytic cost model
     bool has_mlp = false, has_cost = false;
@@ -145,7 +147,6 @@ struct hyset_coll {
     uint64_t n_tokens = 0;
     uint32_t max_size = 0;
     uint32_t universe = 0;  // max token + 1
-    std::vector<uint32_t> h_sizes;
     std::vector<uint64_t> size_hist;  // sets per size, [max_size+1]
     hs::DevBuf first_ge;              // [max_size+2] first id with size >= l
     std::vector<uint32_t> h_first_ge; // host copy (source of the device copy)

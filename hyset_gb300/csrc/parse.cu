@@ -4,15 +4,18 @@
 // reads one set per line with std::getline, skips empty lines and splits each
 // line on single spaces (split, collection.hpp:16-24: std::getline with ' '
 // and atoi per item); sets arrive sorted by size with ascending tokens.  Here
-// the text sits in device memory and two passes over 4 KiB tiles turn it into
-// the CSR arrays:
-//   pass 1  per tile: count token starts and line starts, check the bytes;
+// the text sits in device memory and two passes over 4 KiB tiles (256 threads,
+// 16 bytes each, one 16-byte load per thread) turn it into the CSR arrays:
+//   pass 1  per tile: count token ends and line starts and check the bytes;
 //   scan    exclusive scans of the tile counts give every tile its first
 //           token and first line;
-//   pass 2  per tile: a block scan of the per-thread counts places every token
-//           and line; each token start parses its digits (reading past the
-//           tile when a number crosses it) and writes its value; each line
-//           start records the index of its first token.
+//   pass 2  per tile: a block scan places every token and line; each thread
+//           folds its 16 digits into values, continuing a number that began
+//           in the previous thread's bytes, and the tile's tokens and line
+//           starts are staged in shared memory and stored contiguously.
+// A token belongs to the thread holding its last digit.  Byte classes are
+// computed four bytes at a time and kept as 16-bit masks (bit k = byte k of
+// the thread's chunk).
 // Lines are "d+( d+)* ?\r?\n" (a single trailing space is dropped, as the
 // reference's split drops it).  Inputs the reference turns into token 0 by
 // atoi of an empty or non-numeric item (two spaces, a leading space, a space
@@ -27,67 +30,89 @@ namespace {
 constexpr int PARSE_THREADS = 256;
 constexpr int PARSE_BYTES = 16;                               // per thread
 constexpr uint64_t PARSE_TILE = PARSE_THREADS * PARSE_BYTES;  // 4096
+constexpr int PARSE_MAX_ITEMS = PARSE_TILE / 2;               // tokens (or lines) of one tile, at most
 
-__device__ __forceinline__ bool is_digit(uint32_t c) { return c - '0' < 10u; }
-
-// Byte i of the text, '\n' outside [0, n).
-__device__ __forceinline__ uint32_t byte_at(const uint8_t* t, uint64_t n, int64_t i) {
-    return (i >= 0 && (uint64_t)i < n) ? t[i] : (uint32_t)'\n';
+// 0x80 in every byte of x that is zero.
+__device__ __forceinline__ uint32_t zero_bytes(uint32_t x) {
+    const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+    return ~(t | x | 0x7F7F7F7Fu);
 }
 
-struct Chunk {
-    uint32_t b[PARSE_BYTES + 2];  // b[0] = byte before the chunk, b[17] = byte after it
+// The high bits of the four bytes of m (0x80 per byte) as bits 0..3.
+__device__ __forceinline__ uint32_t pack4(uint32_t m) { return ((m >> 7) * 0x00204081u >> 21) & 0xFu; }
+
+__device__ __forceinline__ uint32_t byte_eq(uint32_t w, uint32_t c) { return pack4(zero_bytes(w ^ (c * 0x01010101u))); }
+
+// Bytes 0x30..0x39: (b - 0x30) < 10, four bytes at a time without borrows.
+__device__ __forceinline__ uint32_t digit_bytes(uint32_t w) {
+    const uint32_t hi = w & 0x80808080u;     // bytes >= 0x80 are not digits
+    const uint32_t lo = w & 0x7F7F7F7Fu;
+    const uint32_t ge0 = (lo + 0x50505050u) & 0x80808080u;  // lo >= 0x30
+    const uint32_t ge10 = (lo + 0x46464646u) & 0x80808080u; // lo >= 0x3A
+    return pack4(ge0 & ~ge10 & ~hi);
+}
+
+struct Masks {
+    uint32_t digit, space, nl, cr, valid;  // bit k: byte k of the chunk (valid: inside the text)
+    uint32_t prev_nl, prev_sp, next_digit, next_nl, next_cr;
 };
 
-__device__ __forceinline__ void load_chunk(const uint8_t* t, uint64_t n, uint64_t base, Chunk& c) {
-    c.b[0] = byte_at(t, n, (int64_t)base - 1);
+__device__ __forceinline__ uint32_t byte_at(const uint8_t* t, uint64_t n, int64_t i) {
+    return (i >= 0 && (uint64_t)i < n) ? t[i] : (uint32_t)'\n';  // outside the text: a line end
+}
+
+// The chunk's four words (bytes past the text read as '\n') and its masks.
+__device__ __forceinline__ void load_chunk(const uint8_t* t, uint64_t n, uint64_t base, uint32_t (&w)[4], Masks& m) {
     if (base + PARSE_BYTES <= n) {
         const uint4 v = *reinterpret_cast<const uint4*>(t + base);  // base is a multiple of 16
-        const uint32_t w[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-        for (int k = 0; k < PARSE_BYTES; ++k) c.b[1 + k] = (w[k >> 2] >> (8 * (k & 3))) & 0xFFu;
+        w[0] = v.x;
+        w[1] = v.y;
+        w[2] = v.z;
+        w[3] = v.w;
     } else {
 #pragma unroll
-        for (int k = 0; k < PARSE_BYTES; ++k) c.b[1 + k] = byte_at(t, n, (int64_t)(base + k));
-    }
-    c.b[PARSE_BYTES + 1] = byte_at(t, n, (int64_t)(base + PARSE_BYTES));
-}
-
-// Token starts and line starts in the chunk; error bits and the first bad
-// offset go to err.
-__device__ __forceinline__ void chunk_counts(const Chunk& c, uint64_t base, uint64_t n, uint32_t& toks,
-                                             uint32_t& lines, uint32_t& err, uint64_t& err_at) {
-    toks = lines = err = 0;
-    err_at = ~0ull;
+        for (int q = 0; q < 4; ++q) {
+            uint32_t x = 0;
 #pragma unroll
-    for (int k = 1; k <= PARSE_BYTES; ++k) {
-        if (base + k - 1 >= n) break;
-        const uint32_t prev = c.b[k - 1], x = c.b[k], next = c.b[k + 1];
-        const bool at_line_start = prev == '\n';
-        uint32_t e = 0;
-        if (is_digit(x)) {
-            toks += (prev == ' ' || at_line_start) ? 1u : 0u;
-        } else if (x == ' ') {
-            if (prev == ' ' || at_line_start || next == '\r') e |= PARSE_E_EMPTY_ITEM;
-        } else if (x == '\r') {
-            if (next != '\n' || at_line_start) e |= PARSE_E_LINE_END;
-        } else if (x != '\n') {
-            e |= PARSE_E_CHAR;
-        }
-        lines += (at_line_start && x != '\n') ? 1u : 0u;
-        if (e) {
-            err |= e;
-            const uint64_t at = base + k - 1;
-            err_at = at < err_at ? at : err_at;
+            for (int b = 0; b < 4; ++b) x |= byte_at(t, n, (int64_t)(base + 4 * q + b)) << (8 * b);
+            w[q] = x;
         }
     }
+    m.digit = m.space = m.nl = m.cr = 0;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        m.digit |= digit_bytes(w[q]) << (4 * q);
+        m.space |= byte_eq(w[q], ' ') << (4 * q);
+        m.nl |= byte_eq(w[q], '\n') << (4 * q);
+        m.cr |= byte_eq(w[q], '\r') << (4 * q);
+    }
+    m.valid = base >= n ? 0u : (n - base >= PARSE_BYTES ? 0xFFFFu : (1u << (n - base)) - 1u);
+    const uint32_t before = byte_at(t, n, (int64_t)base - 1), after = byte_at(t, n, (int64_t)(base + PARSE_BYTES));
+    m.prev_nl = ((m.nl << 1) | (before == '\n' ? 1u : 0u)) & 0xFFFFu;
+    m.prev_sp = ((m.space << 1) | (before == ' ' ? 1u : 0u)) & 0xFFFFu;
+    m.next_digit = (m.digit >> 1) | ((after - '0' < 10u) ? 0x8000u : 0u);
+    m.next_nl = (m.nl >> 1) | (after == '\n' ? 0x8000u : 0u);
+    m.next_cr = (m.cr >> 1) | (after == '\r' ? 0x8000u : 0u);
 }
 
-__device__ __forceinline__ void record_error(uint32_t err, uint64_t err_at, uint32_t* flags,
+__device__ __forceinline__ uint32_t token_ends(const Masks& m) { return m.digit & ~m.next_digit & m.valid; }
+__device__ __forceinline__ uint32_t line_starts(const Masks& m) { return m.prev_nl & ~m.nl & m.valid; }
+
+// Error bits of the chunk and the first offending byte (bit index, 16 if none).
+__device__ __forceinline__ uint32_t chunk_errors(const Masks& m, int& first) {
+    const uint32_t bad_char = ~(m.digit | m.space | m.nl | m.cr) & m.valid;
+    const uint32_t empty_item = m.space & (m.prev_sp | m.prev_nl | m.next_cr) & m.valid;
+    const uint32_t bad_cr = m.cr & (~m.next_nl | m.prev_nl) & m.valid;
+    const uint32_t any = bad_char | empty_item | bad_cr;
+    first = any ? __ffs(any) - 1 : PARSE_BYTES;
+    return (bad_char ? PARSE_E_CHAR : 0u) | (empty_item ? PARSE_E_EMPTY_ITEM : 0u) | (bad_cr ? PARSE_E_LINE_END : 0u);
+}
+
+__device__ __forceinline__ void record_error(uint32_t err, uint64_t at, uint32_t* flags,
                                              unsigned long long* first_bad) {
     if (err) {
         atomicOr(flags, err);
-        atomicMin(first_bad, (unsigned long long)err_at);
+        atomicMin(first_bad, (unsigned long long)at);
     }
 }
 
@@ -97,15 +122,15 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_count(const uint8_t* __
     __shared__ uint32_t red[2][PARSE_THREADS / 32];
     const uint64_t tile = blockIdx.x;
     const uint64_t base = tile * PARSE_TILE + (uint64_t)threadIdx.x * PARSE_BYTES;
-    Chunk c;
-    load_chunk(t, n, base, c);
-    uint32_t toks, lines, err;
-    uint64_t err_at;
-    chunk_counts(c, base, n, toks, lines, err, err_at);
-    record_error(err, err_at, flags, first_bad);
+    uint32_t w[4];
+    Masks m;
+    load_chunk(t, n, base, w, m);
+    int first;
+    const uint32_t err = chunk_errors(m, first);
+    record_error(err, base + first, flags, first_bad);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    toks = __reduce_add_sync(FULL, toks);
-    lines = __reduce_add_sync(FULL, lines);
+    const uint32_t toks = __reduce_add_sync(FULL, __popc(token_ends(m)));
+    const uint32_t lines = __reduce_add_sync(FULL, __popc(line_starts(m)));
     if (lane == 0) {
         red[0][warp] = toks;
         red[1][warp] = lines;
@@ -113,28 +138,29 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_count(const uint8_t* __
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t a = 0, b = 0;
-        for (int w = 0; w < PARSE_THREADS / 32; ++w) {
-            a += red[0][w];
-            b += red[1][w];
+        for (int q = 0; q < PARSE_THREADS / 32; ++q) {
+            a += red[0][q];
+            b += red[1][q];
         }
         tile_toks[tile] = a;
         tile_lines[tile] = b;
     }
 }
 
-// Parses the number starting at byte i (at most 10 digits, value < 2^32).
-__device__ __forceinline__ bool parse_number(const uint8_t* t, uint64_t n, uint64_t i, uint32_t& value) {
-    uint64_t v = 0;
-    int d = 0;
-    while (i < n) {
-        const uint32_t ch = t[i];
-        if (!is_digit(ch)) break;
-        v = v * 10u + (ch - '0');
-        ++i;
-        if (++d > 10) return false;
+// Folds the chunk's digits into numbers: acc / nd carry the run that reaches
+// the chunk from the left; every token end stores its value (through emit).
+// Returns with acc / nd holding the run that leaves the chunk on the right.
+template <typename Emit>
+__device__ __forceinline__ void fold_digits(const uint32_t (&w)[4], uint32_t digit_mask, uint32_t end_mask,
+                                            unsigned long long& acc, uint32_t& nd, Emit&& emit) {
+#pragma unroll
+    for (int k = 0; k < PARSE_BYTES; ++k) {
+        const uint32_t d = ((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - '0';
+        const bool isd = (digit_mask >> k) & 1u;
+        acc = isd ? acc * 10u + d : 0ull;
+        nd = isd ? min(nd + 1u, 11u) : 0u;
+        if ((end_mask >> k) & 1u) emit(k, acc, nd);
     }
-    value = (uint32_t)v;
-    return v <= 0xFFFFFFFFull;
 }
 
 __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __restrict__ t, uint64_t n,
@@ -144,15 +170,18 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
                                                               uint32_t* __restrict__ line_tok0, uint32_t* flags,
                                                               unsigned long long* first_bad) {
     __shared__ uint32_t wsum[2][PARSE_THREADS / 32];
+    __shared__ unsigned long long tail_acc[PARSE_THREADS / 32];
+    __shared__ uint32_t tail_nd[PARSE_THREADS / 32];
+    __shared__ uint32_t s_tok[PARSE_MAX_ITEMS], s_line[PARSE_MAX_ITEMS];
     const uint64_t tile = blockIdx.x;
     const uint64_t base = tile * PARSE_TILE + (uint64_t)threadIdx.x * PARSE_BYTES;
-    Chunk c;
-    load_chunk(t, n, base, c);
-    uint32_t toks, lines, err;
-    uint64_t err_at;
-    chunk_counts(c, base, n, toks, lines, err, err_at);
-    // block-wide exclusive scan of (toks, lines)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t w[4];
+    Masks m;
+    load_chunk(t, n, base, w, m);
+    const uint32_t ends = token_ends(m), starts = line_starts(m);
+    const uint32_t toks = __popc(ends), lines = __popc(starts);
+    // block-wide exclusive scan of the token and line counts
     const uint32_t ti = warp_incl_scan(toks, lane), li = warp_incl_scan(lines, lane);
     if (lane == 31) {
         wsum[0][warp] = ti;
@@ -160,30 +189,76 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
     }
     __syncthreads();
     uint32_t tw = 0, lw = 0;
-    for (int w = 0; w < warp; ++w) {
-        tw += wsum[0][w];
-        lw += wsum[1][w];
+    for (int q = 0; q < warp; ++q) {
+        tw += wsum[0][q];
+        lw += wsum[1][q];
     }
-    uint32_t tok = tile_tok0[tile] + tw + ti - toks;
-    uint32_t line = tile_line0[tile] + lw + li - lines;
-    uint32_t bad = 0;
-    uint64_t bad_at = ~0ull;
-#pragma unroll
-    for (int k = 1; k <= PARSE_BYTES; ++k) {
-        if (base + k - 1 >= n) break;
-        const uint32_t prev = c.b[k - 1], x = c.b[k];
-        if (prev == '\n' && x != '\n') line_tok0[line++] = tok;
-        if (is_digit(x) && (prev == ' ' || prev == '\n')) {
-            uint32_t v = 0;
-            if (!parse_number(t, n, base + k - 1, v)) {
-                bad |= PARSE_E_RANGE;
-                const uint64_t at = base + k - 1;
-                bad_at = at < bad_at ? at : bad_at;
+    const uint32_t tok_first = tile_tok0[tile], line_first = tile_line0[tile];
+    const uint32_t tok0 = tw + ti - toks;  // within the tile
+    uint32_t line = lw + li - lines;
+    // line starts: the index of the line's first token = tokens ending before it
+    uint32_t sm = starts;
+    while (sm) {
+        const int k = __ffs(sm) - 1;
+        sm &= sm - 1;
+        s_line[line++] = tok_first + tok0 + __popc(ends & ((1u << k) - 1u));
+    }
+    // one pass over the chunk's digits; the first token's leading digits
+    // (lead_len of them, value lead) wait for the run carried in from the left
+    unsigned long long acc = 0, lead = 0;
+    uint32_t nd = 0, lead_len = 0, tok = tok0, bad = 0;
+    int bad_k = PARSE_BYTES;
+    const bool starts_in_run = m.digit & 1u;
+    fold_digits(w, m.digit, ends, acc, nd, [&](int k, unsigned long long v, uint32_t digits) {
+        if (tok == tok0 && starts_in_run && digits == (uint32_t)k + 1) {
+            lead = v;
+            lead_len = digits;
+        } else if (digits > 10 || v > 0xFFFFFFFFull) {
+            bad = PARSE_E_RANGE;
+            bad_k = min(bad_k, k);
+        }
+        s_tok[tok++] = (uint32_t)v;
+    });
+    // carry in: the previous chunk's right run (lane - 1; the previous warp's last
+    // lane through shared memory; the previous tile's last chunk from memory)
+    unsigned long long cacc = __shfl_up_sync(FULL, acc, 1);
+    uint32_t cnd = __shfl_up_sync(FULL, nd, 1);
+    if (lane == 31) {
+        tail_acc[warp] = acc;
+        tail_nd[warp] = nd;
+    }
+    __syncthreads();
+    if (lane == 0) {
+        if (warp > 0) {
+            cacc = tail_acc[warp - 1];
+            cnd = tail_nd[warp - 1];
+        } else {
+            cacc = 0;
+            cnd = 0;
+            if (base >= PARSE_BYTES) {
+                uint32_t pw[4];
+                Masks pm;
+                load_chunk(t, n, base - PARSE_BYTES, pw, pm);
+                fold_digits(pw, pm.digit, 0u, cacc, cnd, [](int, unsigned long long, uint32_t) {});
             }
-            tokens[tok++] = v;
         }
     }
-    record_error(bad, bad_at, flags, first_bad);
+    if (lead_len) {  // the first token ends here with lead_len digits from byte 0
+        unsigned long long p10 = 1;
+        for (uint32_t q = 0; q < lead_len; ++q) p10 *= 10u;
+        const unsigned long long v = cacc * p10 + lead;
+        const uint32_t digits = cnd + lead_len;
+        if (digits > 10 || v > 0xFFFFFFFFull) {
+            bad = PARSE_E_RANGE;
+            bad_k = 0;
+        }
+        s_tok[tok0] = (uint32_t)v;
+    }
+    record_error(bad, base + (uint64_t)bad_k, flags, first_bad);
+    __syncthreads();
+    const uint32_t n_tok = tile_tok0[tile + 1] - tok_first, n_line = tile_line0[tile + 1] - line_first;
+    for (uint32_t i = threadIdx.x; i < n_tok; i += PARSE_THREADS) tokens[tok_first + i] = s_tok[i];
+    for (uint32_t i = threadIdx.x; i < n_line; i += PARSE_THREADS) line_tok0[line_first + i] = s_line[i];
 }
 
 __global__ void k_line_sizes(const uint32_t* __restrict__ line_tok0, uint32_t n_lines, uint32_t n_tokens,
