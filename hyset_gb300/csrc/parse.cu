@@ -10,9 +10,10 @@
 //   scan    exclusive scans of the tile counts give every tile its first
 //           token and first line;
 //   pass 2  per tile: a block scan places every token and line; each thread
-//           folds its 16 digits into values, continuing a number that began
-//           in the previous thread's bytes, and the tile's tokens and line
-//           starts are staged in shared memory and stored contiguously.
+//           parses the digit runs that end in its 16 bytes eight digits at a
+//           time, continuing a number that began in the previous thread's
+//           bytes, and the tile's tokens and line starts are staged in shared
+//           memory and stored contiguously.
 // A token belongs to the thread holding its last digit.  Byte classes are
 // computed four bytes at a time and kept as 16-bit masks (bit k = byte k of
 // the thread's chunk).
@@ -147,20 +148,49 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_count(const uint8_t* __
     }
 }
 
-// Folds the chunk's digits into numbers: acc / nd carry the run that reaches
-// the chunk from the left; every token end stores its value (through emit).
-// Returns with acc / nd holding the run that leaves the chunk on the right.
-template <typename Emit>
-__device__ __forceinline__ void fold_digits(const uint32_t (&w)[4], uint32_t digit_mask, uint32_t end_mask,
-                                            unsigned long long& acc, uint32_t& nd, Emit&& emit) {
-#pragma unroll
-    for (int k = 0; k < PARSE_BYTES; ++k) {
-        const uint32_t d = ((w[k >> 2] >> (8 * (k & 3))) & 0xFFu) - '0';
-        const bool isd = (digit_mask >> k) & 1u;
-        acc = isd ? acc * 10u + d : 0ull;
-        nd = isd ? min(nd + 1u, 11u) : 0u;
-        if ((end_mask >> k) & 1u) emit(k, acc, nd);
+// Eight bytes of the 16-byte chunk (lo = bytes 0..7, hi = 8..15) from byte s,
+// byte s in the low byte (zeros past the chunk).
+__device__ __forceinline__ uint64_t bytes_from(uint64_t lo, uint64_t hi, uint32_t s) {
+    if (s == 0) return lo;
+    if (s < 8) return (lo >> (8 * s)) | (hi << (64 - 8 * s));
+    return hi >> (8 * (s - 8));
+}
+
+// Value of len (1..8) ASCII digits in the low bytes of x, the first digit in
+// the lowest byte: the digits are moved to the top bytes over a '0' fill, then
+// combined pairwise, four-wise and eight-wise with three multiplies (the
+// published SWAR method of simdjson's parse_eight_digits_unrolled).
+__device__ __forceinline__ uint32_t digits8(uint64_t x, uint32_t len) {
+    uint64_t y = len == 8 ? x : (x << (8 * (8 - len))) | (0x3030303030303030ull >> (8 * len));
+    y -= 0x3030303030303030ull;
+    y = ((y & 0x0F0F0F0F0F0F0F0Full) * 2561ull) >> 8;
+    y = ((y & 0x00FF00FF00FF00FFull) * 6553601ull) >> 16;
+    return (uint32_t)(((y & 0x0000FFFF0000FFFFull) * 42949672960001ull) >> 32);
+}
+
+// Value of the digit run of len (1..10) bytes starting at byte s.
+__device__ __forceinline__ unsigned long long run_value(uint64_t lo, uint64_t hi, uint32_t s, uint32_t len) {
+    if (len <= 8) return digits8(bytes_from(lo, hi, s), len);
+    return (unsigned long long)digits8(bytes_from(lo, hi, s), len - 8) * 100000000ull +
+           digits8(bytes_from(lo, hi, s + len - 8), 8);
+}
+
+// The digit run that leaves the chunk on the right (nd = 0: none; nd = 11:
+// more than ten digits, an error wherever the number ends).
+__device__ __forceinline__ void right_run(uint32_t digit, uint64_t lo, uint64_t hi, unsigned long long& acc,
+                                          uint32_t& nd) {
+    acc = 0;
+    nd = 0;
+    if (!(digit & 0x8000u)) return;
+    const uint32_t nond = ~digit & 0xFFFFu;
+    const uint32_t s = nond ? 32u - __clz(nond) : 0u;  // one past the last non-digit
+    const uint32_t len = PARSE_BYTES - s;
+    if (s == 0 || len > 10) {
+        nd = 11;
+        return;
     }
+    acc = run_value(lo, hi, s, len);
+    nd = len;
 }
 
 __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __restrict__ t, uint64_t n,
@@ -203,29 +233,41 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
         sm &= sm - 1;
         s_line[line++] = tok_first + tok0 + __popc(ends & ((1u << k) - 1u));
     }
-    // one pass over the chunk's digits; the first token's leading digits
-    // (lead_len of them, value lead) wait for the run carried in from the left
-    unsigned long long acc = 0, lead = 0;
-    uint32_t nd = 0, lead_len = 0, tok = tok0, bad = 0;
+    // every token ending here: its run of digits [s, k] parsed eight digits at a
+    // time; a run from byte 0 may continue a number of the previous chunk and
+    // waits for the carry (lead_len digits, value lead)
+    const uint64_t lo = w[0] | (uint64_t)w[1] << 32, hi = w[2] | (uint64_t)w[3] << 32;
+    unsigned long long lead = 0;
+    uint32_t lead_len = 0, tok = tok0, bad = 0;
     int bad_k = PARSE_BYTES;
-    const bool starts_in_run = m.digit & 1u;
-    fold_digits(w, m.digit, ends, acc, nd, [&](int k, unsigned long long v, uint32_t digits) {
-        if (tok == tok0 && starts_in_run && digits == (uint32_t)k + 1) {
+    uint32_t e = ends;
+    while (e) {
+        const int k = __ffs(e) - 1;
+        e &= e - 1;
+        const uint32_t below = ~m.digit & ((1u << k) - 1u);
+        const uint32_t st = below ? 32u - __clz(below) : 0u;
+        const uint32_t len = (uint32_t)k - st + 1u;
+        unsigned long long v = 0;
+        if (len <= 10) v = run_value(lo, hi, st, len);
+        if (st == 0 && (m.digit & 1u)) {
             lead = v;
-            lead_len = digits;
-        } else if (digits > 10 || v > 0xFFFFFFFFull) {
+            lead_len = len;
+        } else if (len > 10 || v > 0xFFFFFFFFull) {
             bad = PARSE_E_RANGE;
             bad_k = min(bad_k, k);
         }
         s_tok[tok++] = (uint32_t)v;
-    });
+    }
     // carry in: the previous chunk's right run (lane - 1; the previous warp's last
     // lane through shared memory; the previous tile's last chunk from memory)
-    unsigned long long cacc = __shfl_up_sync(FULL, acc, 1);
-    uint32_t cnd = __shfl_up_sync(FULL, nd, 1);
+    unsigned long long racc;
+    uint32_t rnd;
+    right_run(m.digit, lo, hi, racc, rnd);
+    unsigned long long cacc = __shfl_up_sync(FULL, racc, 1);
+    uint32_t cnd = __shfl_up_sync(FULL, rnd, 1);
     if (lane == 31) {
-        tail_acc[warp] = acc;
-        tail_nd[warp] = nd;
+        tail_acc[warp] = racc;
+        tail_nd[warp] = rnd;
     }
     __syncthreads();
     if (lane == 0) {
@@ -239,13 +281,13 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
                 uint32_t pw[4];
                 Masks pm;
                 load_chunk(t, n, base - PARSE_BYTES, pw, pm);
-                fold_digits(pw, pm.digit, 0u, cacc, cnd, [](int, unsigned long long, uint32_t) {});
+                right_run(pm.digit, pw[0] | (uint64_t)pw[1] << 32, pw[2] | (uint64_t)pw[3] << 32, cacc, cnd);
             }
         }
     }
     if (lead_len) {  // the first token ends here with lead_len digits from byte 0
         unsigned long long p10 = 1;
-        for (uint32_t q = 0; q < lead_len; ++q) p10 *= 10u;
+        for (uint32_t q = 0; q < lead_len && q < 11; ++q) p10 *= 10u;
         const unsigned long long v = cacc * p10 + lead;
         const uint32_t digits = cnd + lead_len;
         if (digits > 10 || v > 0xFFFFFFFFull) {
