@@ -365,11 +365,18 @@ hyset_status build_groups(hyset_ctx* ctx, hyset_coll* c, const uint32_t* d_pre, 
     return HYSET_OK;
 }
 
-// Signatures are regenerated on every join (the buffer is reused).
-hyset_status get_bitmaps(hyset_ctx* ctx, hyset_coll* c, int words, const uint64_t** out) {
+// Signatures are regenerated on every join (the buffer is reused); the buffer
+// is sized on the context's stream, the generation runs on `gen` (default: the
+// same stream).
+hyset_status get_bitmaps(hyset_ctx* ctx, hyset_coll* c, int words, const uint64_t** out,
+                         cudaStream_t gen = nullptr) {
     DevBuf& d = c->bitmaps[words];
     CK(d.ensure((size_t)c->n * words * 8 + 8, ctx->stream));
-    CK(generate_bitmaps(c->view(), words, d.as<uint64_t>(), ctx->stream));
+    if (gen && gen != ctx->stream) {
+        CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
+        CK(cudaStreamWaitEvent(gen, ctx->ev_fork, 0));
+    }
+    CK(generate_bitmaps(c->view(), words, d.as<uint64_t>(), gen ? gen : ctx->stream));
     *out = d.as<uint64_t>();
     return HYSET_OK;
 }
@@ -816,20 +823,25 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
         T.universe = U;
         T.self = self ? 1 : 0;
         T.grab = 16;
-    } else if (tech == HYSET_TECH_FGSS) {
-        ST(build_fgss_indexes(ctx, R, b, self, R->index, R->index_mid, P));
-        if (P.X2.set) P.grab = std::min<uint32_t>(P.grab, 16);  // two bands per probe share a warp batch
     }
+    // signatures do not depend on the index: they are generated on the
+    // auxiliary stream while the index builds on the context's stream
     const int words = (int)(tn.bits / 64);
     if (words) {
         const uint64_t *br = nullptr, *bs = nullptr;
-        ST(get_bitmaps(ctx, R, words, &br));
+        ST(get_bitmaps(ctx, R, words, &br, ctx->aux));
         if (self) bs = br;
-        else ST(get_bitmaps(ctx, S, words, &bs));
+        else ST(get_bitmaps(ctx, S, words, &bs, ctx->aux));
+        CK(cudaEventRecord(ctx->ev_join, ctx->aux));
         P.bits_R = br;
         P.bits_S = bs;
         P.words = words;
     }
+    if (!token_major && tech == HYSET_TECH_FGSS) {
+        ST(build_fgss_indexes(ctx, R, b, self, R->index, R->index_mid, P));
+        if (P.X2.set) P.grab = std::min<uint32_t>(P.grab, 16);  // two bands per probe share a warp batch
+    }
+    if (words) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     int ktech = tech == HYSET_TECH_FGSS ? TECH_FGSS : (tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
     if (token_major) {
         T.bits_R = P.bits_R;
@@ -1159,6 +1171,9 @@ hyset_status hyset_create(int device, hyset_ctx** out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ek0);
@@ -1193,6 +1208,12 @@ void hyset_destroy(hyset_ctx* ctx) {
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
     }
+    if (ctx->aux) {
+        cudaStreamSynchronize(ctx->aux);
+        cudaStreamDestroy(ctx->aux);
+    }
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->ek0) cudaEventDestroy(ctx->ek0);

@@ -117,6 +117,8 @@ struct hyset_ctx {
     int sm_count = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ek0 = nullptr, ek1 = nullptr;
+    cudaStream_t aux = nullptr;                         // work that overlaps the index build
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // fork to / join from aux
     std::string err;
     std::map<std::tuple<int, double, uint32_t, int>, std::unique_ptr<hs::Bounds>> bounds;
     // scratch reused across joins; a batch being prepared points sc at its own

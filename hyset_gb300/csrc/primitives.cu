@@ -101,21 +101,38 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_upsweep(const uint32_t*
 
 // Stable scatter: an item's rank inside its tile is the number of equal digits
 // before it (warp w owns items [w*512, w*512+512) of the tile, processed in
-// order, 32 at a time, peers found with __match_any_sync).
+// order, 32 at a time, peers found with __match_any_sync).  The tile is first
+// reordered by digit in shared memory, so each digit's run of the tile leaves
+// as consecutive addresses (coalesced stores instead of one sector per item).
+constexpr int RADIX_THREAD_BINS = RADIX_BINS / RADIX_THREADS;  // 4
+struct RadixSmem {
+    union {
+        uint32_t whist[RADIX_WARPS][RADIX_BINS];  // per-warp digit counts, then per-warp bases
+        struct {
+            uint32_t k[RADIX_TILE], v[RADIX_TILE];  // the tile ordered by digit
+        } tile;
+    } u;
+    uint32_t start[RADIX_BINS];  // tile-local first position of each digit
+    uint32_t gpos[RADIX_BINS];   // global first position of each digit for this tile
+    uint32_t wsum[RADIX_WARPS];
+};
+
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_t* __restrict__ keys,
                                                                    const uint32_t* __restrict__ vals, uint64_t n,
                                                                    int shift, uint32_t mask,
                                                                    const uint32_t* __restrict__ tile_off,
                                                                    uint32_t tiles, uint32_t* keys_out,
                                                                    uint32_t* vals_out) {
-    __shared__ uint32_t whist[RADIX_WARPS][RADIX_BINS];
+    extern __shared__ __align__(16) uint8_t radix_smem[];
+    RadixSmem& sm = *reinterpret_cast<RadixSmem*>(radix_smem);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t bins = mask + 1;
-    for (uint32_t d = threadIdx.x; d < bins; d += RADIX_THREADS)
+    for (uint32_t d = threadIdx.x; d < RADIX_BINS; d += RADIX_THREADS)
 #pragma unroll
-        for (int w = 0; w < RADIX_WARPS; ++w) whist[w][d] = 0;
+        for (int w = 0; w < RADIX_WARPS; ++w) sm.u.whist[w][d] = 0;
     __syncthreads();
-    uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE + (uint64_t)warp * (32 * RADIX_ROUNDS);
+    const uint64_t tile_base = (uint64_t)blockIdx.x * RADIX_TILE;
+    const uint64_t base = tile_base + (uint64_t)warp * (32 * RADIX_ROUNDS);
     uint32_t k[RADIX_ROUNDS], v[RADIX_ROUNDS], rank[RADIX_ROUNDS];
 #pragma unroll
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
@@ -125,34 +142,69 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_
         uint32_t d = valid ? ((key >> shift) & mask) : 0xFFFFFFFFu;
         unsigned peers = __match_any_sync(FULL, d);
         int leader = __ffs(peers) - 1;
-        uint32_t cnt = valid ? whist[warp][d] : 0;
+        uint32_t cnt = valid ? sm.u.whist[warp][d] : 0;
         __syncwarp();
-        if (valid && lane == leader) whist[warp][d] = cnt + __popc(peers);
+        if (valid && lane == leader) sm.u.whist[warp][d] = cnt + __popc(peers);
         __syncwarp();
         rank[r] = cnt + __popc(peers & lanemask_lt(lane));
         k[r] = key;
         v[r] = valid ? vals[idx] : 0;
     }
     __syncthreads();
-    for (uint32_t d = threadIdx.x; d < bins; d += RADIX_THREADS) {
-        uint32_t run = tile_off[(uint64_t)d * tiles + blockIdx.x];
+    // per digit: warp bases (exclusive over warps) and the digit's tile total;
+    // thread t owns digits [4t, 4t+4)
+    uint32_t tot[RADIX_THREAD_BINS], run = 0;
+#pragma unroll
+    for (int j = 0; j < RADIX_THREAD_BINS; ++j) {
+        const uint32_t d = threadIdx.x * RADIX_THREAD_BINS + j;
+        uint32_t acc = 0;
 #pragma unroll
         for (int w = 0; w < RADIX_WARPS; ++w) {
-            uint32_t t = whist[w][d];
-            whist[w][d] = run;
-            run += t;
+            const uint32_t c = sm.u.whist[w][d];
+            sm.u.whist[w][d] = acc;
+            acc += c;
         }
+        tot[j] = acc;
+        run += acc;
+    }
+    // block exclusive scan of the per-thread digit totals -> tile-local digit starts
+    const uint32_t incl = warp_incl_scan(run, lane);
+    if (lane == 31) sm.wsum[warp] = incl;
+    __syncthreads();
+    uint32_t before = incl - run;
+    for (int w = 0; w < warp; ++w) before += sm.wsum[w];
+#pragma unroll
+    for (int j = 0; j < RADIX_THREAD_BINS; ++j) {
+        const uint32_t d = threadIdx.x * RADIX_THREAD_BINS + j;
+        sm.start[d] = before;
+        sm.gpos[d] = d < bins ? tile_off[(uint64_t)d * tiles + blockIdx.x] : 0u;
+        before += tot[j];
+    }
+    __syncthreads();
+    // tile-local sorted position of every item (registers), then the tile in
+    // digit order over the (now free) counts
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {  // rank becomes the tile-local position
+        const uint64_t idx = base + (uint64_t)r * 32 + lane;
+        const uint32_t d = (k[r] >> shift) & mask;
+        rank[r] = idx < n ? sm.start[d] + sm.u.whist[warp][d] + rank[r] : 0xFFFFFFFFu;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
-        uint64_t idx = base + (uint64_t)r * 32 + lane;
-        if (idx < n) {
-            uint32_t d = (k[r] >> shift) & mask;
-            uint32_t pos = whist[warp][d] + rank[r];
-            keys_out[pos] = k[r];
-            vals_out[pos] = v[r];
+        if (rank[r] != 0xFFFFFFFFu) {
+            sm.u.tile.k[rank[r]] = k[r];
+            sm.u.tile.v[rank[r]] = v[r];
         }
+    }
+    __syncthreads();
+    const uint32_t in_tile = n - tile_base < RADIX_TILE ? (uint32_t)(n - tile_base) : RADIX_TILE;
+    for (uint32_t i = threadIdx.x; i < in_tile; i += RADIX_THREADS) {
+        const uint32_t key = sm.u.tile.k[i];
+        const uint32_t d = (key >> shift) & mask;
+        const uint32_t pos = sm.gpos[d] + (i - sm.start[d]);
+        keys_out[pos] = key;
+        vals_out[pos] = sm.u.tile.v[i];
     }
 }
 
@@ -387,7 +439,8 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
         if (e != cudaSuccess) return e;
         e = scan_exclusive(tile_counts, tile_counts, counts, scan_tmp, s);
         if (e != cudaSuccess) return e;
-        k_radix_downsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, vin, n, shift, mask, tile_counts, tiles, kout, vout);
+        k_radix_downsweep<<<tiles, RADIX_THREADS, sizeof(RadixSmem), s>>>(kin, vin, n, shift, mask, tile_counts,
+                                                                          tiles, kout, vout);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         uint32_t* t;
