@@ -60,6 +60,28 @@ __device__ __forceinline__ uint32_t lower_bound_u32(const uint32_t* a, uint32_t 
     return lo;
 }
 
+// Two lower bounds over the same sorted range, searched in lockstep: each
+// step issues both probes' loads together, so the two dependent chains cost
+// one chain's latency.
+__device__ __forceinline__ void lower_bound2_u32(const uint32_t* __restrict__ a, uint32_t lo, uint32_t hi,
+                                                 uint32_t k1, uint32_t k2, uint32_t& r1, uint32_t& r2) {
+    uint32_t l1 = lo, h1 = hi, l2 = lo, h2 = hi;
+    while (l1 < h1 || l2 < h2) {
+        const uint32_t m1 = (l1 + h1) >> 1, m2 = (l2 + h2) >> 1;
+        const uint32_t v1 = l1 < h1 ? __ldg(a + m1) : 0u, v2 = l2 < h2 ? __ldg(a + m2) : 0u;
+        if (l1 < h1) {
+            if (v1 < k1) l1 = m1 + 1;
+            else h1 = m1;
+        }
+        if (l2 < h2) {
+            if (v2 < k2) l2 = m2 + 1;
+            else h2 = m2;
+        }
+    }
+    r1 = l1;
+    r2 = l2;
+}
+
 __device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v, int lane) {
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {

@@ -199,8 +199,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                         b1 = b0 + nhi;
                         b0 = b0 + nlo;
                     } else {
-                        b0 = lower_bound_u32(x_set, b0, b1, klo);
-                        b1 = lower_bound_u32(x_set, b0, b1, khi);
+                        lower_bound2_u32(x_set, b0, b1, klo, khi, b0, b1);
                     }
                 }
                 first = b0;
