@@ -275,7 +275,7 @@ def run_ours(args, ws, rank, local):
             h.close()
         plain_ms = 1000.0 * min(plain) if plain else None
         peak, peak_kind = measured_peaks()
-        words = (args.bitmap // 64) if args.bitmap else 0
+        words = st_run.bitmap_bits // 64
         st = st_run.stats
         alg = algorithmic_bytes(st, st_run.count, words, p_hi - p_lo)
         kms = statistics.mean(kern_ms)
@@ -291,7 +291,7 @@ def run_ours(args, ws, rank, local):
                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "strong",
                "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
                "config": {"workload": WORKLOAD, "threshold": THRESHOLD, "sim": "jaccard",
-                          "technique": r.technique, "bitmap_bits": args.bitmap, "result_pairs": total_pairs,
+                          "technique": r.technique, "bitmap_bits": r.bitmap_bits, "result_pairs": total_pairs,
                           "parallelism": f"probe shards x{ws}" if ws > 1 else "single GPU",
                           "l2": "512 MB buffer written between timed steps; tokens 449 MB > L2",
                           "plain_block_pair_ms": plain_ms,
@@ -473,7 +473,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--technique", default="auto")
-    ap.add_argument("--bitmap", type=int, default=256)
+    ap.add_argument("--bitmap", type=int, default=0, help="signature bits; 0 = the library's autotuner")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the block-pair baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")

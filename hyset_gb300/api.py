@@ -30,6 +30,7 @@ class JoinResult:
     device_pairs: int = 0  # device address when device_pairs was requested
     launches: int = 0      # kernel launches the join issued
     selector: str = "explicit"  # which selector chose the technique
+    bitmap_bits: int = 0        # signature width the join ran with
 
 
 # R-S joins: which collection is indexed (hyset_join_opts.orientation)
@@ -67,7 +68,8 @@ def _take_result(lib, r) -> JoinResult:
         return JoinResult(int(n), pairs, TECH_NAMES.get(lib.hyset_result_technique(r), "?"),
                           float(lib.hyset_result_device_ms(r)), float(lib.hyset_result_kernel_ms(r)),
                           [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0),
-                          int(lib.hyset_result_launches(r)), SELECTOR_NAMES.get(lib.hyset_result_selector(r), "?"))
+                          int(lib.hyset_result_launches(r)), SELECTOR_NAMES.get(lib.hyset_result_selector(r), "?"),
+                          int(lib.hyset_result_bitmap_bits(r)))
     finally:
         lib.hyset_result_free(r)
 

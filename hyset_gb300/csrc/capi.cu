@@ -398,7 +398,7 @@ hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
 // The autotuner's per-join configuration (technique, kernel variant, signature
 // width, batch, verification mode).  Explicit options always win; AUTO fills
 // the rest from collection statistics with rules measured on GB300
-// (1M-set long-set workload: probe-major, batch 4, 256-bit signatures; 200K-set
+// (1M-set long-set workload: probe-major, batch 2, 256-bit signatures; 200K-set
 // short-set workload: 128-bit signatures; token-major only on request, it wins
 // only where every token group is small, i.e. high thresholds; enumerating the
 // length window only for small collections).
@@ -420,7 +420,7 @@ Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o,
     if (t.tech == HYSET_TECH_AUTO) t.tech = (pairs_window <= 4000000ull) ? HYSET_TECH_BITMAP : HYSET_TECH_FGSS;
     // explicit FGSS defaults to the token-major kernel; AUTO to probe-major
     t.probe_major = (o->technique == HYSET_TECH_FGSS && !o->probe_major) ? 0 : 1;
-    t.batch = o->fgss_batch ? o->fgss_batch : 4;
+    t.batch = o->fgss_batch ? o->fgss_batch : 2;
     t.bits = o->bitmap_bits;
     if (o->technique == HYSET_TECH_AUTO && t.bits == 0) t.bits = avg <= 48.0 ? 128 : 256;
     if (t.tech == HYSET_TECH_BITMAP && t.bits == 0) t.bits = 64;
@@ -692,10 +692,12 @@ hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
 // Autotuner for the prefix-index join's signature width: on the first AUTO join
 // of a (collections, similarity, threshold), the probe-major kernel runs on
 // three probe samples spread over the probe range with no signatures and with
-// 128-, 256- and 512-bit signatures, and the fastest width is kept for that
-// join.  Measured on GB300: 256 bits wins on long sets at high thresholds, 512
+// 128-, 256- and 512-bit signatures; the samples' time scaled to the whole
+// probe range plus the width's signature generation decides, and the width is
+// kept for that join.  Measured on GB300: 256 bits wins on long sets at high thresholds, 512
 // on long sets at low thresholds, 128 on short ones, none on some collections.
-constexpr uint32_t TUNE_MIN_PROBES = 20000, TUNE_SAMPLE = 2048;
+constexpr uint32_t TUNE_MIN_PROBES = 60000, TUNE_SAMPLE = 16384;  // a sample fills the GPU for about two waves
+constexpr float TUNE_MARGIN = 0.92f;  // leave the rule's width only for an estimated gain of 8 % or more
 
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
                            bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits) {
@@ -722,25 +724,33 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     P.out = Sink{nullptr, ctx->s_count.as<unsigned long long>(), 0, 1};
     P.work = ctx->s_work.as<unsigned int>();
     const uint32_t cand[4] = {0, 128, 256, 512};
+    float est[4] = {0, 0, 0, 0};
     float best_ms = 0;
     uint32_t best = 256;
     for (int k = 0; k < 4; ++k) {
         const int words = (int)(cand[k] / 64);
         P.words = words;
         P.bits_R = P.bits_S = nullptr;
+        float gen_ms = 0;  // the width's signature generation, paid once per join
         if (words) {
             const uint64_t *br = nullptr, *bs = nullptr;
+            CK(cudaEventRecord(ctx->ek0, s));
             ST(get_bitmaps(ctx, R, words, &br));
             if (self) bs = br;
             else ST(get_bitmaps(ctx, S, words, &bs));
+            CK(cudaEventRecord(ctx->ek1, s));
+            CK(cudaEventSynchronize(ctx->ek1));
+            CK(cudaEventElapsedTime(&gen_ms, ctx->ek0, ctx->ek1));
             P.bits_R = br;
             P.bits_S = bs;
         }
         float total = 0;
+        uint32_t sampled = 0;
         for (int c = 0; c < 3; ++c) {  // samples at the start, middle and end of the probe range
             const uint32_t span = p_hi - p_lo, len = std::min(TUNE_SAMPLE, span / 3);
             P.p_lo = p_lo + (uint32_t)((uint64_t)(span - len) * c / 2);
             P.p_hi = P.p_lo + len;
+            sampled += len;
             CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
             CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
             CK(cudaEventRecord(ctx->ek0, s));
@@ -751,11 +761,18 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
             CK(cudaEventElapsedTime(&ms, ctx->ek0, ctx->ek1));
             total += ms;
         }
+        // the whole probe range's estimated kernel time plus the generation
+        total = total * (float)(p_hi - p_lo) / (float)(sampled ? sampled : 1) + gen_ms;
+        est[k] = total;
         if (k == 0 || total < best_ms) {
             best_ms = total;
             best = cand[k];
         }
     }
+    // the rule's width (mean size <= 48: 128 bits, else 256) unless another is clearly faster
+    const uint32_t rule = (double)R->n_tokens / (double)std::max<uint32_t>(R->n, 1) <= 48.0 ? 128u : 256u;
+    const float rule_ms = est[rule == 128u ? 1 : 2];
+    if (best != rule && best_ms > TUNE_MARGIN * rule_ms) best = rule;
     ctx->bits_cache[key] = best;
     *bits = best;
     return HYSET_OK;
@@ -781,6 +798,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
             a_hi - a_lo >= TUNE_MIN_PROBES)
             ST(autotune_bits(ctx, R, S, o, b, self, a_lo, a_hi, &tn.bits));
     }
+    res->bitmap_bits = tech == HYSET_TECH_DIRECT ? 0 : tn.bits;
     if (o->probe_end > S->n || o->probe_begin > o->probe_end)
         return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
     const unsigned long long launches0 = launches();
@@ -1170,6 +1188,7 @@ hyset_status hyset_create(int device, hyset_ctx** out) {
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = prepare_kernels();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming);
@@ -1482,6 +1501,7 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
         out[j] = std::make_unique<hyset_result>();
         hyset_result* r = out[j].get();
         r->technique = bj.tech;
+        r->bitmap_bits = (uint32_t)bj.words * 64u;
         r->device_ms = ms;  // the whole batch: one launch sequence
         r->count = counts[j];
         if (!bj.o.count_only && counts[j] > bj.cap) {
@@ -1663,6 +1683,7 @@ const hyset_pair* hyset_result_pairs(const hyset_result* r) {
 }
 uint64_t hyset_result_launches(const hyset_result* r) { return r ? r->launches : 0; }
 hyset_technique hyset_result_technique(const hyset_result* r) { return r ? r->technique : HYSET_TECH_AUTO; }
+uint32_t hyset_result_bitmap_bits(const hyset_result* r) { return r ? r->bitmap_bits : 0; }
 double hyset_result_device_ms(const hyset_result* r) { return r ? r->device_ms : 0.0; }
 double hyset_result_kernel_ms(const hyset_result* r) { return r ? r->kernel_ms : 0.0; }
 const void* hyset_result_device_pairs(const hyset_result* r) { return r ? r->device_pairs : nullptr; }

@@ -165,6 +165,7 @@ struct hyset_result {
     int has_pairs = 0;
     const void* device_pairs = nullptr;
     hyset_technique technique = HYSET_TECH_AUTO;
+    uint32_t bitmap_bits = 0;  // signature width the join ran with
     double device_ms = 0;
     double kernel_ms = 0;
     uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};

@@ -29,7 +29,7 @@ namespace hs {
 
 namespace {
 
-template <int TECH, int VMODE, int W>
+template <int TECH, int VMODE, int W, bool ST>
 __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinParams P) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -44,9 +44,9 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
         const uint32_t end = min(nprobe, i + grab);
         // largest sets first: the heaviest probes start early, the tail is light
         if constexpr (TECH == TECH_FGSS) {
-            fgss_batch<VMODE, W>(P, i, end - i, lane);
+            fgss_batch<VMODE, W, ST>(P, i, end - i, lane);
         } else {
-            for (; i < end; ++i) enum_probe<VMODE, W>(P, P.p_hi - 1 - i, sbuf, lane);
+            for (; i < end; ++i) enum_probe<VMODE, W, ST>(P, P.p_hi - 1 - i, sbuf, lane);
         }
     }
 }
@@ -125,16 +125,22 @@ cudaError_t launch_persistent(K kernel, int sm_count, cudaStream_t s, const Join
     return cudaGetLastError();
 }
 
-template <int TECH, int VMODE>
-cudaError_t dispatch_words(const JoinParams& P, int sm_count, cudaStream_t s) {
+template <int TECH, int VMODE, bool ST>
+cudaError_t dispatch_words_st(const JoinParams& P, int sm_count, cudaStream_t s) {
     switch (P.bits_R ? P.words : 0) {
-    case 0: return launch_persistent(k_join<TECH, VMODE, 0>, sm_count, s, P);
-    case 1: return launch_persistent(k_join<TECH, VMODE, 1>, sm_count, s, P);
-    case 2: return launch_persistent(k_join<TECH, VMODE, 2>, sm_count, s, P);
-    case 4: return launch_persistent(k_join<TECH, VMODE, 4>, sm_count, s, P);
-    case 8: return launch_persistent(k_join<TECH, VMODE, 8>, sm_count, s, P);
+    case 0: return launch_persistent(k_join<TECH, VMODE, 0, ST>, sm_count, s, P);
+    case 1: return launch_persistent(k_join<TECH, VMODE, 1, ST>, sm_count, s, P);
+    case 2: return launch_persistent(k_join<TECH, VMODE, 2, ST>, sm_count, s, P);
+    case 4: return launch_persistent(k_join<TECH, VMODE, 4, ST>, sm_count, s, P);
+    case 8: return launch_persistent(k_join<TECH, VMODE, 8, ST>, sm_count, s, P);
     default: return cudaErrorInvalidValue;
     }
+}
+
+template <int TECH, int VMODE>
+cudaError_t dispatch_words(const JoinParams& P, int sm_count, cudaStream_t s) {
+    return P.stats ? dispatch_words_st<TECH, VMODE, true>(P, sm_count, s)
+                   : dispatch_words_st<TECH, VMODE, false>(P, sm_count, s);
 }
 
 }  // namespace

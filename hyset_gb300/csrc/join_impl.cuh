@@ -31,7 +31,11 @@ __device__ __forceinline__ Window candidate_window(const JoinParams& P, uint32_t
     return w;
 }
 
+// ST (compile time): the launch collects work counters.  Without them the
+// counter code is not compiled in at all.
+template <bool ST>
 __device__ __forceinline__ void count_stat(const JoinParams& P, int k, uint32_t v, int lane) {
+    if constexpr (!ST) return;
     if (P.stats == nullptr) return;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
@@ -39,7 +43,9 @@ __device__ __forceinline__ void count_stat(const JoinParams& P, int k, uint32_t 
 }
 
 // Per-lane counter update (divergent-safe; stats runs only).
+template <bool ST>
 __device__ __forceinline__ void count_stat_lane(const JoinParams& P, int k, uint32_t v) {
+    if constexpr (!ST) return;
     if (P.stats != nullptr && v) atomicAdd(P.stats + k, (unsigned long long)v);
 }
 
@@ -82,7 +88,7 @@ __device__ __forceinline__ uint32_t bitmap_xor_pop(const JoinParams& P, const ui
 // Verifies the warp's surviving items and appends the accepted pairs.
 // own_a / own_b: the item's position in the probe / candidate (ownership test)
 // or NOWN.
-template <int VMODE>
+template <int VMODE, bool ST>
 __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p, const uint32_t* pg, uint32_t lp,
                                                 uint32_t* sbuf, bool& staged, bool keep, uint32_t cstart,
                                                 uint32_t c, uint32_t lc, uint32_t mo, uint32_t own_a,
@@ -92,7 +98,7 @@ __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p,
     if (m) {
         const bool before = staged;
         const uint32_t* a = stage_probe(pg, lp, sbuf, staged, lane);
-        if (!before) count_stat(P, 4, lane == 0 ? lp : 0u, lane);  // probe tokens read for verification
+        if (!before) count_stat<ST>(P, 4, lane == 0 ? lp : 0u, lane);  // probe tokens read for verification
         if constexpr (VMODE == 1) {
             bool ok = false;
             if (keep) ok = verify_serial(a, lp, P.R.tokens + cstart, lc, mo, own_a, &used);
@@ -113,7 +119,7 @@ __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p,
             }
         }
     }
-    count_stat(P, 6, used, lane);
+    count_stat<ST>(P, 6, used, lane);
 }
 
 // Lane k of the warp holds the k-th value of a non-decreasing inclusive scan;
@@ -137,7 +143,7 @@ __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
 // candidates of probe t at least as long as the probe (its midprefix tokens
 // against the maxprefix index X), lane k + t the shorter ones (its maxprefix
 // tokens against the midprefix index X2).
-template <int VMODE, int W>
+template <int VMODE, int W, bool ST>
 __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
     // lane t < k: probe t of the batch (largest sets first)
     uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
@@ -161,7 +167,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             if (lo < hi) mp = banded && band == 0 ? P.B.mid_prefix[lp] : P.B.probe_prefix[lp];
         }
     }
-    count_stat(P, 4, mp, lane);  // prefix tokens read by the filter
+    count_stat<ST>(P, 4, mp, lane);  // prefix tokens read by the filter
     const uint32_t mp_incl = warp_incl_scan(mp, lane);
     const uint32_t slots = __shfl_sync(FULL, mp_incl, 31);
     for (uint32_t s0 = 0; s0 < slots; s0 += 32) {
@@ -254,8 +260,8 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 mo = minoverlap(P.B, big, small);
                 keep = 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
             }
-            count_stat(P, 0, q < total ? 1u : 0u, lane);
-            count_stat(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
+            count_stat<ST>(P, 0, q < total ? 1u : 0u, lane);
+            count_stat<ST>(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
             if constexpr (W > 4) {
                 if (keep) {
                     const uint64_t* bs = P.bits_S + (uint64_t)ip * W;
@@ -265,8 +271,8 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 }
             }
             if constexpr (W > 0) keep = keep && ilp + lc - pop >= 2u * mo;
-            count_stat(P, 1, keep ? 1u : 0u, lane);
-            count_stat(P, 2, keep ? lc : 0u, lane);
+            count_stat<ST>(P, 1, keep ? 1u : 0u, lane);
+            count_stat<ST>(P, 2, keep ? lc : 0u, lane);
             // ---- verification: the probe is read from HBM/L2 (it was just touched)
             uint32_t used = 0;
             const uint32_t* a = P.S.tokens + ipst;
@@ -289,12 +295,12 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                     emit(P.out, ok && lane == 0, pp, cc, lane);
                 }
             }
-            count_stat(P, 6, used, lane);
+            count_stat<ST>(P, 6, used, lane);
         }
     }
 }
 
-template <int VMODE, int W>
+template <int VMODE, int W, bool ST>
 __device__ void enum_probe(const JoinParams& P, uint32_t p, uint32_t* sbuf, int lane) {
     const uint2 pm = P.S.meta[p];
     const uint32_t lp = pm.y;
@@ -320,11 +326,11 @@ __device__ void enum_probe(const JoinParams& P, uint32_t p, uint32_t* sbuf, int 
             mo = minoverlap(P.B, big, small);
             keep = bitmap_pass<W>(P, bp, c, lp, lc, mo);
         }
-        count_stat(P, 0, c < win.hi ? 1u : 0u, lane);
-        count_stat(P, 5, (W > 0 && c < win.hi) ? 1u : 0u, lane);
-        count_stat(P, 1, keep ? 1u : 0u, lane);
-        count_stat(P, 2, keep ? lc : 0u, lane);
-        verify_and_emit<VMODE>(P, p, pg, lp, sbuf, staged, keep, cstart, c, lc, mo, NOWN, NOWN, lane);
+        count_stat<ST>(P, 0, c < win.hi ? 1u : 0u, lane);
+        count_stat<ST>(P, 5, (W > 0 && c < win.hi) ? 1u : 0u, lane);
+        count_stat<ST>(P, 1, keep ? 1u : 0u, lane);
+        count_stat<ST>(P, 2, keep ? lc : 0u, lane);
+        verify_and_emit<VMODE, ST>(P, p, pg, lp, sbuf, staged, keep, cstart, c, lc, mo, NOWN, NOWN, lane);
     }
     __syncwarp();
 }

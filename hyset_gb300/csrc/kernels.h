@@ -10,6 +10,10 @@
 
 namespace hs {
 
+// Per-device kernel attributes (shared-memory opt-ins); call once per device
+// before the first launch (hyset_create does).
+cudaError_t prepare_kernels();
+
 // Kernel launches issued by this library since load (bench bookkeeping).
 unsigned long long launches();
 void note_launches(unsigned n = 1);

@@ -76,9 +76,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const uint32_t* in, 
 
 // ---- radix sort -----------------------------------------------------------
 // Digits of up to 10 bits (a 20-bit token key sorts in two passes).
-constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_THREADS = 512;
 constexpr int RADIX_WARPS = RADIX_THREADS / 32;
-constexpr int RADIX_ROUNDS = 16;                                  // 32-item rounds per warp
+constexpr int RADIX_ROUNDS = 8;                                   // 32-item rounds per warp
 constexpr uint32_t RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;     // 4096
 constexpr int RADIX_MAX_BITS = 10;
 constexpr int RADIX_BINS = 1 << RADIX_MAX_BITS;
@@ -416,6 +416,12 @@ size_t radix_scratch_words(uint64_t n) {
     uint64_t tiles = (n + RADIX_TILE - 1) / RADIX_TILE;
     uint64_t counts = tiles * RADIX_BINS;
     return counts + scan_scratch_words(counts);
+}
+
+cudaError_t prepare_kernels() {
+    // the downsweep's per-warp digit counts need more than the default 48 KB
+    return cudaFuncSetAttribute(k_radix_downsweep, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sizeof(RadixSmem));
 }
 
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, uint64_t n,

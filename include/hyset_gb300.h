@@ -159,6 +159,7 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
 uint64_t hyset_result_count(const hyset_result* r);
 const hyset_pair* hyset_result_pairs(const hyset_result* r); /* NULL when count_only */
 hyset_technique hyset_result_technique(const hyset_result* r);
+uint32_t hyset_result_bitmap_bits(const hyset_result* r);   /* signature width used (0 = none) */
 double hyset_result_device_ms(const hyset_result* r);       /* CUDA-event time of the join's device work */
 double hyset_result_kernel_ms(const hyset_result* r);       /* CUDA-event time of the filter+verify launch */
 /* Device pointer to count (first, second) uint32 pairs when device_pairs was
