@@ -35,7 +35,7 @@ __device__ __forceinline__ void run_unit(const BatchDesc& d, uint32_t i0, uint32
     }
 }
 
-__global__ void __launch_bounds__(JOIN_THREADS) k_batch_join(const BatchDesc* __restrict__ D,
+__global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_batch_join(const BatchDesc* __restrict__ D,
                                                             const uint32_t* __restrict__ unit_off, uint32_t n_joins,
                                                             unsigned int* work) {
     extern __shared__ uint32_t smem[];

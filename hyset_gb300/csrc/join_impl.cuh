@@ -7,9 +7,12 @@ namespace hs {
 namespace {
 
 #ifndef HS_JOIN_MIN_BLOCKS
-#define HS_JOIN_MIN_BLOCKS 1  // resident blocks per SM the join kernel is compiled for
+#define HS_JOIN_MIN_BLOCKS 5  // resident blocks per SM the join kernels are compiled for (48 registers)
 #endif
-constexpr int JOIN_THREADS = 256;
+#ifndef HS_JOIN_THREADS
+#define HS_JOIN_THREADS 256  // threads per block of the join kernels
+#endif
+constexpr int JOIN_THREADS = HS_JOIN_THREADS;
 constexpr int JOIN_WARPS = JOIN_THREADS / 32;
 constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per warp
 constexpr uint32_t SHORT_LIST = 8;   // inverted lists this short are windowed without bisection
