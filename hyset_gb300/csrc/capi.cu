@@ -398,7 +398,7 @@ hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
 // The autotuner's per-join configuration (technique, kernel variant, signature
 // width, batch, verification mode).  Explicit options always win; AUTO fills
 // the rest from collection statistics with rules measured on GB300
-// (1M-set long-set workload: probe-major, batch 2, 256-bit signatures; 200K-set
+// (1M-set long-set workload: probe-major, batch 3, 256-bit signatures; 200K-set
 // short-set workload: 128-bit signatures; token-major only on request, it wins
 // only where every token group is small, i.e. high thresholds; enumerating the
 // length window only for small collections).
@@ -420,7 +420,7 @@ Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o,
     if (t.tech == HYSET_TECH_AUTO) t.tech = (pairs_window <= 4000000ull) ? HYSET_TECH_BITMAP : HYSET_TECH_FGSS;
     // explicit FGSS defaults to the token-major kernel; AUTO to probe-major
     t.probe_major = (o->technique == HYSET_TECH_FGSS && !o->probe_major) ? 0 : 1;
-    t.batch = o->fgss_batch ? o->fgss_batch : 2;
+    t.batch = o->fgss_batch ? o->fgss_batch : 3;
     t.bits = o->bitmap_bits;
     if (o->technique == HYSET_TECH_AUTO && t.bits == 0) t.bits = avg <= 48.0 ? 128 : 256;
     if (t.tech == HYSET_TECH_BITMAP && t.bits == 0) t.bits = 64;

@@ -15,7 +15,10 @@ namespace {
 constexpr int JOIN_THREADS = HS_JOIN_THREADS;
 constexpr int JOIN_WARPS = JOIN_THREADS / 32;
 constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per warp
-constexpr uint32_t SHORT_LIST = 8;   // inverted lists this short are windowed without bisection
+#ifndef HS_SHORT_LIST
+#define HS_SHORT_LIST 8
+#endif
+constexpr uint32_t SHORT_LIST = HS_SHORT_LIST;  // inverted lists this short are windowed without bisection
 
 struct Window {
     uint32_t lo, hi;
