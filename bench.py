@@ -231,20 +231,26 @@ def run_ours(args, ws, rank, local):
         step_ms, total_pairs = mean_ms, counts[0]
     value = total_pairs / (step_ms / 1000.0)
 
-    # e2e through the public API: pinned host arrays -> upload -> join -> pairs to host
+    # e2e through the public C ABI: pinned host arrays -> one upload+join call -> pairs to host
     tok_p = torch.from_numpy(c.tokens).pin_memory()
     siz_p = torch.from_numpy(c.sizes).pin_memory()
     sta_p = torch.from_numpy(c.starts).pin_memory()
     e2e_kw = dict(kw)
     e2e_kw["device_pairs"] = False
+    whole = (p_lo, p_hi) == (0, c.n)
+    if whole:
+        e2e_kw.pop("probe_range")  # one call: upload and join (hyset_self_join_host)
     e2e_s = []
     for i in range(0 if args.no_e2e else args.warmup + args.steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ec = ctx.upload(tok_p.numpy(), siz_p.numpy(), sta_p.numpy())
-        er = ctx.self_join(ec, **e2e_kw)
-        ec.free()
+        if whole:
+            er = ctx.self_join_host(tok_p.numpy(), siz_p.numpy(), sta_p.numpy(), **e2e_kw)
+        else:  # a rank's shard: upload, then the join over its probe range
+            ec = ctx.upload(tok_p.numpy(), siz_p.numpy(), sta_p.numpy())
+            er = ctx.self_join(ec, **e2e_kw)
+            ec.free()
         dt = time.perf_counter() - t0
         if i >= args.warmup:
             e2e_s.append(dt)

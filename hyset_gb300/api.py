@@ -192,6 +192,26 @@ class Context:
         check(self._lib.hyset_self_join(self.handle, coll.handle, C.byref(o), C.byref(r)), self.handle)
         return _take_result(self._lib, r)
 
+    def self_join_host(self, tokens, sizes, starts=None, threshold: float = 0.8, keep_collection: bool = False,
+                       **kw):
+        """Upload and self-join in one call from host arrays (hyset_self_join_host):
+        the copy overlaps the checks and the index build.  Returns the result, or
+        (result, DeviceCollection) with keep_collection."""
+        tok = np.ascontiguousarray(tokens, dtype=np.uint32)
+        sz = np.ascontiguousarray(sizes, dtype=np.uint32)
+        st = None if starts is None else np.ascontiguousarray(starts, dtype=np.uint32)
+        o = make_opts(threshold, **kw)
+        r = C.c_void_p()
+        h = C.c_void_p()
+        check(self._lib.hyset_self_join_host(
+            self.handle, tok.ctypes.data_as(U32P), tok.size, None if st is None else st.ctypes.data_as(U32P),
+            sz.ctypes.data_as(U32P), sz.size, C.byref(o), C.byref(h) if keep_collection else None, C.byref(r)),
+            self.handle)
+        res = _take_result(self._lib, r)
+        if keep_collection:
+            return res, DeviceCollection(self, h, int(sz.size))
+        return res
+
     def rs_join(self, indexed: DeviceCollection, probe: DeviceCollection, threshold: float = 0.8,
                 **kw) -> JoinResult:
         o = make_opts(threshold, **kw)

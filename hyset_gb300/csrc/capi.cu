@@ -305,7 +305,7 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
                            ctx->sc->pos.as<uint32_t>(), s));
     uint32_t* counts = ctx->sc->counts.as<uint32_t>();
     CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
-    CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, s));
+    CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
     CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
     CK(iota_u32(ctx->sc->order.as<uint32_t>(), E, s));
     CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ctx->sc->order.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
@@ -614,8 +614,8 @@ std::string coll_signature(const hyset_coll* c) {
         h *= 1099511628211ull;
     }
     char buf[96];
-    std::snprintf(buf, sizeof buf, "%u:%llu:%u:%u:%016llx", c->n, (unsigned long long)c->n_tokens, c->universe,
-                  c->max_size, (unsigned long long)h);
+    std::snprintf(buf, sizeof buf, "%u:%llu:%u:%016llx", c->n, (unsigned long long)c->n_tokens, c->max_size,
+                  (unsigned long long)h);
     return buf;
 }
 
@@ -1232,6 +1232,7 @@ void hyset_destroy(hyset_ctx* ctx) {
         cudaStreamDestroy(ctx->aux);
     }
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    for (cudaEvent_t e : ctx->pipe_ev) cudaEventDestroy(e);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -1473,6 +1474,286 @@ hyset_status hyset_rs_join(hyset_ctx* ctx, const hyset_coll* indexed, const hyse
     hyset_coll* S = const_cast<hyset_coll*>(probe);
     if (R == S) return fail(ctx, HYSET_E_INVALID, "use hyset_self_join for R join R");
     ST(do_join(ctx, R, S, opts, res.get()));
+    *out = res.release();
+    return HYSET_OK;
+}
+
+// ---------------------------------------------------------------- joins from host arrays
+
+namespace {
+constexpr uint64_t PIPE_CHUNK_TOKENS = 16ull << 20;  // 64 MB of tokens per copy chunk
+
+cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k) {
+    while (ctx->pipe_ev.size() <= k) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        ctx->pipe_ev.push_back(e);
+    }
+    return ctx->pipe_ev[k];
+}
+}  // namespace
+
+// The upload and the self-join in one call.  The tokens go to the device in
+// 64 MB chunks on the auxiliary stream; while the later chunks are in flight,
+// the sets of the chunks already on the device are checked, their prefix
+// entries emitted and their signatures generated on the context's stream.
+// After the last chunk only the index sort and the join launch remain.  The
+// pipeline needs the join's configuration before the tokens arrive: an explicit
+// probe-major prefix-index join, or one whose technique and signature width
+// the context has already chosen for a collection with the same size profile;
+// every other join runs as hyset_collection_upload + hyset_self_join.
+hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64_t n_tokens, const uint32_t* starts,
+                                  const uint32_t* sizes, uint32_t n_sets, const hyset_join_opts* opts,
+                                  hyset_coll** coll_out, hyset_result** out) {
+    if (!ctx || !out || !opts || (n_sets && (!sizes || (!tokens && n_tokens))))
+        return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    if (coll_out) *coll_out = nullptr;
+    ST(check_opts(ctx, opts));
+    if (n_tokens >= (1ull << 32)) return fail(ctx, HYSET_E_INVALID, "n_tokens must be < 2^32");
+    if (opts->probe_end) return fail(ctx, HYSET_E_INVALID, "probe ranges need an uploaded collection");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream, cp = ctx->aux;
+    auto res = std::make_unique<hyset_result>();
+    auto c = std::make_unique<hyset_coll>();
+    c->ctx = ctx;
+    c->n = n_sets;
+    c->n_tokens = n_tokens;
+    hyset_coll* C = c.get();
+    auto bail = [&](hyset_status st) {
+        cudaStreamSynchronize(cp);
+        hyset_collection_free(ctx, c.release());
+        return st;
+    };
+    const unsigned long long launches0 = launches();
+    CK(cudaEventRecord(ctx->ev0, s));
+    if (C->tokens.ensure(n_tokens * 4 + 4, s) != cudaSuccess || C->starts.ensure((size_t)n_sets * 4 + 4, s) ||
+        C->sizes.ensure((size_t)n_sets * 4 + 4, s) || C->meta.ensure((size_t)n_sets * sizeof(uint2) + 8, s))
+        return bail(fail(ctx, HYSET_E_NOMEM, "device allocation"));
+    C->d_tokens = C->tokens.as<uint32_t>();
+    C->d_starts = C->starts.as<uint32_t>();
+    C->d_sizes = C->sizes.as<uint32_t>();
+    // 1. on the copy stream: the sizes (and starts, when given) first, then every
+    //    token chunk with an event after each; the sizes go first so the
+    //    per-set work is not queued behind the tokens on the copy engine
+    CK(cudaEventRecord(ctx->ev_fork, s));
+    CK(cudaStreamWaitEvent(cp, ctx->ev_fork, 0));
+    const bool starts_given = starts != nullptr;
+    if (n_sets) {
+        CK(cudaMemcpyAsync(C->sizes.p, sizes, (size_t)n_sets * 4, cudaMemcpyHostToDevice, cp));
+        if (starts_given) CK(cudaMemcpyAsync(C->starts.p, starts, (size_t)n_sets * 4, cudaMemcpyHostToDevice, cp));
+    }
+    CK(cudaEventRecord(ctx->ev_join, cp));
+    CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    if (!starts_given && n_sets) {  // contiguous sets: starts are the exclusive scan of the sizes
+        CK(ctx->sc->scan.ensure(scan_scratch_words(n_sets) * 4, s));
+        CK(scan_exclusive(C->d_sizes, C->starts.as<uint32_t>(), n_sets, ctx->sc->scan.as<uint32_t>(), s));
+    }
+    const uint64_t n_chunks = n_tokens ? (n_tokens + PIPE_CHUNK_TOKENS - 1) / PIPE_CHUNK_TOKENS : 0;
+    for (uint64_t k = 0; k < n_chunks; ++k) {
+        const uint64_t t0 = k * PIPE_CHUNK_TOKENS, t1 = std::min(n_tokens, t0 + PIPE_CHUNK_TOKENS);
+        CK(cudaMemcpyAsync(C->tokens.as<uint32_t>() + t0, tokens + t0, (t1 - t0) * 4, cudaMemcpyHostToDevice, cp));
+        cudaEvent_t e = pipe_event(ctx, k);
+        if (!e) return bail(fail(ctx, HYSET_E_CUDA, "event creation"));
+        CK(cudaEventRecord(e, cp));
+    }
+    // 2. on the host meanwhile: starts (when absent), contiguity, size order, histogram
+    std::vector<uint32_t> st_host;
+    bool contiguous = true, ordered = true;
+    {
+        uint64_t run = 0;
+        if (!starts) {
+            st_host.resize(n_sets);
+            for (uint32_t i = 0; i < n_sets; ++i) {
+                st_host[i] = (uint32_t)run;
+                run += sizes[i];
+            }
+            if (run > n_tokens) return bail(fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens"));
+            starts = st_host.data();
+        } else {
+            for (uint32_t i = 0; i < n_sets && contiguous; ++i) {
+                contiguous = starts[i] == run;
+                run += sizes[i];
+            }
+        }
+        for (uint32_t i = 1; i < n_sets && ordered; ++i) ordered = sizes[i - 1] <= sizes[i];
+    }
+    if (!ordered) return bail(fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size"));
+    ST(build_size_meta(ctx, C, sizes));
+    // 3. the configuration, from the options or the context's earlier choices
+    const hyset_join_opts* o = opts;
+    bool pipelined = contiguous && n_sets > 0;
+    hyset_technique selected = HYSET_TECH_AUTO;
+    int selector = -1;
+    const std::string key = join_key(C, C, o);
+    if (o->technique == HYSET_TECH_AUTO) {
+        auto it = ctx->select_cache.find(key);
+        if (it == ctx->select_cache.end()) pipelined = false;
+        else {
+            selected = it->second.first;
+            selector = it->second.second;
+        }
+    }
+    Tuned tn = tune(C, C, o, selected);
+    if (tn.tech != HYSET_TECH_FGSS || !tn.probe_major) pipelined = false;
+    if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && n_sets >= TUNE_MIN_PROBES) {
+        auto it = ctx->bits_cache.find(key);
+        if (it == ctx->bits_cache.end()) pipelined = false;
+        else tn.bits = it->second;
+    }
+    Bounds* b = nullptr;
+    ST(get_bounds(ctx, o->sim, o->threshold, C->max_size, 0, &b));
+    uint32_t max_pre = 1;
+    for (size_t l = 0; l < C->size_hist.size(); ++l)
+        if (C->size_hist[l]) max_pre = std::max(max_pre, b->index_prefix[l]);
+    const uint32_t pb = bits_for(max_pre);
+    const uint64_t E = prefix_entries(C, b->index_prefix);
+    if (pb + bits_for(n_sets) > 32 || E >= (1ull << 32)) pipelined = false;  // packed layout only
+    if (!pipelined) {
+        // the plain sequence: all tokens, the checks, then the join
+        CK(cudaStreamWaitEvent(s, pipe_event(ctx, n_chunks ? n_chunks - 1 : 0), 0));
+        hyset_status stt = enqueue_collection_checks(ctx, C, sizes);
+        if (stt == HYSET_OK) {
+            CK(cudaStreamSynchronize(s));
+            stt = finish_collection_checks(ctx, C, sizes);
+        }
+        if (stt == HYSET_OK) stt = do_join(ctx, C, C, o, res.get());
+        if (stt != HYSET_OK) return bail(stt);
+    } else {
+        // 4. per chunk: checks, prefix entries (no histogram yet) and signatures
+        const uint32_t n = n_sets;
+        CK(ctx->sc->len.ensure((size_t)n * 4 + 4, s));
+        CK(ctx->sc->off.ensure((size_t)n * 4 + 4, s));
+        CK(ctx->sc->tok.ensure(E ? E * 4 : 4, s));
+        CK(ctx->sc->altk.ensure(E ? E * 4 : 4, s));
+        CK(ctx->sc->altv.ensure(E ? E * 4 : 4, s));
+        Index& ix = C->index;
+        CK(ix.set.ensure(E ? E * 4 : 4, s));
+        CK(ix.pos.ensure(4, s));
+        CK(ctx->s_flags.ensure(16, s));
+        CK(cudaMemsetAsync(ctx->s_flags.p, 0, 16, s));
+        const size_t scan_words = std::max(scan_scratch_words(n), radix_scratch_words(E ? E : 1));
+        CK(ctx->sc->scan.ensure(scan_words * 4, s));
+        uint32_t* len = ctx->sc->len.as<uint32_t>();
+        uint32_t* off = ctx->sc->off.as<uint32_t>();
+        CollView v = C->view();
+        CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
+        CK(scan_exclusive(len, off, n, ctx->sc->scan.as<uint32_t>(), s));
+        const int words = (int)(tn.bits / 64);
+        DevBuf& bits = C->bitmaps[words];
+        if (words) CK(bits.ensure((size_t)n * words * 8 + 8, s));
+        uint32_t lo = 0;
+        for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
+            const uint64_t t1 = std::min(n_tokens, (k + 1) * PIPE_CHUNK_TOKENS);
+            // sets whose tokens end inside the chunks copied so far
+            uint32_t hi = lo;
+            if (k + 1 == n_chunks) hi = n;
+            else {
+                uint32_t a = lo, z = n;  // first set ending past t1
+                while (a < z) {
+                    const uint32_t m = (a + z) >> 1;
+                    if ((uint64_t)starts[m] + sizes[m] <= t1) a = m + 1;
+                    else z = m;
+                }
+                hi = a;
+            }
+            CK(cudaStreamWaitEvent(s, pipe_event(ctx, k), 0));
+            if (hi <= lo) continue;
+            CollView part = v;
+            part.sizes += lo;
+            part.starts += lo;
+            part.meta += lo;
+            part.n = hi - lo;
+            CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
+            CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr, s, lo,
+                                   hi));
+            if (words) CK(generate_bitmaps(part, words, bits.as<uint64_t>() + (size_t)lo * words, s));
+            lo = hi;
+        }
+        if (n_chunks) CK(cudaStreamWaitEvent(s, pipe_event(ctx, n_chunks - 1), 0));  // every copy has landed
+        // 5. the index and the join.  The universe (largest token + 1) sizes the
+        //    list offsets; when a collection with the same size profile was
+        //    joined before, its universe is assumed and the checks are read
+        //    after the join (one synchronisation); a different universe means
+        //    the index is built again and the join re-run.
+        uint32_t* f = ctx->h_flags;
+        auto verdict = [&]() -> hyset_status {
+            if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
+            if (f[0] & 1) return fail(ctx, HYSET_E_INVALID, "empty set in collection");
+            if (f[0] & 2) return fail(ctx, HYSET_E_INVALID, "set tokens must be strictly ascending");
+            if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
+            return HYSET_OK;
+        };
+        const std::string ukey = coll_signature(C);
+        auto uit = ctx->universe_cache.find(ukey);
+        bool assumed = uit != ctx->universe_cache.end();
+        uint32_t U = 0;
+        if (assumed) {
+            U = uit->second;
+        } else {
+            CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            const hyset_status vs = verdict();
+            if (vs != HYSET_OK) return bail(vs);
+            U = f[1] + 1;
+        }
+        JoinParams P{};
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            C->universe = U;
+            CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
+            CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
+            CK(ctx->sc->scan.ensure(std::max(scan_words, scan_scratch_words((uint64_t)U + 1)) * 4, s));
+            if (attempt > 0)  // the sort reordered the entries: emit them again
+                CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr, s));
+            uint32_t* counts = ctx->sc->counts.as<uint32_t>();
+            CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+            CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
+            CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, ctx->sc->scan.as<uint32_t>(), s));
+            CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
+                                ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));
+            ix.sim = b->sim;
+            ix.tau = b->tau;
+            ix.kind = 0;
+            ix.universe = U;
+            ix.entries = E;
+            ix.pos_bits = pb;
+            P = JoinParams{};
+            P.R = C->view();
+            P.S = P.R;
+            P.B = b->view;
+            P.first_ge = C->first_ge.as<uint32_t>();
+            P.R_L = C->max_size;
+            P.self = 1;
+            P.grab = std::min<uint32_t>(tn.batch, 32);
+            P.p_lo = 0;
+            P.p_hi = n;
+            P.r_lo = 0;
+            P.r_hi = n;
+            P.X = ix.view();
+            if (words) {
+                P.bits_R = P.bits_S = bits.as<uint64_t>();
+                P.words = words;
+            }
+            if (assumed) CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+            const hyset_status js = run_join(ctx, P, TECH_FGSS, tn.vmode, o, res.get(), true);  // synchronises
+            if (js != HYSET_OK) return bail(js);
+            if (!assumed) break;
+            const hyset_status vs = verdict();
+            if (vs != HYSET_OK) return bail(vs);
+            if (f[1] + 1 <= U) break;  // every token was indexed: the join stands
+            U = f[1] + 1;              // a larger token: index and join again
+            assumed = false;
+        }
+        C->universe = f[1] + 1;
+        ctx->universe_cache[ukey] = C->universe;
+        res->technique = HYSET_TECH_FGSS;
+        res->bitmap_bits = tn.bits;
+        res->selector = selector;
+        if (o->collect_stats) res->stats[3] = E;
+        res->launches = launches() - launches0;
+    }
+    if (coll_out) *coll_out = c.release();
+    else hyset_collection_free(ctx, c.release());
     *out = res.release();
     return HYSET_OK;
 }
@@ -1770,7 +2051,7 @@ hyset_status build_block_index(hyset_handler* h, const hyset_block& blk) {
     CK(emit_prefix_entries(v, lo, hi, h->e_off.as<uint32_t>(), h->e_len.as<uint32_t>(), h->e_tok.as<uint32_t>(),
                            h->e_set.as<uint32_t>(), h->e_pos.as<uint32_t>(), s));
     CK(cudaMemsetAsync(h->counts.p, 0, ((size_t)U + 1) * 4, s));
-    CK(token_histogram(h->e_tok.as<uint32_t>(), E, h->counts.as<uint32_t>(), s));
+    CK(token_histogram(h->e_tok.as<uint32_t>(), E, h->counts.as<uint32_t>(), U + 1, s));
     CK(scan_exclusive(h->counts.as<uint32_t>(), h->list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
     // the scatter advances a cursor copy of the list starts
     CK(cudaMemcpyAsync(h->counts.p, h->list_off.p, ((size_t)U + 1) * 4, cudaMemcpyDeviceToDevice, s));

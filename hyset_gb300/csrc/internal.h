@@ -119,6 +119,7 @@ struct hyset_ctx {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, ek0 = nullptr, ek1 = nullptr;
     cudaStream_t aux = nullptr;                         // work that overlaps the index build
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // fork to / join from aux
+    std::vector<cudaEvent_t> pipe_ev;                   // one per copy chunk of a host-input join
     std::string err;
     std::map<std::tuple<int, double, uint32_t, int>, std::unique_ptr<hs::Bounds>> bounds;
     // scratch reused across joins; a batch being prepared points sc at its own
@@ -137,6 +138,7 @@ struct hyset_ctx {
     hs::DevBuf d_mlp, d_feat, d_moments, d_hist;
     std::map<std::string, std::pair<hyset_technique, int>> select_cache;  // decision, selector
     std::map<std::string, uint32_t> bits_cache;  // autotuned signature width per join
+    std::map<std::string, uint32_t> universe_cache;  // universe by collection size profile (host-input joins)
 };
 
 struct hyset_coll {

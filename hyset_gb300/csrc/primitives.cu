@@ -234,11 +234,14 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 
 // One warp per set: (token, (set << pos_bits) | position) for the first len
 // tokens, and the token histogram with one atomic per distinct token per warp.
-__global__ void k_emit_packed(CollView c, const uint32_t* __restrict__ off, const uint32_t* __restrict__ len,
-                              uint32_t pos_bits, uint32_t* e_token, uint32_t* e_val, uint32_t* counts) {
+// Sets [lo, c.n): c, off and len are indexed by absolute set id.  counts may be
+// nullptr (no histogram: the caller counts the emitted tokens later).
+__global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
+                              const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* e_token, uint32_t* e_val,
+                              uint32_t* counts) {
     const int lane = threadIdx.x & 31;
     uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < c.n; s += warps) {
+    for (uint32_t s = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); s < c.n; s += warps) {
         const uint32_t l = len[s], o = off[s];
         const uint32_t* t = c.tokens + c.meta[s].x;
         for (uint32_t i0 = 0; i0 < l; i0 += 32) {
@@ -250,12 +253,13 @@ __global__ void k_emit_packed(CollView c, const uint32_t* __restrict__ off, cons
                 e_val[o + i] = (s << pos_bits) | i;
             }
             // tokens inside one set are distinct: one atomic per lane
-            if (valid) atomicAdd(&counts[tok], 1u);
+            if (valid && counts) atomicAdd(&counts[tok], 1u);
         }
     }
 }
 
-__global__ void k_histogram(const uint32_t* __restrict__ tok, uint64_t n, uint32_t* counts) {
+// counts has `limit` entries; tokens at or above it are not counted.
+__global__ void k_histogram(const uint32_t* __restrict__ tok, uint64_t n, uint32_t* counts, uint32_t limit) {
     const int lane = threadIdx.x & 31;
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t i0 = (uint64_t)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {
@@ -263,7 +267,7 @@ __global__ void k_histogram(const uint32_t* __restrict__ tok, uint64_t n, uint32
         bool valid = i < n;
         uint32_t t = valid ? tok[i] : 0xFFFFFFFFu;
         unsigned peers = __match_any_sync(FULL, t);
-        if (valid && lane == __ffs(peers) - 1) atomicAdd(&counts[t], (uint32_t)__popc(peers));
+        if (valid && t < limit && lane == __ffs(peers) - 1) atomicAdd(&counts[t], (uint32_t)__popc(peers));
     }
 }
 
@@ -480,18 +484,22 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
 }
 
 cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
-                                uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s) {
-    if (c.n == 0) return cudaSuccess;
+                                uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s, uint32_t lo,
+                                uint32_t hi) {
+    if (hi == 0xFFFFFFFFu) hi = c.n;
+    if (hi <= lo) return cudaSuccess;
     note_launches();
-    k_emit_packed<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, entry_off, len, pos_bits, e_token, e_val,
-                                                                     counts);
+    CollView v = c;
+    v.n = hi;  // the kernel walks ids [lo, hi)
+    k_emit_packed<<<grid_for((uint64_t)(hi - lo) * 32, 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
+                                                                          e_val, counts);
     return cudaGetLastError();
 }
 
-cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, cudaStream_t s) {
+cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, uint32_t limit, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     note_launches();
-    k_histogram<<<grid_for(n, 256), 256, 0, s>>>(e_token, n, counts);
+    k_histogram<<<grid_for(n, 256), 256, 0, s>>>(e_token, n, counts, limit);
     return cudaGetLastError();
 }
 

@@ -144,6 +144,16 @@ hyset_status hyset_self_join(hyset_ctx* ctx, const hyset_coll* coll, const hyset
  * the self-join's predicate applied across two collections. */
 hyset_status hyset_rs_join(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
                            const hyset_join_opts* opts, hyset_result** out);
+/* The upload and the self-join in one call, from host arrays (the reference's
+ * read_collection -> device_collection -> handler sequence, src/fgss.cu:88-116):
+ * the tokens travel in chunks while the sets already on the device are checked
+ * and indexed.  The arguments mean what they mean for hyset_collection_upload and
+ * hyset_self_join (probe ranges are not accepted here); *coll_out (may be NULL)
+ * receives the uploaded collection for later joins.  Same result and the same
+ * input checks as the two calls. */
+hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64_t n_tokens, const uint32_t* starts,
+                                  const uint32_t* sizes, uint32_t n_sets, const hyset_join_opts* opts,
+                                  hyset_coll** coll_out, hyset_result** out);
 
 /* Many independent joins in one persistent, work-stealing launch (the
  * device-resident form of src/queue.cu:142-281's block-pair queue).
