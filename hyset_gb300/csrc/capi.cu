@@ -1557,26 +1557,27 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         if (!e) return bail(fail(ctx, HYSET_E_CUDA, "event creation"));
         CK(cudaEventRecord(e, cp));
     }
-    // 2. on the host meanwhile: starts (when absent), contiguity, size order, histogram
-    std::vector<uint32_t> st_host;
+    // 2. on the host meanwhile, one pass over the sizes: contiguity of the given
+    //    starts, size order, and for every chunk the first set that ends past it
+    //    (sets before it are complete once the chunk has landed)
     bool contiguous = true, ordered = true;
+    std::vector<uint32_t> chunk_hi(n_chunks, n_sets);
     {
-        uint64_t run = 0;
-        if (!starts) {
-            st_host.resize(n_sets);
-            for (uint32_t i = 0; i < n_sets; ++i) {
-                st_host[i] = (uint32_t)run;
-                run += sizes[i];
+        uint64_t run = 0, bound = PIPE_CHUNK_TOKENS, k = 0;
+        uint32_t prev = 0;
+        for (uint32_t i = 0; i < n_sets; ++i) {
+            const uint32_t z = sizes[i];
+            if (starts_given) contiguous &= starts[i] == run;
+            ordered &= z >= prev;
+            prev = z;
+            const uint64_t end = run + z;
+            while (k < n_chunks && end > bound) {
+                chunk_hi[k++] = i;
+                bound += PIPE_CHUNK_TOKENS;
             }
-            if (run > n_tokens) return bail(fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens"));
-            starts = st_host.data();
-        } else {
-            for (uint32_t i = 0; i < n_sets && contiguous; ++i) {
-                contiguous = starts[i] == run;
-                run += sizes[i];
-            }
+            run = end;
         }
-        for (uint32_t i = 1; i < n_sets && ordered; ++i) ordered = sizes[i - 1] <= sizes[i];
+        if (!starts_given && run > n_tokens) return bail(fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens"));
     }
     if (!ordered) return bail(fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size"));
     ST(build_size_meta(ctx, C, sizes));
@@ -1644,19 +1645,8 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         if (words) CK(bits.ensure((size_t)n * words * 8 + 8, s));
         uint32_t lo = 0;
         for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
-            const uint64_t t1 = std::min(n_tokens, (k + 1) * PIPE_CHUNK_TOKENS);
             // sets whose tokens end inside the chunks copied so far
-            uint32_t hi = lo;
-            if (k + 1 == n_chunks) hi = n;
-            else {
-                uint32_t a = lo, z = n;  // first set ending past t1
-                while (a < z) {
-                    const uint32_t m = (a + z) >> 1;
-                    if ((uint64_t)starts[m] + sizes[m] <= t1) a = m + 1;
-                    else z = m;
-                }
-                hi = a;
-            }
+            const uint32_t hi = k + 1 == n_chunks ? n : std::max(lo, chunk_hi[k]);
             CK(cudaStreamWaitEvent(s, pipe_event(ctx, k), 0));
             if (hi <= lo) continue;
             CollView part = v;
