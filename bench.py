@@ -463,6 +463,79 @@ def run_parse(args):
                 "d2h_bytes_per_step": 32, "ms_per_step": e2e * 1000}}), flush=True)
 
 
+def verify_candidates(c, n_probes=262144, per_probe=32, seed=0x5E7C, threshold=THRESHOLD):
+    """Seeded candidate lists over the collection: sorted probe ids and, for
+    each, `per_probe` candidates drawn uniformly from its length window (ids
+    below the probe whose size is at least minsize(|probe|)), the shape of
+    what a CPU filter hands the reference's device_handler."""
+    import numpy as np
+    from hyset_gb300 import similarity
+    rng = np.random.default_rng(seed)
+    n = c.n
+    probes = np.sort(rng.choice(np.arange(1, n), size=min(n - 1, n_probes), replace=False)).astype(np.int64)
+    sizes = c.sizes.astype(np.int64)
+    minsize = np.array([similarity.minsize("jaccard", int(l), threshold) for l in range(int(sizes.max()) + 1)])
+    lo = np.searchsorted(sizes, minsize[sizes[probes]], side="left")
+    span = probes - lo
+    keep = span > 0
+    probes, lo, span = probes[keep], lo[keep], span[keep]
+    cands = lo[:, None] + (rng.random((probes.size, per_probe)) * span[:, None]).astype(np.int64)
+    offsets = np.arange(1, probes.size + 1, dtype=np.int64) * per_probe
+    return probes.astype(np.uint32), offsets.astype(np.uint32), cands.reshape(-1).astype(np.uint32)
+
+
+def run_verify(args):
+    """The candidate verifier alone (hybrid::device_handler's kernels): seeded
+    candidate lists of the 1M-set workload, resident in HBM, verified with one
+    warp per candidate (merge-path steps of 32 tokens) and with one lane per
+    candidate; the roofline counts the tokens the early-exit merges must read."""
+    import numpy as np
+    import torch
+    import hyset_gb300 as hs
+    import oracle
+    c = make_workload(args.sets or None)
+    ctx = hs.Context(0)
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    probes, offsets, cands = verify_candidates(c)
+    t0 = time.perf_counter()
+    exp, tokens_read = oracle.verify_csr((c.tokens, c.starts, c.sizes), probes, offsets, cands, THRESHOLD)
+    cpu_s = time.perf_counter() - t0
+    dp, do, dc = (torch.from_numpy(a.view(np.int32)).cuda() for a in (probes, offsets, cands))
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    legs = {}
+    for vm in (3, 2, 1):
+        ms = []
+        for i in range(args.warmup + args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            r = ctx.verify_device(coll, dp.data_ptr(), do.data_ptr(), dc.data_ptr(), probes.size,
+                                  threshold=THRESHOLD, verify_mode=vm)
+            if i == 0:
+                assert oracle.as_set(r.pairs) == oracle.as_set(exp), "verifier differs from the oracle"
+            if i >= args.warmup:
+                ms.append(r.kernel_ms)
+        legs[vm] = statistics.median(ms)
+    best = min(legs, key=legs.get)
+    kms = legs[best]
+    peak, peak_kind = measured_peaks()
+    alg = 4 * tokens_read + 4 * cands.size + 8 * probes.size + 8 * len(exp)  # tokens read, ids, sizes, pairs
+    print(json.dumps({
+        "metric": "candidate pairs verified/s (hybrid::device_handler verifier)", "value": cands.size / kms * 1e3,
+        "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": kms,
+        "higher_is_better": True, "dtype": "u32", "data": "synthetic (seeded generator and candidate lists)",
+        "config": {"workload": WORKLOAD.split(":")[0] + ": candidate lists", "probes": int(probes.size),
+                   "candidates": int(cands.size), "result_pairs": int(len(exp)),
+                   "tokens_read_by_merges": int(tokens_read), "staged_lane_ms": legs[3],
+                   "warp_per_candidate_ms": legs[2], "lane_per_candidate_ms": legs[1],
+                   "verify_mode": best, "l2": "512 MB buffer written between timed steps"},
+        "roofline": {"bound": "hbm", "achieved": alg / kms / 1e6, "peak": peak, "unit": "GB/s",
+                     "frac": alg / kms / 1e6 / peak, "traffic": None, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg},
+        "cpu_baseline": {"value": cands.size / cpu_s, "unit": "pairs/s", "cores": 1, "kind": "port",
+                         "sample": "all candidate lists once (oracle_verify_csr, verification.hpp:9-31)"}}),
+          flush=True)
+
+
 def hs_text_bytes(c):
     from hyset_gb300 import synth
     lib = synth._load()
@@ -486,9 +559,9 @@ def main():
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
     ap.add_argument("--vmode", type=int, default=0, help="verification: 0 auto, 1 lane, 2 warp per candidate")
-    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse"],
-                    help="batch: the batched R-S workload; parse: the collection text reader "
-                         "(separate measurements, not the headline)")
+    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse", "verify"],
+                    help="batch: the batched R-S workload; parse: the collection text reader; verify: the "
+                         "candidate verifier alone (separate measurements, not the headline)")
     ap.add_argument("--joins", type=int, default=256)
     args = ap.parse_args()
     ws, rank, local = dist_env()
@@ -497,6 +570,9 @@ def main():
         return
     if args.workload == "parse":
         run_parse(args)
+        return
+    if args.workload == "verify":
+        run_verify(args)
         return
     if args.impl == "reference":
         run_reference(args, ws, rank)

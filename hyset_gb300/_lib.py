@@ -62,6 +62,8 @@ PROTOTYPES = {
                                           C.POINTER(C.c_void_p)]),
     "hyset_collection_from_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                                C.c_uint32, C.POINTER(C.c_void_p)]),
+    "hyset_verify_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "hyset_self_join_host": (C.c_int, [C.c_void_p, U32P, C.c_uint64, U32P, U32P, C.c_uint32, C.c_void_p,
                                        C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "hyset_collection_parse": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),

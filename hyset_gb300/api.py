@@ -212,6 +212,18 @@ class Context:
             return res, DeviceCollection(self, h, int(sz.size))
         return res
 
+    def verify_device(self, indexed: DeviceCollection, d_probes: int, d_offsets: int, d_candidates: int,
+                      n_probes: int, probe: Optional[DeviceCollection] = None, threshold: float = 0.8,
+                      **kw) -> JoinResult:
+        """Verifies device-resident candidate lists (raw device pointers to uint32
+        arrays: probe ids, inclusive end offsets, candidate ids)."""
+        o = make_opts(threshold, **kw)
+        r = C.c_void_p()
+        check(self._lib.hyset_verify_device(self.handle, indexed.handle, probe.handle if probe else None,
+                                            C.c_void_p(d_probes), C.c_void_p(d_offsets), C.c_void_p(d_candidates),
+                                            n_probes, C.byref(o), C.byref(r)), self.handle)
+        return _take_result(self._lib, r)
+
     def rs_join(self, indexed: DeviceCollection, probe: DeviceCollection, threshold: float = 0.8,
                 **kw) -> JoinResult:
         o = make_opts(threshold, **kw)

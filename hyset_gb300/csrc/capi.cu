@@ -390,7 +390,7 @@ hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
     if (o->bitmap_bits != 0 && o->bitmap_bits != 64 && o->bitmap_bits != 128 && o->bitmap_bits != 256 &&
         o->bitmap_bits != 512)
         return fail(ctx, HYSET_E_INVALID, "bitmap_bits must be 0, 64, 128, 256 or 512");
-    if (o->verify_mode > 2) return fail(ctx, HYSET_E_INVALID, "verify_mode must be 0, 1 or 2");
+    if (o->verify_mode > 3) return fail(ctx, HYSET_E_INVALID, "verify_mode must be 0, 1, 2 or 3");
     if (o->orientation > 2) return fail(ctx, HYSET_E_INVALID, "orientation must be 0, 1 or 2");
     return HYSET_OK;
 }
@@ -426,6 +426,7 @@ Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o,
     if (t.tech == HYSET_TECH_BITMAP && t.bits == 0) t.bits = 64;
     if (t.tech == HYSET_TECH_DIRECT) t.bits = 0;
     t.vmode = o->verify_mode ? (int)o->verify_mode : 1;
+    if (t.vmode == 3) t.vmode = 1;  // the staged mode exists for explicit candidate lists only
     return t;
 }
 
@@ -2255,6 +2256,61 @@ hyset_status hyset_verifier_add_candidates(hyset_verifier* v, uint32_t probe_id,
         v->h_offsets.push_back((uint32_t)v->h_cands.size());
         done += take;
     } while (done < n);
+    return HYSET_OK;
+}
+
+hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                                 const uint32_t* d_probes, const uint32_t* d_offsets, const uint32_t* d_candidates,
+                                 uint32_t n_probes, const hyset_join_opts* opts, hyset_result** out) {
+    if (!ctx || !indexed || !opts || !out || (n_probes && (!d_probes || !d_offsets || !d_candidates)))
+        return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    ST(check_opts(ctx, opts));
+    CK(cudaSetDevice(ctx->device));
+    const hyset_coll* R = indexed;
+    const hyset_coll* S = probe ? probe : indexed;
+    Bounds* b = nullptr;
+    ST(get_bounds(ctx, opts->sim, opts->threshold, std::max(R->max_size, S->max_size), 0, &b));
+    auto res = std::make_unique<hyset_result>();
+    cudaStream_t s = ctx->stream;
+    const int vmode = opts->verify_mode ? (int)opts->verify_mode : 3;
+    const int count_only = opts->count_only ? 1 : 0;
+    uint64_t cap = opts->pair_capacity ? opts->pair_capacity : (1u << 20);
+    CK(ctx->s_count.ensure(16, s));
+    CK(ctx->s_work.ensure(16, s));
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (!count_only) CK(ctx->s_pairs.ensure(std::max<uint64_t>(cap, 1) * sizeof(uint2), s));
+        Sink sk{count_only ? nullptr : ctx->s_pairs.as<uint2>(), ctx->s_count.as<unsigned long long>(),
+                count_only ? 0ull : (unsigned long long)cap, count_only};
+        CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+        CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
+        CK(cudaEventRecord(ctx->ek0, s));
+        CK(launch_verify_candidates(R->view(), S->view(), b->view, d_probes, d_offsets, d_candidates, n_probes, vmode,
+                                    sk, ctx->s_work.as<unsigned int>(), ctx->sm_count, s));
+        CK(cudaEventRecord(ctx->ek1, s));
+        unsigned long long count = 0;
+        CK(cudaMemcpyAsync(&count, ctx->s_count.p, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        float kms = 0;
+        CK(cudaEventElapsedTime(&kms, ctx->ek0, ctx->ek1));
+        res->kernel_ms = res->device_ms = kms;
+        res->count = count;
+        if (count_only || count <= cap) break;
+        cap = count + count / 8 + 1024;
+        if (attempt == 1) return fail(ctx, HYSET_E_OVERFLOW, "pair buffer overflow after resize");
+    }
+    if (!count_only && opts->device_pairs) {
+        res->device_pairs = ctx->s_pairs.p;
+    } else if (!count_only) {
+        res->pairs.resize(res->count);
+        if (res->count)
+            CK(cudaMemcpyAsync(res->pairs.data(), ctx->s_pairs.p, res->count * sizeof(hyset_pair),
+                               cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        res->has_pairs = 1;
+    }
+    res->technique = HYSET_TECH_DIRECT;
+    *out = res.release();
     return HYSET_OK;
 }
 

@@ -36,19 +36,48 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     uint32_t* sbuf = smem + warp * MAXP;
     const uint32_t nprobe = P.p_hi - P.p_lo;
     const uint32_t grab = P.grab ? P.grab : 1;
+    const uint32_t steal = grab * HS_JOIN_STEAL;  // probes per atomic on the shared counter
+    uint32_t i = 0, i_end = 0;
     for (;;) {
-        uint32_t i = 0;
-        if (lane == 0) i = atomicAdd(P.work, grab);
-        i = __shfl_sync(FULL, i, 0);
+        if (i >= i_end) {
+            if (lane == 0) i = atomicAdd(P.work, steal);
+            i = __shfl_sync(FULL, i, 0);
+            i_end = min(nprobe, i + steal);
+        }
         if (i >= nprobe) break;
-        const uint32_t end = min(nprobe, i + grab);
+        const uint32_t end = min(i_end, i + grab);
         // largest sets first: the heaviest probes start early, the tail is light
         if constexpr (TECH == TECH_FGSS) {
             fgss_batch<VMODE, W, ST>(P, i, end - i, lane);
         } else {
-            for (; i < end; ++i) enum_probe<VMODE, W, ST>(P, P.p_hi - 1 - i, sbuf, lane);
+            for (uint32_t q = i; q < end; ++q) enum_probe<VMODE, W, ST>(P, P.p_hi - 1 - q, sbuf, lane);
+        }
+        i = end;
+    }
+}
+
+// Staged lane-serial merge: b's first VSTAGE tokens are in `head` (shared
+// memory), the rest in global memory; same early-exit bounds as verify_serial.
+constexpr uint32_t VSTAGE = 16;            // candidate tokens staged per candidate
+constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fall in distinct banks
+__device__ __forceinline__ bool verify_staged(const uint32_t* a, uint32_t na, const uint32_t* head,
+                                              const uint32_t* __restrict__ b, uint32_t nb, uint32_t thr) {
+    uint32_t i = 0, k = 0, found = 0, maxa = na, maxb = nb;
+    while (maxa >= thr && maxb >= thr && found < thr) {
+        const uint32_t x = a[i], y = k < VSTAGE ? head[k] : __ldg(b + k);
+        if (x == y) {
+            ++i;
+            ++k;
+            ++found;
+        } else if (x < y) {
+            ++i;
+            --maxa;
+        } else {
+            ++k;
+            --maxb;
         }
     }
+    return found >= thr;
 }
 
 // Explicit candidate lists: probes[i] owns candidates [offsets[i-1], offsets[i]).
@@ -60,7 +89,7 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
                                                                     uint32_t n_probes, Sink out, unsigned int* work) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* sbuf = smem + warp * MAXP;
+    uint32_t* sbuf = smem + warp * (MAXP + (VMODE == 3 ? 32 * VSTRIDE : 0));
     for (;;) {
         uint32_t i = 0;
         if (lane == 0) i = atomicAdd(work, 1u);
@@ -94,6 +123,23 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
             }
             if constexpr (VMODE == 1) {
                 bool ok = keep && verify_serial(a, lp, R.tokens + cs, lc, mo, NOWN);
+                emit(out, ok, p, c, lane);
+            } else if constexpr (VMODE == 3) {
+                // the first VSTAGE tokens of the round's 32 candidates arrive with
+                // 16 coalesced loads (two candidates per load, one per half-warp);
+                // each lane then merges its candidate out of shared memory and
+                // reads global memory only past the staged prefix
+                uint32_t* tile = sbuf + MAXP;
+                const uint32_t t = lane & (VSTAGE - 1);
+#pragma unroll
+                for (int r = 0; r < 16; ++r) {
+                    const int j = 2 * r + (lane >> 4);
+                    const uint32_t cj = __shfl_sync(FULL, cs, j), lj = __shfl_sync(FULL, keep ? lc : 0u, j);
+                    if (t < lj) tile[j * VSTRIDE + t] = __ldg(R.tokens + cj + t);
+                }
+                __syncwarp();
+                const bool ok = keep && verify_staged(a, lp, tile + lane * VSTRIDE, R.tokens + cs, lc, mo);
+                __syncwarp();
                 emit(out, ok, p, c, lane);
             } else {
                 unsigned m = __ballot_sync(FULL, keep);
@@ -160,10 +206,15 @@ cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const
                                      Sink out, unsigned int* work, int sm_count, cudaStream_t s) {
     if (n_probes == 0) return cudaSuccess;
     note_launches();
-    const size_t smem = JOIN_WARPS * MAXP * sizeof(uint32_t);
+    const size_t smem = JOIN_WARPS * (MAXP + (vmode == 3 ? 32 * VSTRIDE : 0)) * sizeof(uint32_t);
     int per_sm = 0;
     cudaError_t e;
-    if (vmode == 2) {
+    if (vmode == 3) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verify_candidates<3>, JOIN_THREADS, smem);
+        if (e != cudaSuccess) return e;
+        k_verify_candidates<3><<<sm_count * (per_sm ? per_sm : 1), JOIN_THREADS, smem, s>>>(
+            R, S, B, probes, offsets, cands, n_probes, out, work);
+    } else if (vmode == 2) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verify_candidates<2>, JOIN_THREADS, smem);
         if (e != cudaSuccess) return e;
         k_verify_candidates<2><<<sm_count * (per_sm ? per_sm : 1), JOIN_THREADS, smem, s>>>(

@@ -15,6 +15,9 @@ namespace {
 constexpr int JOIN_THREADS = HS_JOIN_THREADS;
 constexpr int JOIN_WARPS = JOIN_THREADS / 32;
 constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per warp
+#ifndef HS_JOIN_STEAL
+#define HS_JOIN_STEAL 1  // probe batches taken per atomic on the work counter
+#endif
 #ifndef HS_SHORT_LIST
 #define HS_SHORT_LIST 8
 #endif

@@ -68,7 +68,9 @@ typedef struct {
     hyset_technique technique;
     uint32_t bitmap_bits;      /* 0 = no signature filter; else 64, 128, 256 or 512 */
     uint32_t count_only;       /* 1 = count result pairs, do not materialise them */
-    uint32_t verify_mode;      /* 0 = auto, 1 = one lane per candidate, 2 = one warp per candidate */
+    uint32_t verify_mode;      /* 0 = auto, 1 = one lane per candidate, 2 = one warp per candidate,
+                                  3 = one lane per candidate from staged prefixes (explicit candidate
+                                  lists; joins treat it as 1) */
     uint32_t sort_pairs;       /* 1 = return pairs sorted by (first, second) */
     uint64_t pair_capacity;    /* initial device pair buffer; 0 = automatic (grows on demand) */
     uint32_t device_pairs;     /* 1 = leave the pairs in device memory (hyset_result_device_pairs) */
@@ -224,6 +226,16 @@ hyset_status hyset_verifier_add_candidates(hyset_verifier* v, uint32_t probe_id,
 hyset_status hyset_verifier_flush(hyset_verifier* v);
 hyset_status hyset_verifier_output(const hyset_verifier* v, uint64_t* count, const hyset_pair** pairs);
 void hyset_verifier_destroy(hyset_verifier* v);
+/* Device-resident candidate lists (the input of hybrid::device_handler's
+ * kernels, hybrid_kernels.hpp:14-165, already on the device): probe
+ * d_probes[i] of `probe` (NULL = indexed) owns candidates [d_offsets[i-1]
+ * (0 for i = 0), d_offsets[i]) of `indexed`; pairs with overlap >= minoverlap
+ * are returned as a join result (kernel_ms = the verification launch).  Uses
+ * opts->sim, threshold, verify_mode (0 = 3: one lane per candidate merging from
+ * a staged 16-token prefix), count_only, pair_capacity and device_pairs. */
+hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
+                                 const uint32_t* d_probes, const uint32_t* d_offsets, const uint32_t* d_candidates,
+                                 uint32_t n_probes, const hyset_join_opts* opts, hyset_result** out);
 
 /* ---- technique selector ------------------------------------------ */
 /* statistics::extract (include/hyset/statistics.hpp:163-213) and the analytic

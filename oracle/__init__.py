@@ -185,3 +185,17 @@ def read_text(text: bytes):
     nt, ne = C.c_uint64(), C.c_uint64()
     ns = fn(text, len(text), tok.ctypes.data_as(U32P), cap, siz.ctypes.data_as(U32P), cap, C.byref(nt), C.byref(ne))
     return tok[:nt.value].copy(), siz[:ns].copy(), int(ne.value)
+
+
+def verify_csr(coll, probes, offsets, cands, threshold, sim="jaccard"):
+    """(pairs, tokens read) of explicit candidate lists over one collection
+    (tokens, starts, sizes), verified as hybrid::device_handler's kernels do."""
+    lib = _load()
+    fn = lib.oracle_verify_csr
+    fn.restype = C.c_void_p
+    fn.argtypes = [U32P] * 9 + [C.c_uint32, C.c_int, C.c_double, C.POINTER(C.c_uint64)]
+    t, tp = _p(coll[0]); s_, sp = _p(coll[1]); z, zp = _p(coll[2])
+    pr, prp = _p(probes); of, ofp = _p(offsets); ca, cap = _p(cands)
+    read = C.c_uint64()
+    out = _take(fn(tp, sp, zp, tp, sp, zp, prp, ofp, cap, len(pr), SIM[sim], float(threshold), C.byref(read)))
+    return out, int(read.value)

@@ -494,3 +494,38 @@ uint64_t oracle_read_text(const char* text, uint64_t n, uint32_t* tokens, uint64
     *empty_items = empty;
     return sets;
 }
+
+/* ---- explicit candidate lists -------------------------------------------- */
+
+/* Candidate lists verified as hybrid::device_handler's kernels do: every
+ * (probe, candidate) merged from the start of both sets with the early-exit
+ * bounds of verification.hpp:9-31.  *tokens_read receives the tokens the
+ * merges read (positions consumed on both sides when each merge stops). */
+oracle_pairs* oracle_verify_csr(const uint32_t* r_tokens, const uint32_t* r_starts, const uint32_t* r_sizes,
+                                const uint32_t* s_tokens, const uint32_t* s_starts, const uint32_t* s_sizes,
+                                const uint32_t* probes, const uint32_t* offsets, const uint32_t* cands,
+                                uint32_t n_probes, int sim, double t, uint64_t* tokens_read) {
+    oracle_pairs* out = pairs_new();
+    if (!out) return NULL;
+    uint64_t read = 0;
+    for (uint32_t i = 0; i < n_probes; ++i) {
+        const uint32_t p = probes[i], lp = s_sizes[p];
+        const uint32_t* a = s_tokens + s_starts[p];
+        const uint32_t cb = i ? offsets[i - 1] : 0, ce = offsets[i];
+        for (uint32_t k = cb; k < ce; ++k) {
+            const uint32_t c = cands[k], lc = r_sizes[c];
+            const uint32_t* b = r_tokens + r_starts[c];
+            const uint32_t thr = oracle_minoverlap(sim, lp, lc, t);
+            uint32_t x = 0, y = 0, found = 0, maxa = lp, maxb = lc;
+            while (maxa >= thr && maxb >= thr && found < thr) {
+                if (a[x] == b[y]) { ++x; ++y; ++found; }
+                else if (a[x] < b[y]) { ++x; --maxa; }
+                else { ++y; --maxb; }
+            }
+            read += x + y;
+            if (found >= thr && pairs_add(out, p, c)) { oracle_pairs_free(out); return NULL; }
+        }
+    }
+    *tokens_read = read;
+    return out;
+}

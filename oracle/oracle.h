@@ -81,6 +81,14 @@ oracle_pairs* oracle_brute_rs(const uint32_t* r_tokens, const uint32_t* r_starts
 uint64_t oracle_read_text(const char* text, uint64_t n, uint32_t* tokens, uint64_t tok_cap, uint32_t* sizes,
                           uint64_t size_cap, uint64_t* n_tokens, uint64_t* empty_items);
 
+/* Explicit candidate lists (probe probes[i] owns cands[offsets[i-1], offsets[i]))
+ * verified as hybrid::device_handler's kernels do; *tokens_read receives the
+ * tokens the early-exit merges read. */
+oracle_pairs* oracle_verify_csr(const uint32_t* r_tokens, const uint32_t* r_starts, const uint32_t* r_sizes,
+                                const uint32_t* s_tokens, const uint32_t* s_starts, const uint32_t* s_sizes,
+                                const uint32_t* probes, const uint32_t* offsets, const uint32_t* cands,
+                                uint32_t n_probes, int sim, double t, uint64_t* tokens_read);
+
 uint64_t oracle_pairs_count(const oracle_pairs* p);
 const uint32_t* oracle_pairs_data(const oracle_pairs* p); /* 2*count: (first, second) */
 void oracle_pairs_free(oracle_pairs* p);
