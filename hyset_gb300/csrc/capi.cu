@@ -2217,7 +2217,9 @@ hyset_status verifier_run(hyset_verifier* v) {
     Sink out{v->aggregate ? nullptr : v->pairs.as<uint2>(), v->count.as<unsigned long long>(),
              (unsigned long long)v->max_candidates, v->aggregate};
     CK(launch_verify_candidates(v->indexed->view(), v->probe->view(), v->bounds->view, v->d_probes.as<uint32_t>(),
-                                v->d_offsets.as<uint32_t>(), v->d_cands.as<uint32_t>(), np, (int)v->scenario, out,
+                                v->d_offsets.as<uint32_t>(), v->d_cands.as<uint32_t>(), np,
+                                v->scenario == 1 ? 3 : 2,  // scenario 1 (lane per candidate) runs staged
+                                out,
                                 v->work.as<unsigned int>(), ctx->sm_count, s));
     unsigned long long count = 0;
     CK(cudaMemcpyAsync(&count, v->count.p, 8, cudaMemcpyDeviceToHost, s));
