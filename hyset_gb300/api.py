@@ -31,6 +31,8 @@ class JoinResult:
     launches: int = 0      # kernel launches the join issued
     selector: str = "explicit"  # which selector chose the technique
     bitmap_bits: int = 0        # signature width the join ran with
+    split_at: int = 0           # partition split: first probe id of the high range (0 = none)
+    split_low: str = ""         # the low range's technique when split
 
 
 # R-S joins: which collection is indexed (hyset_join_opts.orientation)
@@ -55,6 +57,12 @@ def make_opts(threshold: float = 0.8, sim: str = "jaccard", technique: str = "au
                     ORIENTATION[orientation])
 
 
+def _split(lib, r):
+    low = C.c_int(0)
+    at = int(lib.hyset_result_split(r, C.byref(low)))
+    return at, (TECH_NAMES.get(low.value, "?") if at else "")
+
+
 def _take_result(lib, r) -> JoinResult:
     try:
         n = lib.hyset_result_count(r)
@@ -69,7 +77,7 @@ def _take_result(lib, r) -> JoinResult:
                           float(lib.hyset_result_device_ms(r)), float(lib.hyset_result_kernel_ms(r)),
                           [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0),
                           int(lib.hyset_result_launches(r)), SELECTOR_NAMES.get(lib.hyset_result_selector(r), "?"),
-                          int(lib.hyset_result_bitmap_bits(r)))
+                          int(lib.hyset_result_bitmap_bits(r)), *_split(lib, r))
     finally:
         lib.hyset_result_free(r)
 

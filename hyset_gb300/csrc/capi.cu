@@ -690,6 +690,64 @@ hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
     return HYSET_OK;
 }
 
+// Partition split (the selector's second decision, dichotomy.cu's split of a
+// join into partitions handled by different techniques): the learned network
+// predicts each technique's time for the whole probe range and for its two
+// halves; when the halves prefer different techniques and their predicted sum
+// is at least 10 % below the whole's best, the join runs as two probe ranges.
+// Self-joins from 40,000 probes with technique AUTO and the network installed;
+// the plan is cached with the technique choice.  The pair set does not change.
+constexpr uint32_t SPLIT_MIN_PROBES = 40000;
+constexpr float SPLIT_MARGIN = 0.9f;
+
+hyset_status plan_split(hyset_ctx* ctx, hyset_coll* R, const hyset_join_opts* o, uint32_t* split_at,
+                        hyset_technique* low, hyset_technique* high) {
+    *split_at = 0;
+    if (o->technique != HYSET_TECH_AUTO || !ctx->has_mlp || o->probe_end || o->device_pairs ||
+        R->n < SPLIT_MIN_PROBES)
+        return HYSET_OK;
+    const std::string key = "split|" + join_key(R, R, o);
+    auto it = ctx->split_cache.find(key);
+    if (it != ctx->split_cache.end()) {
+        *split_at = it->second.at;
+        *low = it->second.low;
+        *high = it->second.high;
+        return HYSET_OK;
+    }
+    const uint32_t mid = R->n / 2;
+    float x[3][MLP_IN], y[3][MLP_OUT];
+    for (int part = 0; part < 3; ++part) {
+        hyset_join_opts q = *o;
+        q.probe_begin = part == 2 ? mid : 0;
+        q.probe_end = part == 0 ? 0 : (part == 1 ? mid : R->n);
+        float f[MLP_IN];
+        ST(compute_features(ctx, R, R, &q, f, nullptr));
+        for (int k = 0; k < MLP_IN; ++k) x[part][k] = (f[k] - ctx->feat_mean[k]) / ctx->feat_scale[k];
+    }
+    cudaStream_t s = ctx->stream;
+    CK(ctx->d_feat.ensure(512, s));
+    float* dx = ctx->d_feat.as<float>();
+    CK(cudaMemcpyAsync(dx, x, sizeof x, cudaMemcpyHostToDevice, s));
+    CK(mlp_forward(ctx->d_mlp.as<float>(), dx, 3, dx + 64, ctx->sm_count, s));
+    CK(cudaMemcpyAsync(y, dx + 64, sizeof y, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    int best[3];
+    for (int part = 0; part < 3; ++part) {
+        best[part] = 0;
+        for (int k = 1; k < MLP_OUT; ++k)
+            if (y[part][k] < y[part][best[part]]) best[part] = k;
+    }
+    const double whole = std::exp((double)y[0][best[0]]);
+    const double parts = std::exp((double)y[1][best[1]]) + std::exp((double)y[2][best[2]]);
+    hyset_ctx::SplitPlan plan{0, kSelectable[best[1]], kSelectable[best[2]]};
+    if (best[1] != best[2] && parts < SPLIT_MARGIN * whole) plan.at = mid;
+    ctx->split_cache[key] = plan;
+    *split_at = plan.at;
+    *low = plan.low;
+    *high = plan.high;
+    return HYSET_OK;
+}
+
 // Autotuner for the prefix-index join's signature width: on the first AUTO join
 // of a (collections, similarity, threshold), the probe-major kernel runs on
 // three probe samples spread over the probe range with no signatures and with
@@ -784,6 +842,36 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     const bool swapped = swap_sides(R, S, o);
     if (swapped) std::swap(R, S);
     const bool self = (S == R);
+    if (self) {
+        uint32_t split_at = 0;
+        hyset_technique low = HYSET_TECH_AUTO, high = HYSET_TECH_AUTO;
+        ST(plan_split(ctx, R, o, &split_at, &low, &high));
+        if (split_at) {  // two probe ranges, each with its technique; pairs of the low range first
+            hyset_result part[2];
+            for (int k = 0; k < 2; ++k) {
+                hyset_join_opts q = *o;
+                q.technique = k == 0 ? low : high;
+                q.probe_major = 1;
+                q.probe_begin = k == 0 ? 0 : split_at;
+                q.probe_end = k == 0 ? split_at : R->n;
+                ST(do_join(ctx, R, S, &q, &part[k]));
+            }
+            res->count = part[0].count + part[1].count;
+            res->has_pairs = part[0].has_pairs;
+            res->pairs = std::move(part[0].pairs);
+            res->pairs.insert(res->pairs.end(), part[1].pairs.begin(), part[1].pairs.end());
+            res->device_ms = part[0].device_ms + part[1].device_ms;
+            res->kernel_ms = part[0].kernel_ms + part[1].kernel_ms;
+            for (int k = 0; k < 8; ++k) res->stats[k] = part[0].stats[k] + part[1].stats[k];
+            res->launches = part[0].launches + part[1].launches;
+            res->technique = part[1].technique;
+            res->bitmap_bits = part[1].bitmap_bits;
+            res->selector = 2;
+            res->split_at = split_at;
+            res->split_low = part[0].technique;
+            return HYSET_OK;
+        }
+    }
     const uint32_t L = std::max(R->max_size, S->max_size);
     Bounds* b = nullptr;
     ST(get_bounds(ctx, o->sim, o->threshold, L, self ? 0 : 1, &b));
@@ -1927,6 +2015,7 @@ hyset_status hyset_selector_set(hyset_ctx* ctx, const float* params, const float
     if (!ctx) return HYSET_E_INVALID;
     CK(cudaSetDevice(ctx->device));
     ctx->select_cache.clear();
+    ctx->split_cache.clear();
     ctx->has_mlp = false;
     if (params) {
         if (!feature_mean || !feature_scale) return fail(ctx, HYSET_E_INVALID, "normalisation missing");
@@ -1956,6 +2045,10 @@ const hyset_pair* hyset_result_pairs(const hyset_result* r) {
 uint64_t hyset_result_launches(const hyset_result* r) { return r ? r->launches : 0; }
 hyset_technique hyset_result_technique(const hyset_result* r) { return r ? r->technique : HYSET_TECH_AUTO; }
 uint32_t hyset_result_bitmap_bits(const hyset_result* r) { return r ? r->bitmap_bits : 0; }
+uint32_t hyset_result_split(const hyset_result* r, hyset_technique* low_technique) {
+    if (low_technique) *low_technique = r ? r->split_low : HYSET_TECH_AUTO;
+    return r ? r->split_at : 0;
+}
 double hyset_result_device_ms(const hyset_result* r) { return r ? r->device_ms : 0.0; }
 double hyset_result_kernel_ms(const hyset_result* r) { return r ? r->kernel_ms : 0.0; }
 const void* hyset_result_device_pairs(const hyset_result* r) { return r ? r->device_pairs : nullptr; }

@@ -139,6 +139,11 @@ struct hyset_ctx {
     std::map<std::string, std::pair<hyset_technique, int>> select_cache;  // decision, selector
     std::map<std::string, uint32_t> bits_cache;  // autotuned signature width per join
     std::map<std::string, uint32_t> universe_cache;  // universe by collection size profile (host-input joins)
+    struct SplitPlan {
+        uint32_t at;  // first probe id of the high range; 0 = no split
+        hyset_technique low, high;
+    };
+    std::map<std::string, SplitPlan> split_cache;  // partition plans of AUTO self-joins
 };
 
 struct hyset_coll {
@@ -168,6 +173,8 @@ struct hyset_result {
     const void* device_pairs = nullptr;
     hyset_technique technique = HYSET_TECH_AUTO;
     uint32_t bitmap_bits = 0;  // signature width the join ran with
+    uint32_t split_at = 0;     // partition split: first probe id of the high range (0 = none)
+    hyset_technique split_low = HYSET_TECH_AUTO;  // the low range's technique
     double device_ms = 0;
     double kernel_ms = 0;
     uint64_t stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};

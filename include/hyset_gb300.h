@@ -172,6 +172,11 @@ uint64_t hyset_result_count(const hyset_result* r);
 const hyset_pair* hyset_result_pairs(const hyset_result* r); /* NULL when count_only */
 hyset_technique hyset_result_technique(const hyset_result* r);
 uint32_t hyset_result_bitmap_bits(const hyset_result* r);   /* signature width used (0 = none) */
+/* Partition split chosen by the learned selector for an AUTO self-join: the
+ * first probe id of the high range (0 = the join ran as one range) and, in
+ * *low_technique (may be NULL), the low range's technique (the high range's is
+ * hyset_result_technique). */
+uint32_t hyset_result_split(const hyset_result* r, hyset_technique* low_technique);
 double hyset_result_device_ms(const hyset_result* r);       /* CUDA-event time of the join's device work */
 double hyset_result_kernel_ms(const hyset_result* r);       /* CUDA-event time of the filter+verify launch */
 /* Device pointer to count (first, second) uint32 pairs when device_pairs was

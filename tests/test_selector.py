@@ -149,3 +149,41 @@ def test_shipped_report_recomputes_from_samples():
     assert abs(np.mean(reg_rules) - rep["rules"]["mean_regret"]) < 1e-3
     assert abs(np.mean(reg_mlp) - rep["mlp"]["mean_regret"]) < 0.02  # float32 GPU vs float64 argmin ties
     assert np.mean(reg_mlp) < np.mean(reg_rules)
+
+
+@pytest.mark.gpu
+def test_learned_partition_split_keeps_the_pairs():
+    """A network that prefers the bitmap technique for short sets and the prefix
+    index for long ones, and finds both dear on the whole range, splits an AUTO
+    self-join into two probe ranges; the pairs stay the oracle's."""
+    import hyset_gb300 as hs
+    import oracle
+    from hyset_gb300 import synth
+    c = synth.generate(synth.C2, n_sets=60000, seed=130)
+    sctx = hs.Context(0, selector=False)
+    coll = sctx.upload(c.tokens, c.sizes, c.starts)
+    n, mid = c.n, c.n // 2
+    f_low, _ = sctx.features(coll, threshold=0.6, probe_range=(0, mid))
+    f_high, _ = sctx.features(coll, threshold=0.6, probe_range=(mid, n))
+    assert f_low[1] < f_high[1]
+    T, L = (f_low[1] + f_high[1]) / 2, f_low[0]
+    W1, b1 = np.zeros((12, 64)), np.zeros(64)
+    W1[1, 0], b1[0] = 1.0, -T          # h0: the range's sets are long
+    W1[1, 1], b1[1] = -1.0, T          # h1: the range's sets are short
+    W1[0, 2], b1[2] = 1.0, -(L + 0.5)  # h2: more probes than a half
+    W2, b2 = np.zeros((64, 64)), np.zeros(64)
+    W2[0, 0] = W2[1, 1] = W2[2, 2] = 1.0
+    W3, b3 = np.zeros((64, 3)), np.array([1.0, 1.0, 20.0])
+    W3[0, 0] = 10.0                    # bitmap dear on long sets
+    W3[1, 1] = 10.0                    # prefix index dear on short sets
+    W3[2, 0] = W3[2, 1] = 8.0          # both dear on the whole range
+    params = np.concatenate([a.ravel() for a in (W1, b1, W2, b2, W3, b3)]).astype(np.float32)
+    sctx.selector_set(params, np.zeros(12, np.float32), np.ones(12, np.float32))
+    exp = oracle.join(c.tokens, c.starts, c.sizes, 0.6)
+    r = sctx.self_join(coll, threshold=0.6)
+    assert r.split_at == mid and r.split_low == "bitmap" and r.technique == "fgss"
+    assert r.count == len(exp) and oracle.as_set(r.pairs) == oracle.as_set(exp)
+    rs = sctx.self_join(coll, threshold=0.6, sort_pairs=True)
+    np.testing.assert_array_equal(rs.pairs, exp[np.lexsort((exp[:, 1], exp[:, 0]))])
+    assert sctx.self_join(coll, threshold=0.6, count_only=True).count == len(exp)
+    sctx.close()
