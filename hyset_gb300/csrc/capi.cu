@@ -1402,6 +1402,19 @@ hyset_status hyset_collection_from_device(hyset_ctx* ctx, const uint32_t* d_toke
     return HYSET_OK;
 }
 
+namespace {
+constexpr uint64_t PIPE_CHUNK_TOKENS = 16ull << 20;  // 64 MB of tokens per copy chunk
+
+cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k) {
+    while (ctx->pipe_ev.size() <= k) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        ctx->pipe_ev.push_back(e);
+    }
+    return ctx->pipe_ev[k];
+}
+}  // namespace
+
 hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n_bytes, hyset_coll** out) {
     if (!ctx || !out || (n_bytes && !text)) return fail(ctx, HYSET_E_INVALID, "null argument");
     if (n_bytes >= (1ull << 33)) return fail(ctx, HYSET_E_UNSUPPORTED, "text of 2^33 bytes or more");
@@ -1420,9 +1433,26 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
     } rel{{&staged, &counts, &err}, s};
     cudaPointerAttributes attr{};
     if (cudaPointerGetAttributes(&attr, text) != cudaSuccess) cudaGetLastError();
+    // host text travels in 64 MB chunks on the auxiliary stream; the tiles of a
+    // chunk are counted once it and the next chunk (a tile reads one byte past
+    // its end) have landed, so counting overlaps the copy
+    constexpr uint64_t PARSE_CHUNK = 64ull << 20;  // a multiple of the 4 KiB tile
+    uint64_t n_chunks = 0;
     if (n_bytes && attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) {
         CK(staged.ensure(n_bytes + 16, s));
-        CK(cudaMemcpyAsync(staged.p, text, n_bytes, cudaMemcpyHostToDevice, s));
+        CK(cudaEventRecord(ctx->ev_fork, s));
+        CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
+        n_chunks = (n_bytes + PARSE_CHUNK - 1) / PARSE_CHUNK;
+        for (uint64_t k = 0; k < n_chunks; ++k) {
+            const uint64_t b0 = k * PARSE_CHUNK, b1 = std::min(n_bytes, b0 + PARSE_CHUNK);
+            CK(cudaMemcpyAsync(staged.as<uint8_t>() + b0, text + b0, b1 - b0, cudaMemcpyHostToDevice, ctx->aux));
+            cudaEvent_t e = pipe_event(ctx, k);
+            if (!e) {
+                cudaStreamSynchronize(ctx->aux);
+                return fail(ctx, HYSET_E_CUDA, "event creation");
+            }
+            CK(cudaEventRecord(e, ctx->aux));
+        }
         d_text = staged.as<uint8_t>();
     }
     if (n_bytes && (reinterpret_cast<uintptr_t>(d_text) & 15u)) {  // tiles load 16-byte words
@@ -1444,7 +1474,15 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
     CK(cudaMemsetAsync(flags, 0, 8, s));
     CK(cudaMemsetAsync(first_bad, 0xFF, 8, s));
     CK(cudaMemsetAsync(tile_toks, 0, (2 * tiles + 2) * 4, s));
-    CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s));
+    if (n_chunks) {
+        const uint64_t per = PARSE_CHUNK / 4096;  // tiles per chunk
+        for (uint64_t k = 0; k < n_chunks; ++k) {
+            CK(cudaStreamWaitEvent(s, pipe_event(ctx, std::min(k + 1, n_chunks - 1)), 0));
+            CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s, k * per, (k + 1) * per));
+        }
+    } else {
+        CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s));
+    }
     CK(ctx->sc->scan.ensure(scan_scratch_words(tiles + 1) * 4, s));
     CK(scan_exclusive(tile_toks, tile_toks, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
     CK(scan_exclusive(tile_lines, tile_lines, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
@@ -1569,18 +1607,7 @@ hyset_status hyset_rs_join(hyset_ctx* ctx, const hyset_coll* indexed, const hyse
 
 // ---------------------------------------------------------------- joins from host arrays
 
-namespace {
-constexpr uint64_t PIPE_CHUNK_TOKENS = 16ull << 20;  // 64 MB of tokens per copy chunk
 
-cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k) {
-    while (ctx->pipe_ev.size() <= k) {
-        cudaEvent_t e = nullptr;
-        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
-        ctx->pipe_ev.push_back(e);
-    }
-    return ctx->pipe_ev[k];
-}
-}  // namespace
 
 // The upload and the self-join in one call.  The tokens go to the device in
 // 64 MB chunks on the auxiliary stream; while the later chunks are in flight,

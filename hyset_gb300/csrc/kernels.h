@@ -28,8 +28,11 @@ constexpr uint32_t PARSE_E_RANGE = 8;       // a number of more than 10 digits o
 uint64_t parse_tiles(uint64_t n_bytes);
 // Per 4 KiB tile: token starts and line starts; flags / first_bad (byte offset,
 // atomicMin) record errors.
+// Tiles [tile_lo, tile_hi) only (default: all); a tile reads one byte on
+// either side of its 4 KiB.
 cudaError_t parse_count(const uint8_t* text, uint64_t n_bytes, uint32_t* tile_toks, uint32_t* tile_lines,
-                        uint32_t* flags, unsigned long long* first_bad, cudaStream_t s);
+                        uint32_t* flags, unsigned long long* first_bad, cudaStream_t s, uint64_t tile_lo = 0,
+                        uint64_t tile_hi = ~0ull);
 // tile_tok0 / tile_line0: exclusive scans of the tile counts.  Writes every
 // token and line_tok0[line] = index of the line's first token.
 cudaError_t parse_emit(const uint8_t* text, uint64_t n_bytes, const uint32_t* tile_tok0, const uint32_t* tile_line0,

@@ -118,10 +118,11 @@ __device__ __forceinline__ void record_error(uint32_t err, uint64_t at, uint32_t
 }
 
 __global__ void __launch_bounds__(PARSE_THREADS) k_parse_count(const uint8_t* __restrict__ t, uint64_t n,
-                                                               uint32_t* tile_toks, uint32_t* tile_lines,
-                                                               uint32_t* flags, unsigned long long* first_bad) {
+                                                               uint64_t tile0, uint32_t* tile_toks,
+                                                               uint32_t* tile_lines, uint32_t* flags,
+                                                               unsigned long long* first_bad) {
     __shared__ uint32_t red[2][PARSE_THREADS / 32];
-    const uint64_t tile = blockIdx.x;
+    const uint64_t tile = tile0 + blockIdx.x;
     const uint64_t base = tile * PARSE_TILE + (uint64_t)threadIdx.x * PARSE_BYTES;
     uint32_t w[4];
     Masks m;
@@ -317,12 +318,15 @@ __global__ void k_line_sizes(const uint32_t* __restrict__ line_tok0, uint32_t n_
 uint64_t parse_tiles(uint64_t n_bytes) { return (n_bytes + PARSE_TILE - 1) / PARSE_TILE; }
 
 cudaError_t parse_count(const uint8_t* text, uint64_t n_bytes, uint32_t* tile_toks, uint32_t* tile_lines,
-                        uint32_t* flags, unsigned long long* first_bad, cudaStream_t s) {
+                        uint32_t* flags, unsigned long long* first_bad, cudaStream_t s, uint64_t tile_lo,
+                        uint64_t tile_hi) {
     const uint64_t tiles = parse_tiles(n_bytes);
-    if (tiles == 0) return cudaSuccess;
-    if (tiles > 0x7FFFFFFFull) return cudaErrorInvalidValue;
+    if (tile_hi > tiles) tile_hi = tiles;
+    if (tile_hi <= tile_lo) return cudaSuccess;
+    if (tile_hi - tile_lo > 0x7FFFFFFFull) return cudaErrorInvalidValue;
     note_launches();
-    k_parse_count<<<(unsigned)tiles, PARSE_THREADS, 0, s>>>(text, n_bytes, tile_toks, tile_lines, flags, first_bad);
+    k_parse_count<<<(unsigned)(tile_hi - tile_lo), PARSE_THREADS, 0, s>>>(text, n_bytes, tile_lo, tile_toks,
+                                                                         tile_lines, flags, first_bad);
     return cudaGetLastError();
 }
 
