@@ -288,11 +288,12 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     const uint32_t pb = force_pb > 0 ? (uint32_t)force_pb : bits_for(max_pre), sb = bits_for(n);
     if (force_pb != 0 && pb + sb <= 32) {
         uint32_t* counts = ctx->sc->counts.as<uint32_t>();
+        CK(ctx->sc->gate.ensure(4, s));
         CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
         CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
-        CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
-        CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
-                            ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
+        CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts, ix.list_off.as<uint32_t>(),
+                       ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(), ctx->sc->gate.as<uint32_t>(),
+                       key_bits_for(U), scr, s));
         ix.sim = b->sim;
         ix.tau = b->tau;
         ix.kind = kind;
@@ -309,7 +310,7 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, scr, s));
     CK(iota_u32(ctx->sc->order.as<uint32_t>(), E, s));
     CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ctx->sc->order.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
-                        ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), scr, s));
+                        ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), scr, s, false));
     CK(gather_entries(ctx->sc->order.as<uint32_t>(), E, ctx->sc->set.as<uint32_t>(), ctx->sc->pos.as<uint32_t>(),
                       ix.set.as<uint32_t>(), ix.pos.as<uint32_t>(), s));
     ix.sim = b->sim;
@@ -1200,6 +1201,7 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
     CK(ctx->sc->order.ensure(e4, s));
     CK(ctx->sc->altk.ensure(e4, s));
     CK(ctx->sc->altv.ensure(e4, s));
+    CK(ctx->sc->gate.ensure(4, s));
     CK(ctx->sc->counts.ensure((size_t)maxU * 4, s));
     const size_t scan_words = std::max(std::max(scan_scratch_words(maxN), scan_scratch_words(maxU)),
                                        radix_scratch_words(maxE));
@@ -1744,6 +1746,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         CK(ctx->sc->tok.ensure(E ? E * 4 : 4, s));
         CK(ctx->sc->altk.ensure(E ? E * 4 : 4, s));
         CK(ctx->sc->altv.ensure(E ? E * 4 : 4, s));
+        CK(ctx->sc->gate.ensure(4, s));
         Index& ix = C->index;
         CK(ix.set.ensure(E ? E * 4 : 4, s));
         CK(ix.pos.ensure(4, s));
@@ -1814,9 +1817,9 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             uint32_t* counts = ctx->sc->counts.as<uint32_t>();
             CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
             CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
-            CK(scan_exclusive(counts, ix.list_off.as<uint32_t>(), (uint64_t)U + 1, ctx->sc->scan.as<uint32_t>(), s));
-            CK(radix_sort_pairs(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(),
-                                ctx->sc->altv.as<uint32_t>(), E, key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));
+            CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts,
+                           ix.list_off.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(),
+                           ctx->sc->gate.as<uint32_t>(), key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));
             ix.sim = b->sim;
             ix.tau = b->tau;
             ix.kind = 0;

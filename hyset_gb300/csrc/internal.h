@@ -91,9 +91,9 @@ struct BatchJoin {
 // Scratch of an index build (prefix lengths and offsets, entries, radix sort
 // ping-pong buffers, token counts, scan/sort scratch).
 struct Scratch {
-    DevBuf len, off, tok, set, pos, order, altk, altv, counts, scan;
+    DevBuf len, off, tok, set, pos, order, altk, altv, counts, scan, gate;
     void release(cudaStream_t s) {
-        DevBuf* all[] = {&len, &off, &tok, &set, &pos, &order, &altk, &altv, &counts, &scan};
+        DevBuf* all[] = {&len, &off, &tok, &set, &pos, &order, &altk, &altv, &counts, &scan, &gate};
         for (DevBuf* d : all) d->release(s);
     }
 };

@@ -46,14 +46,33 @@ cudaError_t parse_line_sizes(const uint32_t* line_tok0, uint32_t n_lines, uint32
 // Exclusive prefix sum of n uint32 values (in may equal out).  `scratch` must
 // hold scan_scratch_words(n) words.
 size_t scan_scratch_words(uint64_t n);
-cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s);
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s,
+                           const uint32_t* gate = nullptr);
 
 // Stable LSD radix sort of (key, value) pairs on the low `key_bits` bits of the
 // keys.  Result lands in keys/vals; alt_* are ping-pong buffers of n words;
-// `scratch` holds radix_scratch_words(n) words.
+// `scratch` holds radix_scratch_words(n) words.  keep_keys = false leaves the
+// keys array unsorted (only the values are wanted; the last pass skips them).
 size_t radix_scratch_words(uint64_t n);
+// gate: when non-null, every kernel of the sort runs only if the device word
+// is above the short-list bound (see index_lists).
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals,
-                             uint64_t n, int key_bits, uint32_t* scratch, cudaStream_t s);
+                             uint64_t n, int key_bits, uint32_t* scratch, cudaStream_t s, bool keep_keys = true,
+                             const uint32_t* gate = nullptr);
+
+// The index lists from prefix entries emitted in set order (e_token, e_val)
+// and the per-token counts of tokens below U (counts[U+1]): list_off[U+1]
+// (exclusive scan of counts) and e_val reordered so that each list holds its
+// entries in emission order.  Without a host round trip: the longest list is
+// written to *gate on the device; when every list has at most 64 entries the
+// entries are scattered into their lists with atomics and each list is
+// ordered by a rank sort inside a warp, otherwise the stable radix passes on
+// the token sort them (each kernel checks the gate and returns early when it
+// is not its case).  counts, e_token, alt_* and scratch (max of
+// scan_scratch_words(U + 1) and radix_scratch_words(n) words) are clobbered.
+cudaError_t index_lists(uint32_t* e_token, uint32_t* e_val, uint64_t n, uint32_t U, uint32_t* counts,
+                        uint32_t* list_off, uint32_t* alt_keys, uint32_t* alt_vals, uint32_t* gate, int key_bits,
+                        uint32_t* scratch, cudaStream_t s);
 
 // Prefix entries of sets [lo, hi): the first prefix_len(size) tokens of every
 // set (include/hyset/collection.hpp:128-135).  entry_off must hold the

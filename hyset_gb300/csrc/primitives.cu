@@ -18,6 +18,12 @@ void note_launches(unsigned n) { g_launches += n; }
 
 namespace {
 
+// Index lists of at most LIST_SHORT entries are ordered by a rank sort inside
+// one warp (k_list_rank); longer ones go through the radix passes.
+constexpr uint32_t LIST_SHORT = 64;
+constexpr int RANK_THREADS = 128;
+constexpr uint32_t RANK_CAP = 2048;  // staged entries per warp: 32 lists of up to 64
+
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
 constexpr uint32_t SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;  // 2048
@@ -41,7 +47,14 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_s
     return r;
 }
 
-__global__ void __launch_bounds__(SCAN_THREADS) k_tile_reduce(const uint32_t* in, uint64_t n, uint32_t* sums) {
+// gate: when non-null, the scans (and the radix kernels) run only when the
+// word is above LIST_SHORT (an index whose lists are not all short is sorted
+// by the radix passes; see k_list_scatter)
+__device__ __forceinline__ bool gated_off(const uint32_t* gate) { return gate && *gate <= LIST_SHORT; }
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_reduce(const uint32_t* in, uint64_t n, uint32_t* sums,
+                                                              const uint32_t* gate) {
+    if (gated_off(gate)) return;
     __shared__ uint32_t ws[SCAN_THREADS / 32 + 1];
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
     uint32_t s = 0;
@@ -55,7 +68,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_reduce(const uint32_t* in
 
 // in/out may alias: every tile reads all its inputs before writing.
 __global__ void __launch_bounds__(SCAN_THREADS) k_tile_scan(const uint32_t* in, uint32_t* out, uint64_t n,
-                                                            const uint32_t* tile_off) {
+                                                            const uint32_t* tile_off, const uint32_t* gate) {
+    if (gated_off(gate)) return;
     __shared__ uint32_t ws[SCAN_THREADS / 32 + 1];
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE + (uint64_t)threadIdx.x * SCAN_ITEMS;
     uint32_t v[SCAN_ITEMS];
@@ -85,15 +99,21 @@ constexpr int RADIX_BINS = 1 << RADIX_MAX_BITS;
 
 __global__ void __launch_bounds__(RADIX_THREADS) k_radix_upsweep(const uint32_t* keys, uint64_t n, int shift,
                                                                  uint32_t mask, uint32_t* tile_counts,
-                                                                 uint32_t tiles) {
+                                                                 uint32_t tiles, const uint32_t* gate) {
+    if (gated_off(gate)) return;
     __shared__ uint32_t hist[RADIX_BINS];
+    const uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE + threadIdx.x;
+    uint32_t k[RADIX_ROUNDS];  // loads first, in flight under the zeroing
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        const uint64_t idx = base + (uint64_t)r * RADIX_THREADS;
+        k[r] = idx < n ? keys[idx] : 0u;
+    }
     for (uint32_t d = threadIdx.x; d <= mask; d += RADIX_THREADS) hist[d] = 0;
     __syncthreads();
-    uint64_t base = (uint64_t)blockIdx.x * RADIX_TILE;
-    for (uint32_t i = threadIdx.x; i < RADIX_TILE; i += RADIX_THREADS) {
-        uint64_t idx = base + i;
-        if (idx < n) atomicAdd(&hist[(keys[idx] >> shift) & mask], 1u);
-    }
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r)
+        if (base + (uint64_t)r * RADIX_THREADS < n) atomicAdd(&hist[(k[r] >> shift) & mask], 1u);
     __syncthreads();
     for (uint32_t d = threadIdx.x; d <= mask; d += RADIX_THREADS)
         tile_counts[(uint64_t)d * tiles + blockIdx.x] = hist[d];
@@ -104,7 +124,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_upsweep(const uint32_t*
 // order, 32 at a time, peers found with __match_any_sync).  The tile is first
 // reordered by digit in shared memory, so each digit's run of the tile leaves
 // as consecutive addresses (coalesced stores instead of one sector per item).
-constexpr int RADIX_THREAD_BINS = RADIX_BINS / RADIX_THREADS;  // 4
+constexpr int RADIX_THREAD_BINS = RADIX_BINS / RADIX_THREADS;  // 2
 struct RadixSmem {
     union {
         uint32_t whist[RADIX_WARPS][RADIX_BINS];  // per-warp digit counts, then per-warp bases
@@ -114,49 +134,60 @@ struct RadixSmem {
     } u;
     uint32_t start[RADIX_BINS];  // tile-local first position of each digit
     uint32_t gpos[RADIX_BINS];   // global first position of each digit for this tile
-    uint32_t wsum[RADIX_WARPS];
+    uint32_t wsum[RADIX_THREAD_BINS][RADIX_WARPS];
 };
 
-__global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_t* __restrict__ keys,
+#ifndef HS_RADIX_MIN_BLOCKS
+#define HS_RADIX_MIN_BLOCKS 2  // 54 registers, no spills; two 72 KB blocks per SM
+#endif
+__global__ void __launch_bounds__(RADIX_THREADS, HS_RADIX_MIN_BLOCKS) k_radix_downsweep(const uint32_t* __restrict__ keys,
                                                                    const uint32_t* __restrict__ vals, uint64_t n,
                                                                    int shift, uint32_t mask,
                                                                    const uint32_t* __restrict__ tile_off,
                                                                    uint32_t tiles, uint32_t* keys_out,
-                                                                   uint32_t* vals_out) {
+                                                                   uint32_t* vals_out, const uint32_t* gate) {
+    if (gated_off(gate)) return;
     extern __shared__ __align__(16) uint8_t radix_smem[];
     RadixSmem& sm = *reinterpret_cast<RadixSmem*>(radix_smem);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t bins = mask + 1;
-    for (uint32_t d = threadIdx.x; d < RADIX_BINS; d += RADIX_THREADS)
-#pragma unroll
-        for (int w = 0; w < RADIX_WARPS; ++w) sm.u.whist[w][d] = 0;
-    __syncthreads();
     const uint64_t tile_base = (uint64_t)blockIdx.x * RADIX_TILE;
     const uint64_t base = tile_base + (uint64_t)warp * (32 * RADIX_ROUNDS);
     uint32_t k[RADIX_ROUNDS], v[RADIX_ROUNDS], rank[RADIX_ROUNDS];
+    // the warp's key loads first (8 in flight per thread, under the zeroing
+    // below), then the ranking rounds, whose warp barriers would otherwise hold
+    // each round's load behind the previous round; the values follow later
 #pragma unroll
     for (int r = 0; r < RADIX_ROUNDS; ++r) {
-        uint64_t idx = base + (uint64_t)r * 32 + lane;
-        bool valid = idx < n;
-        uint32_t key = valid ? keys[idx] : 0;
-        uint32_t d = valid ? ((key >> shift) & mask) : 0xFFFFFFFFu;
-        unsigned peers = __match_any_sync(FULL, d);
-        int leader = __ffs(peers) - 1;
-        uint32_t cnt = valid ? sm.u.whist[warp][d] : 0;
+        const uint64_t idx = base + (uint64_t)r * 32 + lane;
+        k[r] = idx < n ? keys[idx] : 0u;
+    }
+    {  // zero the per-warp counts, 16 bytes a store
+        uint4* z = reinterpret_cast<uint4*>(&sm.u.whist[0][0]);
+        for (uint32_t q = threadIdx.x; q < RADIX_WARPS * RADIX_BINS / 4; q += RADIX_THREADS)
+            z[q] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        const bool valid = base + (uint64_t)r * 32 + lane < n;
+        const uint32_t d = valid ? ((k[r] >> shift) & mask) : 0xFFFFFFFFu;
+        const unsigned peers = __match_any_sync(FULL, d);
+        const int leader = __ffs(peers) - 1;
+        const uint32_t cnt = valid ? sm.u.whist[warp][d] : 0;
         __syncwarp();
         if (valid && lane == leader) sm.u.whist[warp][d] = cnt + __popc(peers);
         __syncwarp();
         rank[r] = cnt + __popc(peers & lanemask_lt(lane));
-        k[r] = key;
-        v[r] = valid ? vals[idx] : 0;
     }
     __syncthreads();
-    // per digit: warp bases (exclusive over warps) and the digit's tile total;
-    // thread t owns digits [4t, 4t+4)
-    uint32_t tot[RADIX_THREAD_BINS], run = 0;
+    // per digit: warp bases (exclusive over warps) and the digit's tile total.
+    // Thread t owns digits t and t + 512, so a warp's accesses are 32
+    // consecutive words (no bank conflicts).
+    uint32_t tot[RADIX_THREAD_BINS];
 #pragma unroll
     for (int j = 0; j < RADIX_THREAD_BINS; ++j) {
-        const uint32_t d = threadIdx.x * RADIX_THREAD_BINS + j;
+        const uint32_t d = threadIdx.x + j * RADIX_THREADS;
         uint32_t acc = 0;
 #pragma unroll
         for (int w = 0; w < RADIX_WARPS; ++w) {
@@ -165,20 +196,34 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_
             acc += c;
         }
         tot[j] = acc;
-        run += acc;
     }
-    // block exclusive scan of the per-thread digit totals -> tile-local digit starts
-    const uint32_t incl = warp_incl_scan(run, lane);
-    if (lane == 31) sm.wsum[warp] = incl;
-    __syncthreads();
-    uint32_t before = incl - run;
-    for (int w = 0; w < warp; ++w) before += sm.wsum[w];
+    // tile-local digit starts: an exclusive scan over the digits in order,
+    // digits [0, 512) in thread order, then [512, 1024) after all of them
+    uint32_t incl[RADIX_THREAD_BINS];
 #pragma unroll
     for (int j = 0; j < RADIX_THREAD_BINS; ++j) {
-        const uint32_t d = threadIdx.x * RADIX_THREAD_BINS + j;
+        incl[j] = warp_incl_scan(tot[j], lane);
+        if (lane == 31) sm.wsum[j][warp] = incl[j];
+    }
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; ++r) {
+        const uint64_t idx = base + (uint64_t)r * 32 + lane;
+        v[r] = idx < n ? vals[idx] : 0u;
+    }
+    __syncthreads();
+    uint32_t carry = 0;
+#pragma unroll
+    for (int j = 0; j < RADIX_THREAD_BINS; ++j) {
+        uint32_t before = carry + incl[j] - tot[j];
+#pragma unroll
+        for (int w = 0; w < RADIX_WARPS; ++w) {
+            const uint32_t ws = sm.wsum[j][w];
+            if (w < warp) before += ws;
+            carry += ws;
+        }
+        const uint32_t d = threadIdx.x + j * RADIX_THREADS;
         sm.start[d] = before;
         sm.gpos[d] = d < bins ? tile_off[(uint64_t)d * tiles + blockIdx.x] : 0u;
-        before += tot[j];
     }
     __syncthreads();
     // tile-local sorted position of every item (registers), then the tile in
@@ -203,7 +248,7 @@ __global__ void __launch_bounds__(RADIX_THREADS) k_radix_downsweep(const uint32_
         const uint32_t key = sm.u.tile.k[i];
         const uint32_t d = (key >> shift) & mask;
         const uint32_t pos = sm.gpos[d] + (i - sm.start[d]);
-        keys_out[pos] = key;
+        if (keys_out) keys_out[pos] = key;
         vals_out[pos] = sm.u.tile.v[i];
     }
 }
@@ -232,28 +277,174 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
     }
 }
 
-// One warp per set: (token, (set << pos_bits) | position) for the first len
-// tokens, and the token histogram with one atomic per distinct token per warp.
-// Sets [lo, c.n): c, off and len are indexed by absolute set id.  counts may be
-// nullptr (no histogram: the caller counts the emitted tokens later).
+// (token, (set << pos_bits) | position) for the first len tokens of every set,
+// and the token histogram (one atomic per entry).  A warp takes 32 consecutive
+// sets: their entries are contiguous in the output (off is the scan of len),
+// so the warp walks them flattened, 32 entries per round, each lane finding
+// its set by a 5-step bisection over the lanes' running lengths.  Every lane
+// carries an entry in every round (prefixes are far shorter than 32), the
+// stores coalesce, and the token loads of EMIT_ROUNDS rounds are issued before
+// any of their stores.  Sets [lo, c.n): c, off and len are indexed by absolute
+// set id.  counts may be nullptr (no histogram).
+constexpr int EMIT_ROUNDS = 4;
 __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
-                              const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* e_token, uint32_t* e_val,
-                              uint32_t* counts) {
+                              const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
+                              uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts) {
     const int lane = threadIdx.x & 31;
-    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t s = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); s < c.n; s += warps) {
-        const uint32_t l = len[s], o = off[s];
-        const uint32_t* t = c.tokens + c.meta[s].x;
-        for (uint32_t i0 = 0; i0 < l; i0 += 32) {
-            const uint32_t i = i0 + lane;
-            const bool valid = i < l;
-            const uint32_t tok = valid ? __ldg(t + i) : 0xFFFFFFFFu;
-            if (valid) {
-                e_token[o + i] = tok;
-                e_val[o + i] = (s << pos_bits) | i;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t s0 = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; s0 < c.n; s0 += warps * 32u) {
+        const uint32_t s = s0 + lane;
+        const bool has = s < c.n;
+        const uint32_t l = has ? len[s] : 0u;
+        const uint32_t start = has ? c.meta[s].x : 0u;
+        const uint32_t o0 = __shfl_sync(FULL, has ? off[s] : 0u, 0);
+        const uint32_t incl = warp_incl_scan(l, lane);
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        for (uint32_t j0 = 0; j0 < total; j0 += 32 * EMIT_ROUNDS) {
+            uint32_t tok[EMIT_ROUNDS], val[EMIT_ROUNDS];
+#pragma unroll
+            for (int u = 0; u < EMIT_ROUNDS; ++u) {
+                const uint32_t j = j0 + 32u * u + lane;
+                int k = 0;  // first lane whose running length exceeds j
+#pragma unroll
+                for (int step = 16; step; step >>= 1)
+                    if (__shfl_sync(FULL, incl, k + step - 1) <= j) k += step;
+                const uint32_t end_k = __shfl_sync(FULL, incl, k);
+                const uint32_t len_k = __shfl_sync(FULL, l, k);
+                const uint32_t start_k = __shfl_sync(FULL, start, k);
+                const uint32_t i = j - (end_k - len_k);
+                tok[u] = j < total ? __ldg(c.tokens + start_k + i) : 0u;
+                val[u] = ((s0 + (uint32_t)k) << pos_bits) | i;
             }
-            // tokens inside one set are distinct: one atomic per lane
-            if (valid && counts) atomicAdd(&counts[tok], 1u);
+#pragma unroll
+            for (int u = 0; u < EMIT_ROUNDS; ++u) {
+                const uint32_t j = j0 + 32u * u + lane;
+                if (j < total) {
+                    e_token[o0 + j] = tok[u];
+                    e_val[o0 + j] = val[u];
+                    // tokens inside one set are distinct: one atomic per entry
+                    if (counts) atomicAdd(&counts[tok[u]], 1u);
+                }
+            }
+        }
+    }
+}
+
+// gate = the longest list: the maximum of the per-token counts of tokens
+// below U, reduced per block (one atomic per block on the single word; the
+// caller zeroes it).
+__global__ void k_list_max(const uint32_t* __restrict__ counts, uint32_t U, uint32_t* gate) {
+    __shared__ uint32_t wm[32];
+    uint32_t m = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < U; t += stride) m = max(m, counts[t]);
+    m = __reduce_max_sync(FULL, m);
+    if ((threadIdx.x & 31) == 0) wm[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? wm[threadIdx.x] : 0u;
+        m = __reduce_max_sync(FULL, m);
+        if (threadIdx.x == 0 && m) atomicMax(gate, m);
+    }
+}
+
+// Short-list index build, step 1 (runs when every list is short): each entry
+// (token t, value v) takes the next slot of list t from an atomic on the
+// list's cursor (initialised to the list offsets), so each list holds its
+// entries in arbitrary order.  Tokens at or above U are left out (the counts
+// did not count them).
+constexpr int SCATTER_ITEMS = 4;  // entries per thread per step: four atomics in flight
+__global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t* __restrict__ val, uint64_t n,
+                               uint32_t U, uint32_t* __restrict__ cursor, uint32_t* __restrict__ out,
+                               const uint32_t* gate, bool vec) {
+    if (*gate > LIST_SHORT) return;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * SCATTER_ITEMS;
+    for (uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * SCATTER_ITEMS; i0 < n; i0 += stride) {
+        uint32_t t[SCATTER_ITEMS], v[SCATTER_ITEMS], at[SCATTER_ITEMS];
+        if (vec && i0 + SCATTER_ITEMS <= n) {  // 16-byte loads (vec: both arrays 16-byte aligned)
+            const uint4 tt = *reinterpret_cast<const uint4*>(tok + i0);
+            const uint4 vv = *reinterpret_cast<const uint4*>(val + i0);
+            t[0] = tt.x, t[1] = tt.y, t[2] = tt.z, t[3] = tt.w;
+            v[0] = vv.x, v[1] = vv.y, v[2] = vv.z, v[3] = vv.w;
+        } else {
+#pragma unroll
+            for (int u = 0; u < SCATTER_ITEMS; ++u) {
+                t[u] = i0 + u < n ? tok[i0 + u] : 0xFFFFFFFFu;
+                v[u] = i0 + u < n ? val[i0 + u] : 0u;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < SCATTER_ITEMS; ++u) at[u] = t[u] < U ? atomicAdd(&cursor[t[u]], 1u) : 0xFFFFFFFFu;
+#pragma unroll
+        for (int u = 0; u < SCATTER_ITEMS; ++u)
+            if (at[u] != 0xFFFFFFFFu) out[at[u]] = v[u];
+    }
+}
+
+// Step 2: a warp orders 32 consecutive lists.  Their entries are contiguous;
+// the warp stages them in shared memory, lane k orders list k there by
+// insertion sort (the scatter leaves lists nearly in emission order, since
+// earlier entries mostly take their slots first, so this is close to one pass
+// per list; at most LIST_SHORT^2/2 steps), and the warp writes the range back
+// with coalesced stores.  The gate bounds every list, so 32 lists fit the
+// stage; a larger range (not produced by k_list_scatter under the gate) would
+// be sorted in global memory.
+__global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __restrict__ list_off, uint32_t U,
+                                                           const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                                           const uint32_t* gate) {
+    if (*gate > LIST_SHORT) return;
+    __shared__ uint32_t stage_all[RANK_THREADS / 32][RANK_CAP];
+    const int lane = threadIdx.x & 31;
+    uint32_t* stage = stage_all[threadIdx.x >> 5];
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5 << 5; t0 < U; t0 += (uint64_t)warps * 32) {
+        const uint64_t t = t0 + lane;
+        const uint32_t ls = list_off[t < U ? t : U];
+        const uint32_t le = list_off[t + 1 < U ? t + 1 : U];
+        const uint32_t a = __shfl_sync(FULL, ls, 0);
+        const uint32_t b = __shfl_sync(FULL, le, 31);
+        const uint32_t m = b - a;
+        if (m <= RANK_CAP) {
+            for (uint32_t j0 = 0; j0 < m; j0 += 256) {  // eight loads in flight per lane
+                uint32_t x[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const uint32_t j = j0 + 32u * u + lane;
+                    x[u] = j < m ? in[a + j] : 0u;
+                }
+#pragma unroll
+                for (int u = 0; u < 8; ++u) {
+                    const uint32_t j = j0 + 32u * u + lane;
+                    if (j < m) stage[j] = x[u];
+                }
+            }
+            __syncwarp();
+            const uint32_t lo = ls - a, hi = le - a;
+            for (uint32_t i = lo + 1; i < hi; ++i) {
+                const uint32_t x = stage[i];
+                uint32_t j = i;
+                for (; j > lo; --j) {
+                    const uint32_t y = stage[j - 1];
+                    if (y < x) break;
+                    stage[j] = y;
+                }
+                stage[j] = x;
+            }
+            __syncwarp();
+            for (uint32_t j = lane; j < m; j += 32) out[a + j] = stage[j];
+            __syncwarp();
+        } else {
+            for (uint32_t i = ls; i < le; ++i) out[i] = in[i];
+            for (uint32_t i = ls + 1; i < le; ++i) {
+                const uint32_t x = out[i];
+                uint32_t j = i;
+                for (; j > ls; --j) {
+                    const uint32_t y = out[j - 1];
+                    if (y < x) break;
+                    out[j] = y;
+                }
+                out[j] = x;
+            }
         }
     }
 }
@@ -308,45 +499,56 @@ __global__ void k_iota(uint32_t* out, uint64_t n) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) out[i] = (uint32_t)i;
 }
 
-// Eight lanes per set (four sets per warp): each lane folds its tokens into 2W
-// 32-bit register words, the group XOR-reduces them, and the group's lanes
+// Eight lanes per set (four sets per warp).  The group's 2W 32-bit signature
+// words live in shared memory; every token flips its bit there with one
+// shared-memory XOR (a register fold would cost a compare and select per word
+// per token), four token loads in flight per lane; the group's lanes then
 // store the words (coalesced).  Bit b of the signature is bit b%32 of 32-bit
 // word b/32 (the popcount of a XOR of two signatures does not depend on the
 // bit layout).
+constexpr int BITMAP_THREADS = 256;
+constexpr int BITMAP_UNROLL = 4;
 template <int W>
-__global__ void k_bitmaps(CollView c, uint64_t* out) {
+__global__ void __launch_bounds__(BITMAP_THREADS) k_bitmaps(CollView c, uint64_t* out) {
     constexpr int NW = 2 * W;
+    __shared__ uint32_t sw[BITMAP_THREADS / 8][NW];
     const int lane = threadIdx.x & 31, g = lane & 7;
-    const uint32_t bits = 64u * W;
+    uint32_t* mine = sw[threadIdx.x >> 3];
+    const uint32_t mask = 64u * W - 1u;
     const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
     uint32_t* out32 = reinterpret_cast<uint32_t*>(out);
-    // every lane iterates the same number of times so the shuffles stay converged
+    // every lane iterates the same number of times so the warp barriers match
     const uint32_t rounds = (c.n + groups - 1) / groups;
     uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
     for (uint32_t r = 0; r < rounds; ++r, s += groups) {
-        uint32_t w[NW];
 #pragma unroll
-        for (int i = 0; i < NW; ++i) w[i] = 0;
+        for (int q = g; q < NW; q += 8) mine[q] = 0u;
+        __syncwarp();
         const bool live = s < c.n;
         uint2 m = make_uint2(0, 0);
         if (live) m = c.meta[s];
         const uint32_t* t = c.tokens + m.x;
-        for (uint32_t i = g; i < m.y; i += 8) {
-            const uint32_t b = __ldg(t + i) % bits;
-            const uint32_t word = b >> 5, bit = 1u << (b & 31);
+        for (uint32_t i0 = g; i0 < m.y; i0 += 8 * BITMAP_UNROLL) {
+            uint32_t tok[BITMAP_UNROLL];
 #pragma unroll
-            for (int q = 0; q < NW; ++q) w[q] ^= (word == (uint32_t)q) ? bit : 0u;
+            for (int u = 0; u < BITMAP_UNROLL; ++u) {
+                const uint32_t i = i0 + 8u * u;
+                tok[u] = i < m.y ? __ldg(t + i) : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for (int u = 0; u < BITMAP_UNROLL; ++u) {
+                if (i0 + 8u * u < m.y) {
+                    const uint32_t b = tok[u] & mask;
+                    atomicXor(&mine[b >> 5], 1u << (b & 31));
+                }
+            }
         }
-#pragma unroll
-        for (int q = 0; q < NW; ++q) {
-#pragma unroll
-            for (int o = 4; o > 0; o >>= 1) w[q] ^= __shfl_xor_sync(FULL, w[q], o);
-        }
+        __syncwarp();
         if (live) {
 #pragma unroll
-            for (int q = 0; q < NW; ++q)
-                if ((q & 7) == g) out32[(uint64_t)s * NW + q] = w[q];
+            for (int q = g; q < NW; q += 8) out32[(uint64_t)s * NW + q] = mine[q];
         }
+        __syncwarp();
     }
 }
 
@@ -397,22 +599,23 @@ size_t scan_scratch_words(uint64_t n) {
     return words + 1;
 }
 
-cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s) {
+cudaError_t scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s,
+                           const uint32_t* gate) {
     if (n == 0) return cudaSuccess;
     if (n <= SCAN_TILE) {
         note_launches();
-        k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr);
+        k_tile_scan<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr, gate);
         return cudaGetLastError();
     }
     uint64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;
     uint32_t* sums = scratch;
     note_launches(2);
-    k_tile_reduce<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums);
+    k_tile_reduce<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, n, sums, gate);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    e = scan_exclusive(sums, sums, tiles, scratch + tiles, s);
+    e = scan_exclusive(sums, sums, tiles, scratch + tiles, s, gate);
     if (e != cudaSuccess) return e;
-    k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+    k_tile_scan<<<(unsigned)tiles, SCAN_THREADS, 0, s>>>(in, out, n, sums, gate);
     return cudaGetLastError();
 }
 
@@ -428,8 +631,16 @@ cudaError_t prepare_kernels() {
                                 (int)sizeof(RadixSmem));
 }
 
+namespace {
+__global__ void k_copy_gated(uint32_t* dst, const uint32_t* __restrict__ src, uint64_t n, const uint32_t* gate) {
+    if (gated_off(gate)) return;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) dst[i] = src[i];
+}
+}  // namespace
+
 cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys, uint32_t* alt_vals, uint64_t n,
-                             int key_bits, uint32_t* scratch, cudaStream_t s) {
+                             int key_bits, uint32_t* scratch, cudaStream_t s, bool keep_keys, const uint32_t* gate) {
     if (n <= 1) return cudaSuccess;
     uint32_t tiles = (uint32_t)((n + RADIX_TILE - 1) / RADIX_TILE);
     int passes = (key_bits + RADIX_MAX_BITS - 1) / RADIX_MAX_BITS;
@@ -444,21 +655,28 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
         uint32_t* tile_counts = scratch;
         uint32_t* scan_tmp = scratch + counts;
         note_launches(2);
-        k_radix_upsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, n, shift, mask, tile_counts, tiles);
+        k_radix_upsweep<<<tiles, RADIX_THREADS, 0, s>>>(kin, n, shift, mask, tile_counts, tiles, gate);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        e = scan_exclusive(tile_counts, tile_counts, counts, scan_tmp, s);
+        e = scan_exclusive(tile_counts, tile_counts, counts, scan_tmp, s, gate);
         if (e != cudaSuccess) return e;
-        k_radix_downsweep<<<tiles, RADIX_THREADS, sizeof(RadixSmem), s>>>(kin, vin, n, shift, mask, tile_counts,
-                                                                          tiles, kout, vout);
+        const bool last = p + 1 == passes;
+        k_radix_downsweep<<<tiles, RADIX_THREADS, sizeof(RadixSmem), s>>>(
+            kin, vin, n, shift, mask, tile_counts, tiles, last && !keep_keys ? nullptr : kout, vout, gate);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         uint32_t* t;
         t = kin; kin = kout; kout = t;
         t = vin; vin = vout; vout = t;
     }
-    if (kin != keys) {
-        cudaError_t e = cudaMemcpyAsync(keys, kin, n * 4, cudaMemcpyDeviceToDevice, s);
+    if (vin != vals) {
+        if (gate) {  // the copy back obeys the gate too
+            note_launches(keep_keys ? 2 : 1);
+            if (keep_keys) k_copy_gated<<<grid_for(n, 256), 256, 0, s>>>(keys, kin, n, gate);
+            k_copy_gated<<<grid_for(n, 256), 256, 0, s>>>(vals, vin, n, gate);
+            return cudaGetLastError();
+        }
+        cudaError_t e = keep_keys ? cudaMemcpyAsync(keys, kin, n * 4, cudaMemcpyDeviceToDevice, s) : cudaSuccess;
         if (e != cudaSuccess) return e;
         e = cudaMemcpyAsync(vals, vin, n * 4, cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) return e;
@@ -491,9 +709,33 @@ cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uin
     note_launches();
     CollView v = c;
     v.n = hi;  // the kernel walks ids [lo, hi)
-    k_emit_packed<<<grid_for((uint64_t)(hi - lo) * 32, 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
-                                                                          e_val, counts);
+    k_emit_packed<<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
+                                                                     e_val, counts);  // a warp per 32 sets
     return cudaGetLastError();
+}
+
+cudaError_t index_lists(uint32_t* e_token, uint32_t* e_val, uint64_t n, uint32_t U, uint32_t* counts,
+                        uint32_t* list_off, uint32_t* alt_keys, uint32_t* alt_vals, uint32_t* gate, int key_bits,
+                        uint32_t* scratch, cudaStream_t s) {
+    cudaError_t e = scan_exclusive(counts, list_off, (uint64_t)U + 1, scratch, s);
+    if (e != cudaSuccess) return e;
+    if (n == 0) return cudaSuccess;
+    e = cudaMemsetAsync(gate, 0, 4, s);
+    if (e != cudaSuccess) return e;
+    note_launches(3);
+    k_list_max<<<grid_for(U, 256, 4 * 152), 256, 0, s>>>(counts, U, gate);
+    // short lists: scatter into alt_vals (the counts become the cursors), rank
+    // back into e_val
+    e = cudaMemcpyAsync(counts, list_off, (size_t)U * 4, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    const bool vec = ((reinterpret_cast<uintptr_t>(e_token) | reinterpret_cast<uintptr_t>(e_val)) & 15u) == 0;
+    k_list_scatter<<<grid_for((n + SCATTER_ITEMS - 1) / SCATTER_ITEMS, 256), 256, 0, s>>>(
+        e_token, e_val, n, U, counts, alt_vals, gate, vec);
+    k_list_rank<<<grid_for(U, RANK_THREADS), RANK_THREADS, 0, s>>>(list_off, U, alt_vals, e_val, gate);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    // long lists: the radix passes (each of their kernels checks the gate)
+    return radix_sort_pairs(e_token, e_val, alt_keys, alt_vals, n, key_bits, scratch, s, false, gate);
 }
 
 cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, uint32_t limit, cudaStream_t s) {
@@ -573,13 +815,13 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
 
 cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s) {
     if (c.n == 0) return cudaSuccess;
-    unsigned g = grid_for((uint64_t)c.n * 8, 256);
+    unsigned g = grid_for((uint64_t)c.n * 8, BITMAP_THREADS);
     note_launches();
     switch (words) {
-    case 1: k_bitmaps<1><<<g, 256, 0, s>>>(c, out); break;
-    case 2: k_bitmaps<2><<<g, 256, 0, s>>>(c, out); break;
-    case 4: k_bitmaps<4><<<g, 256, 0, s>>>(c, out); break;
-    case 8: k_bitmaps<8><<<g, 256, 0, s>>>(c, out); break;
+    case 1: k_bitmaps<1><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
+    case 2: k_bitmaps<2><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
+    case 4: k_bitmaps<4><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
+    case 8: k_bitmaps<8><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

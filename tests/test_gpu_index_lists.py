@@ -1,0 +1,65 @@
+"""How the prefix index's lists are built on the GPU.
+
+The lists must hold their entries in set-id order (the join bisects them by
+candidate id).  When every list has at most 64 entries the build fills them
+with one atomic per entry and orders each list with a rank sort inside a warp;
+a longer list sends the whole build through the stable radix passes.  The
+choice is made on the device from the longest list, so both sides of the bound
+are checked here against the oracle, with a token planted in the prefix of
+exactly 64 and 65 sets."""
+import numpy as np
+import pytest
+
+import oracle
+from hyset_gb300 import similarity, synth
+
+pytestmark = pytest.mark.gpu
+
+
+def _longest_list(c, tau):
+    mid = similarity.midprefix_array("jaccard", c.sizes, tau)
+    idx = np.concatenate([c.tokens[s:s + m] for s, m in zip(c.starts, mid)])
+    return int(np.bincount(idx).max())
+
+
+def _plant(c, k, seed):
+    """Token 0 (below every other token, so inside every prefix) added to k
+    random sets; the sets are re-sorted by size (stable)."""
+    rng = np.random.default_rng(seed)
+    sets = [c.tokens[s:s + l].astype(np.uint32) + 1 for s, l in zip(c.starts, c.sizes)]
+    for i in rng.choice(len(sets), size=k, replace=False):
+        sets[i] = np.concatenate([[0], sets[i]]).astype(np.uint32)
+    order = sorted(range(len(sets)), key=lambda i: len(sets[i]))
+    sets = [sets[i] for i in order]
+    sizes = np.array([len(s) for s in sets], np.uint32)
+    starts = np.concatenate([[0], np.cumsum(sizes[:-1], dtype=np.uint64)]).astype(np.uint32)
+    return synth.Collection(np.concatenate(sets).astype(np.uint32), starts, sizes)
+
+
+@pytest.mark.parametrize("k", [64, 65])
+def test_lists_on_both_sides_of_the_bound(ctx, k):
+    c = _plant(synth.generate(synth.C2, n_sets=20000, seed=61), k, seed=k)
+    assert _longest_list(c, 0.8) == k
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.8))
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    for kw in (dict(technique="fgss", probe_major=True, bitmap=0), dict(technique="fgss", probe_major=True,
+                                                                         bitmap=256, verify_mode=2)):
+        r = ctx.self_join(coll, threshold=0.8, **kw)
+        assert r.count == len(exp) and oracle.as_set(r.pairs) == exp, kw
+    # the host-input join builds its index the same way
+    r = ctx.self_join_host(c.tokens, c.sizes, c.starts, threshold=0.8, technique="fgss", probe_major=True,
+                           bitmap=256)
+    assert oracle.as_set(r.pairs) == exp
+
+
+@pytest.mark.parametrize("n,tau", [(10000, 0.5), (200000, 0.6), (200000, 0.8)])
+def test_natural_lists(ctx, n, tau):
+    """Longest lists 63 (atomic + rank path), 141 (radix path) and 25."""
+    c = synth.generate(synth.C2 if n > 10000 else synth.C1, n_sets=n, seed=7)
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, tau))
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    r = ctx.self_join(coll, threshold=tau, technique="fgss", probe_major=True, sort_pairs=True)
+    assert oracle.as_set(r.pairs) == exp
+    p = np.asarray(r.pairs, np.uint64)
+    key = (p[:, 0] << np.uint64(32)) | p[:, 1]
+    assert bool(np.all(key[1:] > key[:-1]))
