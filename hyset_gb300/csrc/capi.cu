@@ -1762,6 +1762,20 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         const int words = (int)(tn.bits / 64);
         DevBuf& bits = C->bitmaps[words];
         if (words) CK(bits.ensure((size_t)n * words * 8 + 8, s));
+        // A collection with the same size profile joined before: its universe
+        // is assumed, so the token histogram is counted as the chunks land and
+        // the checks are read after the join (one synchronisation); a larger
+        // token than assumed means the index is built again and the join re-run.
+        const std::string ukey = coll_signature(C);
+        auto uit = ctx->universe_cache.find(ukey);
+        bool assumed = uit != ctx->universe_cache.end();
+        uint32_t U = assumed ? uit->second : 0;
+        uint32_t* counts = nullptr;
+        if (assumed) {
+            CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
+            counts = ctx->sc->counts.as<uint32_t>();
+            CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+        }
         uint32_t lo = 0;
         for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
             // sets whose tokens end inside the chunks copied so far
@@ -1774,17 +1788,14 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             part.meta += lo;
             part.n = hi - lo;
             CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
-            CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr, s, lo,
-                                   hi));
+            CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s, lo,
+                                   hi, U + 1));
             if (words) CK(generate_bitmaps(part, words, bits.as<uint64_t>() + (size_t)lo * words, s));
             lo = hi;
         }
         if (n_chunks) CK(cudaStreamWaitEvent(s, pipe_event(ctx, n_chunks - 1), 0));  // every copy has landed
         // 5. the index and the join.  The universe (largest token + 1) sizes the
-        //    list offsets; when a collection with the same size profile was
-        //    joined before, its universe is assumed and the checks are read
-        //    after the join (one synchronisation); a different universe means
-        //    the index is built again and the join re-run.
+        //    list offsets: assumed (above), or read with the checks.
         uint32_t* f = ctx->h_flags;
         auto verdict = [&]() -> hyset_status {
             if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
@@ -1793,13 +1804,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
             return HYSET_OK;
         };
-        const std::string ukey = coll_signature(C);
-        auto uit = ctx->universe_cache.find(ukey);
-        bool assumed = uit != ctx->universe_cache.end();
-        uint32_t U = 0;
-        if (assumed) {
-            U = uit->second;
-        } else {
+        if (!assumed) {
             CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
             CK(cudaStreamSynchronize(s));
             const hyset_status vs = verdict();
@@ -1812,11 +1817,13 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
             CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
             CK(ctx->sc->scan.ensure(std::max(scan_words, scan_scratch_words((uint64_t)U + 1)) * 4, s));
-            if (attempt > 0)  // the sort reordered the entries: emit them again
+            if (attempt > 0)  // the list build reordered the entries: emit them again
                 CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr, s));
-            uint32_t* counts = ctx->sc->counts.as<uint32_t>();
-            CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
-            CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
+            counts = ctx->sc->counts.as<uint32_t>();
+            if (!(assumed && attempt == 0)) {  // not counted while the chunks landed
+                CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+                CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
+            }
             CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts,
                            ix.list_off.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(),
                            ctx->sc->gate.as<uint32_t>(), key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));

@@ -83,11 +83,12 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
                                 const uint32_t* len, uint32_t* e_token, uint32_t* e_set,
                                 uint32_t* e_pos, cudaStream_t s);
 // Packed form: e_token[k] = token, e_val[k] = (set << pos_bits) | position, and the
-// token histogram counts[token]++ in the same pass (counts may be nullptr).
-// Sets [lo, hi) only (hi = 0xFFFFFFFF: to the end); ids stay absolute.
+// token histogram counts[token]++ of tokens below `limit` in the same pass
+// (counts may be nullptr).  Sets [lo, hi) only (hi = 0xFFFFFFFF: to the end);
+// ids stay absolute.
 cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
                                 uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s,
-                                uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu);
+                                uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu, uint32_t limit = 0xFFFFFFFFu);
 
 // Token histogram of n entries into counts[limit] (warp-aggregated atomics;
 // tokens >= limit are skipped; the counts are NOT zeroed here).

@@ -289,7 +289,7 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 constexpr int EMIT_ROUNDS = 4;
 __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
-                              uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts) {
+                              uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit) {
     const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t s0 = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; s0 < c.n; s0 += warps * 32u) {
@@ -323,7 +323,7 @@ __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restric
                     e_token[o0 + j] = tok[u];
                     e_val[o0 + j] = val[u];
                     // tokens inside one set are distinct: one atomic per entry
-                    if (counts) atomicAdd(&counts[tok[u]], 1u);
+                    if (counts && tok[u] < limit) atomicAdd(&counts[tok[u]], 1u);
                 }
             }
         }
@@ -703,14 +703,14 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
 
 cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
                                 uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s, uint32_t lo,
-                                uint32_t hi) {
+                                uint32_t hi, uint32_t limit) {
     if (hi == 0xFFFFFFFFu) hi = c.n;
     if (hi <= lo) return cudaSuccess;
     note_launches();
     CollView v = c;
     v.n = hi;  // the kernel walks ids [lo, hi)
     k_emit_packed<<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
-                                                                     e_val, counts);  // a warp per 32 sets
+                                                                     e_val, counts, limit);  // a warp per 32 sets
     return cudaGetLastError();
 }
 
