@@ -18,11 +18,12 @@ void note_launches(unsigned n) { g_launches += n; }
 
 namespace {
 
-// Index lists of at most LIST_SHORT entries are ordered by a rank sort inside
-// one warp (k_list_rank); longer ones go through the radix passes.
+// Index lists of at most LIST_SHORT entries are filled by atomic slots and put
+// back in set order inside one warp (k_list_scatter, k_list_rank); longer
+// ones go through the radix passes.
 constexpr uint32_t LIST_SHORT = 64;
 constexpr int RANK_THREADS = 128;
-constexpr uint32_t RANK_CAP = 2048;  // staged entries per warp: 32 lists of up to 64
+constexpr uint32_t RANK_CAP = 32 * LIST_SHORT;  // staged entries per warp: 32 lists
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
