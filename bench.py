@@ -7,14 +7,16 @@ clamped to [10, 2000], universe 1,000,000, Zipf s=0.9 tokens drawn without
 replacement, 5% planted near-duplicates with 5-15% token edits, tokens renumbered
 by ascending frequency, collection sorted by size (112M tokens, 449 MB).
 
-A step is one whole self-join: prefix-index build (histogram, scan, radix sort),
-signatures, and the persistent filter+verify launch, with the collection already
+A step is one whole self-join: prefix-index build (entries + token histogram,
+scan, list build), signatures, and the persistent filter+verify launch, with the collection already
 resident in HBM (`value`), or through the public API from pinned host memory with
 the pairs copied back (`e2e`).  Between timed steps a 512 MB buffer is written to
 flush the 129 MB L2.  The reference-shaped block-pair path (one launch per block
 pair, synchronous copies, as the reference's handlers do) is timed beside it as
 the plain baseline.  --impl reference times the reference algorithm on the host
-cores (the CPU oracle, cpu_multi semantics, all threads).
+cores (the CPU oracle, cpu_multi semantics, all threads).  --sim cosine (or dice)
+runs the same workload under that similarity (no block-pair leg: the reference's
+handlers are Jaccard only).
 """
 from __future__ import annotations
 
@@ -41,6 +43,10 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def workload_name(sim):
+    return WORKLOAD if sim == "jaccard" else WORKLOAD.replace("Jaccard 0.8", f"{sim} 0.8")
 
 
 def make_workload(n_sets=None):
@@ -130,14 +136,14 @@ def algorithmic_bytes(st, count, words, n_probes):
             + 8 * count)
 
 
-def cpu_baseline(c, threads, sample_note):
+def cpu_baseline(c, threads, sample_note, sim="jaccard"):
     import oracle
     t0 = time.perf_counter()
     if threads == 1:
-        pairs = oracle.join(c.tokens, c.starts, c.sizes, THRESHOLD)
+        pairs = oracle.join(c.tokens, c.starts, c.sizes, THRESHOLD, sim=sim)
         idx_s, join_s = oracle.last_timing()
     else:
-        pairs = oracle.join_multi(c.tokens, c.starts, c.sizes, THRESHOLD, threads)
+        pairs = oracle.join_multi(c.tokens, c.starts, c.sizes, THRESHOLD, threads, sim=sim)
         idx_s, join_s = oracle.last_timing(multi=True)
     wall = time.perf_counter() - t0
     return len(pairs), join_s, idx_s, wall
@@ -151,10 +157,10 @@ def run_reference(args, ws, rank):
     c = make_workload(args.sets)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_baseline(c, threads, "")
+        cpu_baseline(c, threads, "", args.sim)
     times, counts = [], []
     for _ in range(args.steps):
-        n, join_s, idx_s, wall = cpu_baseline(c, threads, "")
+        n, join_s, idx_s, wall = cpu_baseline(c, threads, "", args.sim)
         times.append(join_s + idx_s)
         counts.append(n)
     ms = 1000.0 * statistics.mean(times)
@@ -162,7 +168,8 @@ def run_reference(args, ws, rank):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "strong", "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
-            "config": {"workload": WORKLOAD, "threshold": THRESHOLD, "result_pairs": counts[0]},
+            "config": {"workload": workload_name(args.sim), "threshold": THRESHOLD, "sim": args.sim,
+                       "result_pairs": counts[0]},
             "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
                              "sample": "whole workload each step (index build + join), oracle restatement of "
                                        "host::allpairs with the cpu_multi sqrt split"},
@@ -194,7 +201,7 @@ def run_ours(args, ws, rank, local):
     ctx = hs.Context(local)
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    kw = dict(threshold=THRESHOLD, technique=args.technique, bitmap=args.bitmap, device_pairs=True,
+    kw = dict(threshold=THRESHOLD, sim=args.sim, technique=args.technique, bitmap=args.bitmap, device_pairs=True,
               probe_range=(p_lo, p_hi), probe_major=args.probe_major, verify_mode=args.vmode)
 
     def barrier():
@@ -270,7 +277,7 @@ def run_ours(args, ws, rank, local):
         # the plain reference-shaped path: block pairs of 10,000 sets, one launch each
         hc = hs.from_arrays(c.tokens, c.sizes, 10000, THRESHOLD)
         plain = []
-        for i in range(0 if args.no_plain else 2):
+        for i in range(0 if args.no_plain or args.sim != "jaccard" else 2):
             h = FgssHandler(ctx, hc, coll, 10000, False, THRESHOLD)
             ph = hs.PairsHandler()
             h.set_output_handler(ph)
@@ -289,14 +296,14 @@ def run_ours(args, ws, rank, local):
         traffic = ncu_traffic()
         cpu = {"value": None}
         if not args.no_cpu:
-            n_cpu, join_s, idx_s, wall = cpu_baseline(c, 1, "")
+            n_cpu, join_s, idx_s, wall = cpu_baseline(c, 1, "", args.sim)
             cpu = {"value": n_cpu / (join_s + idx_s), "unit": "pairs/s", "cores": 1, "kind": "port",
                    "sample": f"whole workload once: index {idx_s:.2f} s + join {join_s:.2f} s on 1 core "
                              f"(oracle restatement of host::allpairs)"}
         out = {"metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "strong",
                "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
-               "config": {"workload": WORKLOAD, "threshold": THRESHOLD, "sim": "jaccard",
+               "config": {"workload": workload_name(args.sim), "threshold": THRESHOLD, "sim": args.sim,
                           "technique": r.technique, "bitmap_bits": r.bitmap_bits, "result_pairs": total_pairs,
                           "parallelism": f"probe shards x{ws}" if ws > 1 else "single GPU",
                           "l2": "512 MB buffer written between timed steps; tokens 449 MB > L2",
@@ -552,6 +559,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--technique", default="auto")
+    ap.add_argument("--sim", default="jaccard", choices=["jaccard", "cosine", "dice"])
     ap.add_argument("--bitmap", type=int, default=0, help="signature bits; 0 = the library's autotuner")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the block-pair baseline leg")

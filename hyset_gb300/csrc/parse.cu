@@ -63,6 +63,9 @@ __device__ __forceinline__ uint32_t byte_at(const uint8_t* t, uint64_t n, int64_
 }
 
 // The chunk's four words (bytes past the text read as '\n') and its masks.
+// Called by all lanes of a warp for consecutive chunks: the bytes just before
+// and after the chunk come from the neighbouring lanes (the warp's end lanes
+// read them from memory).
 __device__ __forceinline__ void load_chunk(const uint8_t* t, uint64_t n, uint64_t base, uint32_t (&w)[4], Masks& m) {
     if (base + PARSE_BYTES <= n) {
         const uint4 v = *reinterpret_cast<const uint4*>(t + base);  // base is a multiple of 16
@@ -88,7 +91,10 @@ __device__ __forceinline__ void load_chunk(const uint8_t* t, uint64_t n, uint64_
         m.cr |= byte_eq(w[q], '\r') << (4 * q);
     }
     m.valid = base >= n ? 0u : (n - base >= PARSE_BYTES ? 0xFFFFu : (1u << (n - base)) - 1u);
-    const uint32_t before = byte_at(t, n, (int64_t)base - 1), after = byte_at(t, n, (int64_t)(base + PARSE_BYTES));
+    const int lane = threadIdx.x & 31;
+    const uint32_t up = __shfl_up_sync(FULL, w[3], 1), down = __shfl_down_sync(FULL, w[0], 1);
+    const uint32_t before = lane > 0 ? up >> 24 : byte_at(t, n, (int64_t)base - 1);
+    const uint32_t after = lane < 31 ? down & 0xFFu : byte_at(t, n, (int64_t)(base + PARSE_BYTES));
     m.prev_nl = ((m.nl << 1) | (before == '\n' ? 1u : 0u)) & 0xFFFFu;
     m.prev_sp = ((m.space << 1) | (before == ' ' ? 1u : 0u)) & 0xFFFFu;
     m.next_digit = (m.digit >> 1) | ((after - '0' < 10u) ? 0x8000u : 0u);
@@ -149,14 +155,6 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_count(const uint8_t* __
     }
 }
 
-// Eight bytes of the 16-byte chunk (lo = bytes 0..7, hi = 8..15) from byte s,
-// byte s in the low byte (zeros past the chunk).
-__device__ __forceinline__ uint64_t bytes_from(uint64_t lo, uint64_t hi, uint32_t s) {
-    if (s == 0) return lo;
-    if (s < 8) return (lo >> (8 * s)) | (hi << (64 - 8 * s));
-    return hi >> (8 * (s - 8));
-}
-
 // Value of len (1..8) ASCII digits in the low bytes of x, the first digit in
 // the lowest byte: the digits are moved to the top bytes over a '0' fill, then
 // combined pairwise, four-wise and eight-wise with three multiplies (the
@@ -169,31 +167,21 @@ __device__ __forceinline__ uint32_t digits8(uint64_t x, uint32_t len) {
     return (uint32_t)(((y & 0x0000FFFF0000FFFFull) * 42949672960001ull) >> 32);
 }
 
-// Value of the digit run of len (1..10) bytes starting at byte s.
-__device__ __forceinline__ unsigned long long run_value(uint64_t lo, uint64_t hi, uint32_t s, uint32_t len) {
-    if (len <= 8) return digits8(bytes_from(lo, hi, s), len);
-    return (unsigned long long)digits8(bytes_from(lo, hi, s), len - 8) * 100000000ull +
-           digits8(bytes_from(lo, hi, s + len - 8), 8);
+// Eight bytes of the staged tile from byte s (the tile is followed by eight
+// bytes of '\n' so that reads near its end stay inside the stage).
+__device__ __forceinline__ uint64_t stage_bytes(const uint64_t* st8, uint32_t s) {
+    const uint32_t q = s >> 3, r = (s & 7u) * 8u;
+    const uint64_t a = st8[q];
+    return r ? (a >> r) | (st8[q + 1] << (64u - r)) : a;
 }
 
-// The digit run that leaves the chunk on the right (nd = 0: none; nd = 11:
-// more than ten digits, an error wherever the number ends).
-__device__ __forceinline__ void right_run(uint32_t digit, uint64_t lo, uint64_t hi, unsigned long long& acc,
-                                          uint32_t& nd) {
-    acc = 0;
-    nd = 0;
-    if (!(digit & 0x8000u)) return;
-    const uint32_t nond = ~digit & 0xFFFFu;
-    const uint32_t s = nond ? 32u - __clz(nond) : 0u;  // one past the last non-digit
-    const uint32_t len = PARSE_BYTES - s;
-    if (s == 0 || len > 10) {
-        nd = 11;
-        return;
-    }
-    acc = run_value(lo, hi, s, len);
-    nd = len;
-}
-
+// Pass 2, one block per 4 KiB tile.  Every thread classifies its 16 bytes and
+// stages them with their digit mask in shared memory; a block scan places the
+// tile's tokens and lines; the byte offset of every token's last digit is
+// recorded; then the tile's tokens are parsed round-robin by all threads (no
+// thread waits on a neighbour with more tokens) from the staged bytes, eight
+// digits at a time, and stored contiguously.  A number that begins in the
+// previous tile (at most one per tile) is read back from global memory.
 __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __restrict__ t, uint64_t n,
                                                               const uint32_t* __restrict__ tile_tok0,
                                                               const uint32_t* __restrict__ tile_line0,
@@ -201,15 +189,21 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
                                                               uint32_t* __restrict__ line_tok0, uint32_t* flags,
                                                               unsigned long long* first_bad) {
     __shared__ uint32_t wsum[2][PARSE_THREADS / 32];
-    __shared__ unsigned long long tail_acc[PARSE_THREADS / 32];
-    __shared__ uint32_t tail_nd[PARSE_THREADS / 32];
-    __shared__ uint32_t s_tok[PARSE_MAX_ITEMS], s_line[PARSE_MAX_ITEMS];
+    __shared__ uint64_t s_text[PARSE_TILE / 8 + 1];
+    __shared__ uint32_t s_dig[PARSE_THREADS];
+    __shared__ uint16_t s_end[PARSE_MAX_ITEMS];
+    __shared__ uint32_t s_line[PARSE_MAX_ITEMS];
     const uint64_t tile = blockIdx.x;
-    const uint64_t base = tile * PARSE_TILE + (uint64_t)threadIdx.x * PARSE_BYTES;
+    const uint64_t tile_base = tile * PARSE_TILE;
+    const uint64_t base = tile_base + (uint64_t)threadIdx.x * PARSE_BYTES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t w[4];
     Masks m;
     load_chunk(t, n, base, w, m);
+    s_text[2 * threadIdx.x] = w[0] | (uint64_t)w[1] << 32;
+    s_text[2 * threadIdx.x + 1] = w[2] | (uint64_t)w[3] << 32;
+    if (threadIdx.x == 0) s_text[PARSE_TILE / 8] = 0x0A0A0A0A0A0A0A0Aull;
+    s_dig[threadIdx.x] = m.digit;
     const uint32_t ends = token_ends(m), starts = line_starts(m);
     const uint32_t toks = __popc(ends), lines = __popc(starts);
     // block-wide exclusive scan of the token and line counts
@@ -225,82 +219,58 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
         lw += wsum[1][q];
     }
     const uint32_t tok_first = tile_tok0[tile], line_first = tile_line0[tile];
-    const uint32_t tok0 = tw + ti - toks;  // within the tile
+    uint32_t tok = tw + ti - toks;  // within the tile
     uint32_t line = lw + li - lines;
     // line starts: the index of the line's first token = tokens ending before it
-    uint32_t sm = starts;
-    while (sm) {
+    for (uint32_t sm = starts; sm; sm &= sm - 1) {
         const int k = __ffs(sm) - 1;
-        sm &= sm - 1;
-        s_line[line++] = tok_first + tok0 + __popc(ends & ((1u << k) - 1u));
+        s_line[line++] = tok_first + tok + __popc(ends & ((1u << k) - 1u));
     }
-    // every token ending here: its run of digits [s, k] parsed eight digits at a
-    // time; a run from byte 0 may continue a number of the previous chunk and
-    // waits for the carry (lead_len digits, value lead)
-    const uint64_t lo = w[0] | (uint64_t)w[1] << 32, hi = w[2] | (uint64_t)w[3] << 32;
-    unsigned long long lead = 0;
-    uint32_t lead_len = 0, tok = tok0, bad = 0;
-    int bad_k = PARSE_BYTES;
-    uint32_t e = ends;
-    while (e) {
-        const int k = __ffs(e) - 1;
-        e &= e - 1;
-        const uint32_t below = ~m.digit & ((1u << k) - 1u);
-        const uint32_t st = below ? 32u - __clz(below) : 0u;
-        const uint32_t len = (uint32_t)k - st + 1u;
-        unsigned long long v = 0;
-        if (len <= 10) v = run_value(lo, hi, st, len);
-        if (st == 0 && (m.digit & 1u)) {
-            lead = v;
-            lead_len = len;
-        } else if (len > 10 || v > 0xFFFFFFFFull) {
-            bad = PARSE_E_RANGE;
-            bad_k = min(bad_k, k);
-        }
-        s_tok[tok++] = (uint32_t)v;
-    }
-    // carry in: the previous chunk's right run (lane - 1; the previous warp's last
-    // lane through shared memory; the previous tile's last chunk from memory)
-    unsigned long long racc;
-    uint32_t rnd;
-    right_run(m.digit, lo, hi, racc, rnd);
-    unsigned long long cacc = __shfl_up_sync(FULL, racc, 1);
-    uint32_t cnd = __shfl_up_sync(FULL, rnd, 1);
-    if (lane == 31) {
-        tail_acc[warp] = racc;
-        tail_nd[warp] = rnd;
-    }
-    __syncthreads();
-    if (lane == 0) {
-        if (warp > 0) {
-            cacc = tail_acc[warp - 1];
-            cnd = tail_nd[warp - 1];
-        } else {
-            cacc = 0;
-            cnd = 0;
-            if (base >= PARSE_BYTES) {
-                uint32_t pw[4];
-                Masks pm;
-                load_chunk(t, n, base - PARSE_BYTES, pw, pm);
-                right_run(pm.digit, pw[0] | (uint64_t)pw[1] << 32, pw[2] | (uint64_t)pw[3] << 32, cacc, cnd);
-            }
-        }
-    }
-    if (lead_len) {  // the first token ends here with lead_len digits from byte 0
-        unsigned long long p10 = 1;
-        for (uint32_t q = 0; q < lead_len && q < 11; ++q) p10 *= 10u;
-        const unsigned long long v = cacc * p10 + lead;
-        const uint32_t digits = cnd + lead_len;
-        if (digits > 10 || v > 0xFFFFFFFFull) {
-            bad = PARSE_E_RANGE;
-            bad_k = 0;
-        }
-        s_tok[tok0] = (uint32_t)v;
-    }
-    record_error(bad, base + (uint64_t)bad_k, flags, first_bad);
+    for (uint32_t e = ends; e; e &= e - 1) s_end[tok++] = (uint16_t)(threadIdx.x * PARSE_BYTES + __ffs(e) - 1);
     __syncthreads();
     const uint32_t n_tok = tile_tok0[tile + 1] - tok_first, n_line = tile_line0[tile + 1] - line_first;
-    for (uint32_t i = threadIdx.x; i < n_tok; i += PARSE_THREADS) tokens[tok_first + i] = s_tok[i];
+    uint32_t bad = 0;
+    uint64_t bad_at = ~0ull;
+    for (uint32_t i = threadIdx.x; i < n_tok; i += PARSE_THREADS) {
+        const uint32_t e = s_end[i], c = e >> 4, k = e & 15u;
+        // first digit of the run: after the last non-digit below byte e
+        uint32_t st;
+        const uint32_t below = ~s_dig[c] & ((1u << k) - 1u);
+        bool from_prev_tile = false;
+        if (below) {
+            st = c * PARSE_BYTES + 32u - __clz(below);
+        } else if (c > 0) {
+            const uint32_t nondig = ~s_dig[c - 1] & 0xFFFFu;
+            st = nondig ? (c - 1) * PARSE_BYTES + 32u - __clz(nondig) : 0u;
+            from_prev_tile = !nondig;  // sixteen digits and more: too long, reported below
+        } else {
+            st = 0;
+            from_prev_tile = true;
+        }
+        uint32_t len = e - st + 1;
+        unsigned long long v = 0;
+        if (from_prev_tile && c == 0 && tile_base > 0) {
+            // the number may begin in the previous tile: its digits from memory
+            uint32_t lead = 0;
+            while (lead <= 10 && lead < tile_base && (uint32_t)t[tile_base - 1 - lead] - '0' < 10u) ++lead;
+            len += lead;
+            if (len <= 10)
+                for (uint64_t q = tile_base - lead; q <= tile_base + e; ++q) v = v * 10u + (t[q] - '0');
+        } else if (from_prev_tile && c > 0) {
+            len = 11;  // a run of more than sixteen digits
+        } else if (len <= 8) {
+            v = digits8(stage_bytes(s_text, st), len);
+        } else if (len <= 10) {
+            v = (unsigned long long)digits8(stage_bytes(s_text, st), len - 8) * 100000000ull +
+                digits8(stage_bytes(s_text, st + len - 8), 8);
+        }
+        if (len > 10 || v > 0xFFFFFFFFull) {
+            bad = PARSE_E_RANGE;
+            if (tile_base + e < bad_at) bad_at = tile_base + e;
+        }
+        tokens[tok_first + i] = (uint32_t)v;
+    }
+    record_error(bad, bad_at, flags, first_bad);
     for (uint32_t i = threadIdx.x; i < n_line; i += PARSE_THREADS) line_tok0[line_first + i] = s_line[i];
 }
 

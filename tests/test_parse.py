@@ -163,3 +163,48 @@ def test_gpu_parse_from_device_memory(ctx):
     coll2 = ctx.parse((d2.data_ptr() + 1, d2.numel() - 1))
     gt2, _, _ = coll2.download()
     np.testing.assert_array_equal(gt2, tokens)
+
+
+def _at_tile_edge(number: bytes, offset: int) -> bytes:
+    """A valid collection whose one-token line `number` starts `offset` bytes
+    before the first 4 KiB tile boundary (one-token lines before it, a
+    two-token line after it: sizes stay sorted)."""
+    p = 4096 - offset
+    head = b"1\n" * (p // 2) if p % 2 == 0 else b"11\n" + b"1\n" * ((p - 3) // 2)
+    assert len(head) == p
+    return head + number + b"\n7 8\n"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("offset", range(1, 12))
+def test_gpu_parse_numbers_across_the_tile_edge(ctx, offset):
+    """A ten-digit number split by the tile boundary at every offset; an
+    eleven-digit one and one of 2^32 must be rejected wherever they are cut."""
+    import hyset_gb300 as hs
+    text = _at_tile_edge(b"4294967294", offset)  # 0xFFFFFFFF is reserved
+    t, z, _ = read_text(text)
+    gt, _, gz = ctx.parse(text).download()
+    np.testing.assert_array_equal(gt, t)
+    np.testing.assert_array_equal(gz, z)
+    assert 4294967294 in gt.tolist()
+    with pytest.raises(hs.HysetError, match="parse error at byte"):
+        ctx.parse(_at_tile_edge(b"12345678901", offset))
+    with pytest.raises(hs.HysetError, match="parse error at byte"):
+        ctx.parse(_at_tile_edge(b"4294967296", offset))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("digits", [9, 10, 11, 16, 17, 40])
+def test_gpu_parse_digit_runs_across_chunks(ctx, digits):
+    """Runs of 9 to 40 digits placed across the 16-byte chunk boundaries of a
+    tile: up to ten digits parse (1111111111 is below 2^32), longer runs are
+    rejected."""
+    import hyset_gb300 as hs
+    for lead in range(0, 17, 3):
+        text = b"1\n" * lead + b"1" * digits + b"\n3 4\n"
+        if digits <= 10:
+            t, _, _ = read_text(text)
+            np.testing.assert_array_equal(ctx.parse(text).download()[0], t)
+        else:
+            with pytest.raises(hs.HysetError, match="parse error at byte"):
+                ctx.parse(text)
