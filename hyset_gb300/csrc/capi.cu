@@ -1467,32 +1467,17 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
         d_text = staged.as<uint8_t>();
     }
     const uint64_t tiles = parse_tiles(n_bytes);
-    CK(counts.ensure((2 * tiles + 2) * 4, s));
+    CK(counts.ensure((2 * tiles + 2) * 4 + (2 * n_chunks + 2) * 4, s));
     CK(err.ensure(16, s));
     uint32_t* tile_toks = counts.as<uint32_t>();
     uint32_t* tile_lines = tile_toks + tiles + 1;
+    uint32_t* carry = tile_lines + tiles + 1;  // per chunk: tokens and lines before it
     uint32_t* flags = err.as<uint32_t>();
     unsigned long long* first_bad = reinterpret_cast<unsigned long long*>(err.as<uint8_t>() + 8);
     CK(cudaMemsetAsync(flags, 0, 8, s));
     CK(cudaMemsetAsync(first_bad, 0xFF, 8, s));
-    CK(cudaMemsetAsync(tile_toks, 0, (2 * tiles + 2) * 4, s));
-    if (n_chunks) {
-        const uint64_t per = PARSE_CHUNK / 4096;  // tiles per chunk
-        for (uint64_t k = 0; k < n_chunks; ++k) {
-            CK(cudaStreamWaitEvent(s, pipe_event(ctx, std::min(k + 1, n_chunks - 1)), 0));
-            CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s, k * per, (k + 1) * per));
-        }
-    } else {
-        CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s));
-    }
-    CK(ctx->sc->scan.ensure(scan_scratch_words(tiles + 1) * 4, s));
-    CK(scan_exclusive(tile_toks, tile_toks, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
-    CK(scan_exclusive(tile_lines, tile_lines, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+    CK(cudaMemsetAsync(tile_toks, 0, (2 * tiles + 2) * 4 + (2 * n_chunks + 2) * 4, s));
     uint32_t* h = ctx->h_flags + 8;  // [0] flags, [2..3] first bad offset, [4] tokens, [5] lines
-    CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h + 4, tile_toks + tiles, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaMemcpyAsync(h + 5, tile_lines + tiles, 4, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
     auto parse_error = [&](uint32_t f, unsigned long long at) {
         char msg[160];
         const char* what = (f & PARSE_E_CHAR) ? "unexpected byte"
@@ -1502,17 +1487,77 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
         std::snprintf(msg, sizeof msg, "parse error at byte %llu: %s", at, what);
         return fail(ctx, HYSET_E_INVALID, msg);
     };
-    if (h[0]) return parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
-    const uint32_t n_tokens = h[4], n_lines = h[5];
     auto c = std::make_unique<hyset_coll>();
     c->ctx = ctx;
-    c->n = n_lines;
-    c->n_tokens = n_tokens;
-    CK(c->tokens.ensure((size_t)n_tokens * 4 + 4, s));
-    CK(c->starts.ensure((size_t)n_lines * 4 + 4, s));
-    CK(c->sizes.ensure((size_t)n_lines * 4 + 4, s));
-    CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(), flags,
-                  first_bad, s));
+    struct CollGuard {  // the collection's buffers go back on every early return
+        hyset_ctx* ctx;
+        std::unique_ptr<hyset_coll>& c;
+        ~CollGuard() {
+            if (c) hyset_collection_free(ctx, c.release());
+        }
+    } cguard{ctx, c};
+    uint32_t n_tokens = 0, n_lines = 0;
+    if (n_chunks) {
+        // each chunk is counted, scanned on top of the previous chunks' totals
+        // and emitted as soon as it and the next chunk have landed, so the
+        // whole parse overlaps the copy.  The output is sized from the first
+        // chunk's density (one wait); a text denser further on overflows that
+        // estimate and is emitted again at its exact size.
+        const uint64_t per = PARSE_CHUNK / 4096;  // tiles per chunk
+        uint32_t tok_cap = 0, line_cap = 0;
+        for (uint64_t k = 0; k < n_chunks; ++k) {
+            CK(cudaStreamWaitEvent(s, pipe_event(ctx, std::min(k + 1, n_chunks - 1)), 0));
+            CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s, k * per, (k + 1) * per));
+            CK(parse_chunk_scan(tile_toks, tile_lines, k * per, std::min(tiles, (k + 1) * per), carry, k, s));
+            if (k == 0) {
+                CK(cudaMemcpyAsync(h + 4, carry + 2, 8, cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                const double scale = (double)n_bytes / (double)std::min<uint64_t>(n_bytes, PARSE_CHUNK);
+                const double bound = (double)(n_bytes / 2 + 2);  // a token or a line takes two bytes
+                tok_cap = (uint32_t)std::min({bound, 1.25 * scale * h[4] + 4096.0, 4294967295.0});
+                line_cap = (uint32_t)std::min({bound, 1.25 * scale * h[5] + 4096.0, 4294967295.0});
+                CK(c->tokens.ensure((size_t)tok_cap * 4 + 4, s));
+                CK(c->starts.ensure((size_t)line_cap * 4 + 4, s));
+            }
+            CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(),
+                          flags, first_bad, s, k * per, (k + 1) * per, tok_cap, line_cap));
+        }
+        CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 4, carry + 2 * n_chunks, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h[0] & ~PARSE_E_CAPACITY) return parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        n_tokens = h[4];
+        n_lines = h[5];
+        if (h[0] & PARSE_E_CAPACITY) {  // the estimate was short: every tile again, exact sizes
+            CK(c->tokens.ensure((size_t)n_tokens * 4 + 4, s));
+            CK(c->starts.ensure((size_t)n_lines * 4 + 4, s));
+            CK(cudaMemsetAsync(flags, 0, 4, s));
+            CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(),
+                          flags, first_bad, s));
+        }
+        c->n = n_lines;
+        c->n_tokens = n_tokens;
+        CK(c->sizes.ensure((size_t)n_lines * 4 + 4, s));
+    } else {
+        CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s));
+        CK(ctx->sc->scan.ensure(scan_scratch_words(tiles + 1) * 4, s));
+        CK(scan_exclusive(tile_toks, tile_toks, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+        CK(scan_exclusive(tile_lines, tile_lines, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+        CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 4, tile_toks + tiles, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 5, tile_lines + tiles, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h[0]) return parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        n_tokens = h[4];
+        n_lines = h[5];
+        c->n = n_lines;
+        c->n_tokens = n_tokens;
+        CK(c->tokens.ensure((size_t)n_tokens * 4 + 4, s));
+        CK(c->starts.ensure((size_t)n_lines * 4 + 4, s));
+        CK(c->sizes.ensure((size_t)n_lines * 4 + 4, s));
+        CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(),
+                      flags, first_bad, s));
+    }
     CK(parse_line_sizes(c->starts.as<uint32_t>(), n_lines, n_tokens, c->starts.as<uint32_t>(),
                         c->sizes.as<uint32_t>(), s));
     CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));

@@ -25,6 +25,7 @@ constexpr uint32_t PARSE_E_CHAR = 1;        // a byte other than digit, ' ', '\r
 constexpr uint32_t PARSE_E_EMPTY_ITEM = 2;  // two spaces, a leading space, or a space before '\r'
 constexpr uint32_t PARSE_E_LINE_END = 4;    // '\r' not followed by '\n', or a line of only "\r"
 constexpr uint32_t PARSE_E_RANGE = 8;       // a number of more than 10 digits or >= 2^32
+constexpr uint32_t PARSE_E_CAPACITY = 16;   // (not an input error) a token or line past the output capacity
 uint64_t parse_tiles(uint64_t n_bytes);
 // Per 4 KiB tile: token starts and line starts; flags / first_bad (byte offset,
 // atomicMin) record errors.
@@ -34,10 +35,19 @@ cudaError_t parse_count(const uint8_t* text, uint64_t n_bytes, uint32_t* tile_to
                         uint32_t* flags, unsigned long long* first_bad, cudaStream_t s, uint64_t tile_lo = 0,
                         uint64_t tile_hi = ~0ull);
 // tile_tok0 / tile_line0: exclusive scans of the tile counts.  Writes every
-// token and line_tok0[line] = index of the line's first token.
+// token and line_tok0[line] = index of the line's first token, for tiles
+// [tile_lo, tile_hi) (default: all); indexes at or past tok_cap / line_cap
+// are not written and set PARSE_E_CAPACITY.
 cudaError_t parse_emit(const uint8_t* text, uint64_t n_bytes, const uint32_t* tile_tok0, const uint32_t* tile_line0,
                        uint32_t* tokens, uint32_t* line_tok0, uint32_t* flags, unsigned long long* first_bad,
-                       cudaStream_t s);
+                       cudaStream_t s, uint64_t tile_lo = 0, uint64_t tile_hi = ~0ull, uint32_t tok_cap = ~0u,
+                       uint32_t line_cap = ~0u);
+// In place: exclusive scans of the token and line counts of tiles [tile_lo,
+// tile_hi) (at most 65,536 tiles), offset by carry[2k], carry[2k+1] (tokens,
+// lines before the range); carry[2k+2], carry[2k+3] get the totals after it.
+// One block: for chunks of a text scanned as they arrive.
+cudaError_t parse_chunk_scan(uint32_t* tile_toks, uint32_t* tile_lines, uint64_t tile_lo, uint64_t tile_hi,
+                             uint32_t* carry, uint64_t k, cudaStream_t s);
 // starts[i] = line_tok0[i], sizes[i] = next line's first token - line_tok0[i].
 cudaError_t parse_line_sizes(const uint32_t* line_tok0, uint32_t n_lines, uint32_t n_tokens, uint32_t* starts,
                              uint32_t* sizes, cudaStream_t s);

@@ -183,17 +183,18 @@ __device__ __forceinline__ uint64_t stage_bytes(const uint64_t* st8, uint32_t s)
 // digits at a time, and stored contiguously.  A number that begins in the
 // previous tile (at most one per tile) is read back from global memory.
 __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __restrict__ t, uint64_t n,
-                                                              const uint32_t* __restrict__ tile_tok0,
+                                                              uint64_t tile0, const uint32_t* __restrict__ tile_tok0,
                                                               const uint32_t* __restrict__ tile_line0,
                                                               uint32_t* __restrict__ tokens,
-                                                              uint32_t* __restrict__ line_tok0, uint32_t* flags,
+                                                              uint32_t* __restrict__ line_tok0, uint32_t tok_cap,
+                                                              uint32_t line_cap, uint32_t* flags,
                                                               unsigned long long* first_bad) {
     __shared__ uint32_t wsum[2][PARSE_THREADS / 32];
     __shared__ uint64_t s_text[PARSE_TILE / 8 + 1];
     __shared__ uint32_t s_dig[PARSE_THREADS];
     __shared__ uint16_t s_end[PARSE_MAX_ITEMS];
     __shared__ uint32_t s_line[PARSE_MAX_ITEMS];
-    const uint64_t tile = blockIdx.x;
+    const uint64_t tile = tile0 + blockIdx.x;
     const uint64_t tile_base = tile * PARSE_TILE;
     const uint64_t base = tile_base + (uint64_t)threadIdx.x * PARSE_BYTES;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -213,10 +214,14 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
         wsum[1][warp] = li;
     }
     __syncthreads();
-    uint32_t tw = 0, lw = 0;
-    for (int q = 0; q < warp; ++q) {
-        tw += wsum[0][q];
-        lw += wsum[1][q];
+    uint32_t tw = 0, lw = 0, n_tok = 0, n_line = 0;
+    for (int q = 0; q < PARSE_THREADS / 32; ++q) {
+        if (q < warp) {
+            tw += wsum[0][q];
+            lw += wsum[1][q];
+        }
+        n_tok += wsum[0][q];
+        n_line += wsum[1][q];
     }
     const uint32_t tok_first = tile_tok0[tile], line_first = tile_line0[tile];
     uint32_t tok = tw + ti - toks;  // within the tile
@@ -228,7 +233,6 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
     }
     for (uint32_t e = ends; e; e &= e - 1) s_end[tok++] = (uint16_t)(threadIdx.x * PARSE_BYTES + __ffs(e) - 1);
     __syncthreads();
-    const uint32_t n_tok = tile_tok0[tile + 1] - tok_first, n_line = tile_line0[tile + 1] - line_first;
     uint32_t bad = 0;
     uint64_t bad_at = ~0ull;
     for (uint32_t i = threadIdx.x; i < n_tok; i += PARSE_THREADS) {
@@ -268,10 +272,55 @@ __global__ void __launch_bounds__(PARSE_THREADS) k_parse_emit(const uint8_t* __r
             bad = PARSE_E_RANGE;
             if (tile_base + e < bad_at) bad_at = tile_base + e;
         }
-        tokens[tok_first + i] = (uint32_t)v;
+        if (tok_first + i < tok_cap) tokens[tok_first + i] = (uint32_t)v;
     }
     record_error(bad, bad_at, flags, first_bad);
-    for (uint32_t i = threadIdx.x; i < n_line; i += PARSE_THREADS) line_tok0[line_first + i] = s_line[i];
+    for (uint32_t i = threadIdx.x; i < n_line; i += PARSE_THREADS)
+        if (line_first + i < line_cap) line_tok0[line_first + i] = s_line[i];
+    if (threadIdx.x == 0 && ((uint64_t)tok_first + n_tok > tok_cap || (uint64_t)line_first + n_line > line_cap))
+        atomicOr(flags, PARSE_E_CAPACITY);
+}
+
+// One block scans the token and line counts of up to 65,536 tiles (a chunk of
+// the text) in place, on top of the totals carried from the previous chunks.
+constexpr int CHUNK_SCAN_THREADS = 1024;
+__global__ void __launch_bounds__(CHUNK_SCAN_THREADS) k_parse_chunk_scan(uint32_t* tile_toks, uint32_t* tile_lines,
+                                                                         uint32_t n, uint32_t* carry, uint32_t k) {
+    __shared__ uint32_t ws[2][CHUNK_SCAN_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t per = (n + CHUNK_SCAN_THREADS - 1) / CHUNK_SCAN_THREADS;  // consecutive tiles per thread
+    const uint32_t lo = min(n, threadIdx.x * per), hi = min(n, lo + per);
+    uint32_t a = 0, b = 0;
+    for (uint32_t i = lo; i < hi; ++i) {
+        a += tile_toks[i];
+        b += tile_lines[i];
+    }
+    const uint32_t ia = warp_incl_scan(a, lane), ib = warp_incl_scan(b, lane);
+    if (lane == 31) {
+        ws[0][warp] = ia;
+        ws[1][warp] = ib;
+    }
+    __syncthreads();
+    uint32_t ra = carry[2 * k] + ia - a, rb = carry[2 * k + 1] + ib - b, ta = 0, tb = 0;
+    for (int q = 0; q < CHUNK_SCAN_THREADS / 32; ++q) {
+        if (q < warp) {
+            ra += ws[0][q];
+            rb += ws[1][q];
+        }
+        ta += ws[0][q];
+        tb += ws[1][q];
+    }
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t x = tile_toks[i], y = tile_lines[i];
+        tile_toks[i] = ra;
+        tile_lines[i] = rb;
+        ra += x;
+        rb += y;
+    }
+    if (threadIdx.x == 0) {
+        carry[2 * k + 2] = carry[2 * k] + ta;
+        carry[2 * k + 3] = carry[2 * k + 1] + tb;
+    }
 }
 
 __global__ void k_line_sizes(const uint32_t* __restrict__ line_tok0, uint32_t n_lines, uint32_t n_tokens,
@@ -302,12 +351,24 @@ cudaError_t parse_count(const uint8_t* text, uint64_t n_bytes, uint32_t* tile_to
 
 cudaError_t parse_emit(const uint8_t* text, uint64_t n_bytes, const uint32_t* tile_tok0, const uint32_t* tile_line0,
                        uint32_t* tokens, uint32_t* line_tok0, uint32_t* flags, unsigned long long* first_bad,
-                       cudaStream_t s) {
+                       cudaStream_t s, uint64_t tile_lo, uint64_t tile_hi, uint32_t tok_cap, uint32_t line_cap) {
     const uint64_t tiles = parse_tiles(n_bytes);
-    if (tiles == 0) return cudaSuccess;
+    if (tile_hi > tiles) tile_hi = tiles;
+    if (tile_hi <= tile_lo) return cudaSuccess;
+    if (tile_hi - tile_lo > 0x7FFFFFFFull) return cudaErrorInvalidValue;
     note_launches();
-    k_parse_emit<<<(unsigned)tiles, PARSE_THREADS, 0, s>>>(text, n_bytes, tile_tok0, tile_line0, tokens, line_tok0,
-                                                           flags, first_bad);
+    k_parse_emit<<<(unsigned)(tile_hi - tile_lo), PARSE_THREADS, 0, s>>>(
+        text, n_bytes, tile_lo, tile_tok0, tile_line0, tokens, line_tok0, tok_cap, line_cap, flags, first_bad);
+    return cudaGetLastError();
+}
+
+cudaError_t parse_chunk_scan(uint32_t* tile_toks, uint32_t* tile_lines, uint64_t tile_lo, uint64_t tile_hi,
+                             uint32_t* carry, uint64_t k, cudaStream_t s) {
+    if (tile_hi <= tile_lo) return cudaSuccess;
+    if (tile_hi - tile_lo > 65536u || k > 0x7FFFFFFEull) return cudaErrorInvalidValue;
+    note_launches();
+    k_parse_chunk_scan<<<1, CHUNK_SCAN_THREADS, 0, s>>>(tile_toks + tile_lo, tile_lines + tile_lo,
+                                                       (uint32_t)(tile_hi - tile_lo), carry, (uint32_t)k);
     return cudaGetLastError();
 }
 

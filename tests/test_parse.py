@@ -208,3 +208,18 @@ def test_gpu_parse_digit_runs_across_chunks(ctx, digits):
         else:
             with pytest.raises(hs.HysetError, match="parse error at byte"):
                 ctx.parse(text)
+
+
+@pytest.mark.gpu
+def test_gpu_parse_text_denser_after_the_first_chunk(ctx):
+    """Host text is emitted chunk by chunk into buffers sized from the first
+    64 MB; here the rest is five times denser, so the estimate overflows and the
+    parse falls back to an exact second emission.  Same result as the reader."""
+    sparse = b"1000000000\n" * ((64 << 20) // 11 + 7)
+    dense = b"1 2\n" * (20 << 20)
+    text = sparse + dense
+    t, z, _ = oracle.read_text(text)
+    gt, gs, gz = ctx.parse(text).download()
+    np.testing.assert_array_equal(gt, t)
+    np.testing.assert_array_equal(gz, z)
+    np.testing.assert_array_equal(gs, np.concatenate([[0], np.cumsum(z[:-1])]).astype(np.uint32))
