@@ -282,7 +282,8 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 // and the token histogram (one atomic per entry).  A warp takes 32 consecutive
 // sets: their entries are contiguous in the output (off is the scan of len),
 // so the warp walks them flattened, 32 entries per round, each lane finding
-// its set by a 5-step bisection over the lanes' running lengths.  Every lane
+// its set from one ballot (the sets ending before the round) and one OR of the
+// positions where sets start inside the round.  Every lane
 // carries an entry in every round (prefixes are far shorter than 32), the
 // stores coalesce, and the token loads of EMIT_ROUNDS rounds are issued before
 // any of their stores.  Sets [lo, c.n): c, off and len are indexed by absolute
@@ -306,14 +307,16 @@ __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restric
 #pragma unroll
             for (int u = 0; u < EMIT_ROUNDS; ++u) {
                 const uint32_t j = j0 + 32u * u + lane;
-                int k = 0;  // first lane whose running length exceeds j
-#pragma unroll
-                for (int step = 16; step; step >>= 1)
-                    if (__shfl_sync(FULL, incl, k + step - 1) <= j) k += step;
-                const uint32_t end_k = __shfl_sync(FULL, incl, k);
-                const uint32_t len_k = __shfl_sync(FULL, l, k);
+                // the set of the round's first entry r0 (sets ending at or before
+                // r0 come first), plus the sets that start inside the round up to j
+                const uint32_t r0 = j0 + 32u * u, excl = incl - l;
+                const int kf = __popc(__ballot_sync(FULL, incl <= r0));
+                const uint32_t starts =
+                    __reduce_or_sync(FULL, (l && excl > r0 && excl < r0 + 32u) ? 1u << (excl - r0) : 0u);
+                const int k = (kf + __popc(starts & ((2u << lane) - 1u))) & 31;
+                const uint32_t excl_k = __shfl_sync(FULL, excl, k);
                 const uint32_t start_k = __shfl_sync(FULL, start, k);
-                const uint32_t i = j - (end_k - len_k);
+                const uint32_t i = j - excl_k;
                 tok[u] = j < total ? __ldg(c.tokens + start_k + i) : 0u;
                 val[u] = ((s0 + (uint32_t)k) << pos_bits) | i;
             }
