@@ -75,8 +75,10 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
 // (exclusive scan of counts) and e_val reordered so that each list holds its
 // entries in emission order.  Without a host round trip: the longest list is
 // written to *gate on the device; when every list has at most 64 entries the
-// entries are scattered into their lists with atomics and each list is
-// ordered by a rank sort inside a warp, otherwise the stable radix passes on
+// entries are scattered into their lists with atomics and each list is put
+// back in emission order inside a warp (insertion sort in shared memory, the
+// values being increasing in emission order), otherwise the stable radix
+// passes on
 // the token sort them (each kernel checks the gate and returns early when it
 // is not its case).  counts, e_token, alt_* and scratch (max of
 // scan_scratch_words(U + 1) and radix_scratch_words(n) words) are clobbered.

@@ -49,8 +49,8 @@ __device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t* warp_s
 }
 
 // gate: when non-null, the scans (and the radix kernels) run only when the
-// word is above LIST_SHORT (an index whose lists are not all short is sorted
-// by the radix passes; see k_list_scatter)
+// word is above LIST_SHORT: an index whose lists are not all short is sorted
+// by the radix passes, the others by k_list_scatter and k_list_rank
 __device__ __forceinline__ bool gated_off(const uint32_t* gate) { return gate && *gate <= LIST_SHORT; }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_tile_reduce(const uint32_t* in, uint64_t n, uint32_t* sums,
