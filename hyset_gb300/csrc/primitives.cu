@@ -22,8 +22,8 @@ namespace {
 // back in set order inside one warp (k_list_scatter, k_list_rank); longer
 // ones go through the radix passes.
 constexpr uint32_t LIST_SHORT = 64;
-constexpr int RANK_THREADS = 128;
-constexpr uint32_t RANK_CAP = 32 * LIST_SHORT;  // staged entries per warp: 32 lists
+constexpr int RANK_THREADS = 256;
+constexpr uint32_t RANK_CAP = 1024;  // staged entries per warp (32 lists of 32; larger ranges from global memory)
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
@@ -390,9 +390,8 @@ __global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t*
 // insertion sort (the scatter leaves lists nearly in emission order, since
 // earlier entries mostly take their slots first, so this is close to one pass
 // per list; at most LIST_SHORT^2/2 steps), and the warp writes the range back
-// with coalesced stores.  The gate bounds every list, so 32 lists fit the
-// stage; a larger range (not produced by k_list_scatter under the gate) would
-// be sorted in global memory.
+// with coalesced stores.  A range larger than the stage (32 lists averaging
+// more than 32 entries) is sorted in place in global memory, a lane per list.
 __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __restrict__ list_off, uint32_t U,
                                                            const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                            const uint32_t* gate) {

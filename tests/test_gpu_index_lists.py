@@ -2,7 +2,8 @@
 
 The lists must hold their entries in set-id order (the join bisects them by
 candidate id).  When every list has at most 64 entries the build fills them
-with one atomic per entry and orders each list with a rank sort inside a warp;
+with one atomic per entry and a warp puts 32 lists back in order (insertion
+sort in shared memory, or in global memory when the 32 lists exceed the stage);
 a longer list sends the whole build through the stable radix passes.  The
 choice is made on the device from the longest list, so both sides of the bound
 are checked here against the oracle, with a token planted in the prefix of
@@ -20,6 +21,22 @@ def _longest_list(c, tau):
     mid = similarity.midprefix_array("jaccard", c.sizes, tau)
     idx = np.concatenate([c.tokens[s:s + m] for s, m in zip(c.starts, mid)])
     return int(np.bincount(idx).max())
+
+
+def _plant_many(c, n_tokens, per_token, seed):
+    """Tokens 0..n_tokens-1 (below every other token) each added to per_token
+    distinct sets, one planted token per set; sets re-sorted by size."""
+    rng = np.random.default_rng(seed)
+    shift = n_tokens
+    sets = [c.tokens[s:s + l].astype(np.uint32) + shift for s, l in zip(c.starts, c.sizes)]
+    chosen = rng.choice(len(sets), size=n_tokens * per_token, replace=False)
+    for q, i in enumerate(chosen):
+        sets[i] = np.concatenate([[q % n_tokens], sets[i]]).astype(np.uint32)
+    order = sorted(range(len(sets)), key=lambda i: len(sets[i]))
+    sets = [sets[i] for i in order]
+    sizes = np.array([len(s) for s in sets], np.uint32)
+    starts = np.concatenate([[0], np.cumsum(sizes[:-1], dtype=np.uint64)]).astype(np.uint32)
+    return synth.Collection(np.concatenate(sets).astype(np.uint32), starts, sizes)
 
 
 def _plant(c, k, seed):
@@ -54,7 +71,7 @@ def test_lists_on_both_sides_of_the_bound(ctx, k):
 
 @pytest.mark.parametrize("n,tau", [(10000, 0.5), (200000, 0.6), (200000, 0.8)])
 def test_natural_lists(ctx, n, tau):
-    """Longest lists 63 (atomic + rank path), 141 (radix path) and 25."""
+    """Longest lists 63 (short-list path), 141 (radix path) and 25."""
     c = synth.generate(synth.C2 if n > 10000 else synth.C1, n_sets=n, seed=7)
     exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, tau))
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
@@ -63,3 +80,14 @@ def test_natural_lists(ctx, n, tau):
     p = np.asarray(r.pairs, np.uint64)
     key = (p[:, 0] << np.uint64(32)) | p[:, 1]
     assert bool(np.all(key[1:] > key[:-1]))
+
+
+def test_short_lists_beyond_one_warp_stage(ctx):
+    """32 consecutive lists of 40 entries (1,280 together, more than a warp
+    stages in shared memory): the short-list path orders them in global memory."""
+    c = _plant_many(synth.generate(synth.C2, n_sets=20000, seed=62), 32, 40, seed=5)
+    assert _longest_list(c, 0.8) == 40
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.8))
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    r = ctx.self_join(coll, threshold=0.8, technique="fgss", probe_major=True, bitmap=256, sort_pairs=True)
+    assert r.count == len(exp) and oracle.as_set(r.pairs) == exp
