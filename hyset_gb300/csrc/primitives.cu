@@ -357,7 +357,7 @@ __global__ void k_list_max(const uint32_t* __restrict__ counts, uint32_t U, uint
 // list's cursor (initialised to the list offsets), so each list holds its
 // entries in arbitrary order.  Tokens at or above U are left out (the counts
 // did not count them).
-constexpr int SCATTER_ITEMS = 4;  // entries per thread per step: four atomics in flight
+constexpr int SCATTER_ITEMS = 8;  // entries per thread per step: eight atomics in flight
 __global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t* __restrict__ val, uint64_t n,
                                uint32_t U, uint32_t* __restrict__ cursor, uint32_t* __restrict__ out,
                                const uint32_t* gate, bool vec) {
@@ -365,11 +365,14 @@ __global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t*
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * SCATTER_ITEMS;
     for (uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * SCATTER_ITEMS; i0 < n; i0 += stride) {
         uint32_t t[SCATTER_ITEMS], v[SCATTER_ITEMS], at[SCATTER_ITEMS];
-        if (vec && i0 + SCATTER_ITEMS <= n) {  // 16-byte loads (vec: both arrays 16-byte aligned)
-            const uint4 tt = *reinterpret_cast<const uint4*>(tok + i0);
-            const uint4 vv = *reinterpret_cast<const uint4*>(val + i0);
-            t[0] = tt.x, t[1] = tt.y, t[2] = tt.z, t[3] = tt.w;
-            v[0] = vv.x, v[1] = vv.y, v[2] = vv.z, v[3] = vv.w;
+        if (SCATTER_ITEMS % 4 == 0 && vec && i0 + SCATTER_ITEMS <= n) {  // 16-byte loads (both arrays aligned)
+#pragma unroll
+            for (int q = 0; q < SCATTER_ITEMS / 4; ++q) {
+                const uint4 tt = *reinterpret_cast<const uint4*>(tok + i0 + 4 * q);
+                const uint4 vv = *reinterpret_cast<const uint4*>(val + i0 + 4 * q);
+                t[4 * q] = tt.x, t[4 * q + 1] = tt.y, t[4 * q + 2] = tt.z, t[4 * q + 3] = tt.w;
+                v[4 * q] = vv.x, v[4 * q + 1] = vv.y, v[4 * q + 2] = vv.z, v[4 * q + 3] = vv.w;
+            }
         } else {
 #pragma unroll
             for (int u = 0; u < SCATTER_ITEMS; ++u) {
