@@ -304,7 +304,8 @@ def run_ours(args, ws, rank, local):
                "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "strong",
                "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded generator)",
                "config": {"workload": workload_name(args.sim), "threshold": THRESHOLD, "sim": args.sim,
-                          "technique": r.technique, "bitmap_bits": r.bitmap_bits, "result_pairs": total_pairs,
+                          "technique": r.technique, "bitmap_bits": r.bitmap_bits, "verify_mode": r.verify_mode,
+                          "result_pairs": total_pairs,
                           "parallelism": f"probe shards x{ws}" if ws > 1 else "single GPU",
                           "l2": "512 MB buffer written between timed steps; tokens 449 MB > L2",
                           "plain_block_pair_ms": plain_ms,
@@ -566,7 +567,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
-    ap.add_argument("--vmode", type=int, default=0, help="verification: 0 auto, 1 lane, 2 warp per candidate")
+    ap.add_argument("--vmode", type=int, default=0,
+                    help="verification: 0 auto (the autotuner's samples choose), 1 lane, 2 warp per candidate")
     ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse", "verify"],
                     help="batch: the batched R-S workload; parse: the collection text reader; verify: the "
                          "candidate verifier alone (separate measurements, not the headline)")

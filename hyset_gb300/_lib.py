@@ -78,6 +78,7 @@ PROTOTYPES = {
     "hyset_result_pairs": (C.c_void_p, [C.c_void_p]),
     "hyset_result_technique": (C.c_int, [C.c_void_p]),
     "hyset_result_bitmap_bits": (C.c_uint32, [C.c_void_p]),
+    "hyset_result_verify_mode": (C.c_uint32, [C.c_void_p]),
     "hyset_result_split": (C.c_uint32, [C.c_void_p, C.POINTER(C.c_int)]),
     "hyset_result_device_ms": (C.c_double, [C.c_void_p]),
     "hyset_result_kernel_ms": (C.c_double, [C.c_void_p]),

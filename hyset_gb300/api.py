@@ -33,6 +33,7 @@ class JoinResult:
     bitmap_bits: int = 0        # signature width the join ran with
     split_at: int = 0           # partition split: first probe id of the high range (0 = none)
     split_low: str = ""         # the low range's technique when split
+    verify_mode: int = 0        # 1 lane per candidate, 2 warp per candidate, 3 staged (candidate lists)
 
 
 # R-S joins: which collection is indexed (hyset_join_opts.orientation)
@@ -77,7 +78,8 @@ def _take_result(lib, r) -> JoinResult:
                           float(lib.hyset_result_device_ms(r)), float(lib.hyset_result_kernel_ms(r)),
                           [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0),
                           int(lib.hyset_result_launches(r)), SELECTOR_NAMES.get(lib.hyset_result_selector(r), "?"),
-                          int(lib.hyset_result_bitmap_bits(r)), *_split(lib, r))
+                          int(lib.hyset_result_bitmap_bits(r)), *_split(lib, r),
+                          int(lib.hyset_result_verify_mode(r)))
     finally:
         lib.hyset_result_free(r)
 

@@ -758,13 +758,18 @@ hyset_status plan_split(hyset_ctx* ctx, hyset_coll* R, const hyset_join_opts* o,
 // on long sets at low thresholds, 128 on short ones, none on some collections.
 constexpr uint32_t TUNE_MIN_PROBES = 60000, TUNE_SAMPLE = 16384;  // a sample fills the GPU for about two waves
 constexpr float TUNE_MARGIN = 0.92f;  // leave the rule's width only for an estimated gain of 8 % or more
+constexpr float TUNE_VMODE_MARGIN = 0.97f;  // warp verification only for an estimated gain of 3 % or more
 
+// The signature width (and, when vmode is given, the verification mode) of a
+// prefix-index join, from timed samples of its probe range; cached per join
+// key as bits | vmode << 16.
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
-                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits) {
+                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode = nullptr) {
     const std::string key = join_key(R, S, o);
     auto it = ctx->bits_cache.find(key);
-    if (it != ctx->bits_cache.end()) {
-        *bits = it->second;
+    if (it != ctx->bits_cache.end() && (!vmode || (it->second >> 16))) {
+        *bits = it->second & 0xFFFFu;
+        if (vmode) *vmode = (int)(it->second >> 16);
         return HYSET_OK;
     }
     cudaStream_t s = ctx->stream;
@@ -784,9 +789,32 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     P.out = Sink{nullptr, ctx->s_count.as<unsigned long long>(), 0, 1};
     P.work = ctx->s_work.as<unsigned int>();
     const uint32_t cand[4] = {0, 128, 256, 512};
-    float est[4] = {0, 0, 0, 0};
+    float est[4] = {0, 0, 0, 0}, kern_est[4] = {0, 0, 0, 0};
     float best_ms = 0;
     uint32_t best = 256;
+    // estimated kernel time of the whole probe range with signature words w and
+    // verification mode vm, from three samples (start, middle, end)
+    auto sample = [&](int vm, float* out) -> hyset_status {
+        float total = 0;
+        uint32_t sampled = 0;
+        for (int c = 0; c < 3; ++c) {
+            const uint32_t span = p_hi - p_lo, len = std::min(TUNE_SAMPLE, span / 3);
+            P.p_lo = p_lo + (uint32_t)((uint64_t)(span - len) * c / 2);
+            P.p_hi = P.p_lo + len;
+            sampled += len;
+            CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+            CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
+            CK(cudaEventRecord(ctx->ek0, s));
+            CK(launch_join(P, TECH_FGSS, vm, ctx->sm_count, s));
+            CK(cudaEventRecord(ctx->ek1, s));
+            CK(cudaEventSynchronize(ctx->ek1));
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, ctx->ek0, ctx->ek1));
+            total += ms;
+        }
+        *out = total * (float)(p_hi - p_lo) / (float)(sampled ? sampled : 1);
+        return HYSET_OK;
+    };
     for (int k = 0; k < 4; ++k) {
         const int words = (int)(cand[k] / 64);
         P.words = words;
@@ -805,24 +833,9 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
             P.bits_S = bs;
         }
         float total = 0;
-        uint32_t sampled = 0;
-        for (int c = 0; c < 3; ++c) {  // samples at the start, middle and end of the probe range
-            const uint32_t span = p_hi - p_lo, len = std::min(TUNE_SAMPLE, span / 3);
-            P.p_lo = p_lo + (uint32_t)((uint64_t)(span - len) * c / 2);
-            P.p_hi = P.p_lo + len;
-            sampled += len;
-            CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
-            CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
-            CK(cudaEventRecord(ctx->ek0, s));
-            CK(launch_join(P, TECH_FGSS, 1, ctx->sm_count, s));
-            CK(cudaEventRecord(ctx->ek1, s));
-            CK(cudaEventSynchronize(ctx->ek1));
-            float ms = 0;
-            CK(cudaEventElapsedTime(&ms, ctx->ek0, ctx->ek1));
-            total += ms;
-        }
-        // the whole probe range's estimated kernel time plus the generation
-        total = total * (float)(p_hi - p_lo) / (float)(sampled ? sampled : 1) + gen_ms;
+        ST(sample(1, &total));
+        kern_est[k] = total;
+        total += gen_ms;  // the whole probe range's estimated kernel time plus the generation
         est[k] = total;
         if (k == 0 || total < best_ms) {
             best_ms = total;
@@ -833,7 +846,29 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     const uint32_t rule = (double)R->n_tokens / (double)std::max<uint32_t>(R->n, 1) <= 48.0 ? 128u : 256u;
     const float rule_ms = est[rule == 128u ? 1 : 2];
     if (best != rule && best_ms > TUNE_MARGIN * rule_ms) best = rule;
-    ctx->bits_cache[key] = best;
+    // verification: a lane per surviving item, or the warp per item when the
+    // samples show it faster at the chosen width (long merges: low thresholds,
+    // cosine)
+    int vm = 1;
+    if (vmode) {
+        const int kb = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
+        const int words = (int)(best / 64);
+        P.words = words;
+        P.bits_R = P.bits_S = nullptr;
+        if (words) {
+            const uint64_t *br = nullptr, *bs = nullptr;
+            ST(get_bitmaps(ctx, R, words, &br));
+            if (self) bs = br;
+            else ST(get_bitmaps(ctx, S, words, &bs));
+            P.bits_R = br;
+            P.bits_S = bs;
+        }
+        float warp_ms = 0;
+        ST(sample(2, &warp_ms));
+        if (warp_ms < TUNE_VMODE_MARGIN * kern_est[kb]) vm = 2;
+        *vmode = vm;
+    }
+    ctx->bits_cache[key] = best | (vmode ? (uint32_t)vm << 16 : 0u);
     *bits = best;
     return HYSET_OK;
 }
@@ -867,6 +902,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
             res->launches = part[0].launches + part[1].launches;
             res->technique = part[1].technique;
             res->bitmap_bits = part[1].bitmap_bits;
+            res->verify_mode = part[1].verify_mode;
             res->selector = 2;
             res->split_at = split_at;
             res->split_low = part[0].technique;
@@ -880,14 +916,15 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     ST(select_technique(ctx, R, S, o, &selected, &res->selector));
     Tuned tn = tune(R, S, o, selected);
     const hyset_technique tech = tn.tech;
-    const int vmode = tn.vmode;
     res->technique = tech;
     {
         const uint32_t a_lo = o->probe_end ? o->probe_begin : 0, a_hi = o->probe_end ? o->probe_end : S->n;
         if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && tech == HYSET_TECH_FGSS && tn.probe_major &&
             a_hi - a_lo >= TUNE_MIN_PROBES)
-            ST(autotune_bits(ctx, R, S, o, b, self, a_lo, a_hi, &tn.bits));
+            ST(autotune_bits(ctx, R, S, o, b, self, a_lo, a_hi, &tn.bits, o->verify_mode ? nullptr : &tn.vmode));
     }
+    const int vmode = tn.vmode;
+    res->verify_mode = (uint32_t)vmode;
     res->bitmap_bits = tech == HYSET_TECH_DIRECT ? 0 : tn.bits;
     if (o->probe_end > S->n || o->probe_begin > o->probe_end)
         return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
@@ -1763,7 +1800,10 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
     if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && n_sets >= TUNE_MIN_PROBES) {
         auto it = ctx->bits_cache.find(key);
         if (it == ctx->bits_cache.end()) pipelined = false;
-        else tn.bits = it->second;
+        else {
+            tn.bits = it->second & 0xFFFFu;
+            if (!o->verify_mode && (it->second >> 16)) tn.vmode = (int)(it->second >> 16);
+        }
     }
     Bounds* b = nullptr;
     ST(get_bounds(ctx, o->sim, o->threshold, C->max_size, 0, &b));
@@ -1909,6 +1949,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         ctx->universe_cache[ukey] = C->universe;
         res->technique = HYSET_TECH_FGSS;
         res->bitmap_bits = tn.bits;
+        res->verify_mode = (uint32_t)tn.vmode;
         res->selector = selector;
         if (o->collect_stats) res->stats[3] = E;
         res->launches = launches() - launches0;
@@ -2127,6 +2168,7 @@ const hyset_pair* hyset_result_pairs(const hyset_result* r) {
 uint64_t hyset_result_launches(const hyset_result* r) { return r ? r->launches : 0; }
 hyset_technique hyset_result_technique(const hyset_result* r) { return r ? r->technique : HYSET_TECH_AUTO; }
 uint32_t hyset_result_bitmap_bits(const hyset_result* r) { return r ? r->bitmap_bits : 0; }
+uint32_t hyset_result_verify_mode(const hyset_result* r) { return r ? r->verify_mode : 0; }
 uint32_t hyset_result_split(const hyset_result* r, hyset_technique* low_technique) {
     if (low_technique) *low_technique = r ? r->split_low : HYSET_TECH_AUTO;
     return r ? r->split_at : 0;
@@ -2471,6 +2513,7 @@ hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, cons
         float kms = 0;
         CK(cudaEventElapsedTime(&kms, ctx->ek0, ctx->ek1));
         res->kernel_ms = res->device_ms = kms;
+        res->verify_mode = (uint32_t)vmode;
         res->count = count;
         if (count_only || count <= cap) break;
         cap = count + count / 8 + 1024;

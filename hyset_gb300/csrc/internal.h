@@ -173,6 +173,7 @@ struct hyset_result {
     const void* device_pairs = nullptr;
     hyset_technique technique = HYSET_TECH_AUTO;
     uint32_t bitmap_bits = 0;  // signature width the join ran with
+    uint32_t verify_mode = 0;  // verification mode the join ran with
     uint32_t split_at = 0;     // partition split: first probe id of the high range (0 = none)
     hyset_technique split_low = HYSET_TECH_AUTO;  // the low range's technique
     double device_ms = 0;

@@ -172,6 +172,7 @@ uint64_t hyset_result_count(const hyset_result* r);
 const hyset_pair* hyset_result_pairs(const hyset_result* r); /* NULL when count_only */
 hyset_technique hyset_result_technique(const hyset_result* r);
 uint32_t hyset_result_bitmap_bits(const hyset_result* r);   /* signature width used (0 = none) */
+uint32_t hyset_result_verify_mode(const hyset_result* r);   /* verification mode used (1 lane, 2 warp, 3 staged) */
 /* Partition split chosen by the learned selector for an AUTO self-join: the
  * first probe id of the high range (0 = the join ran as one range) and, in
  * *low_technique (may be NULL), the low range's technique (the high range's is

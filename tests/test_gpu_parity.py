@@ -238,3 +238,24 @@ def test_batch_join_matches_joins_run_one_at_a_time(ctx):
         for k, (r, exp) in enumerate(zip(res, single)):
             assert r.count == len(exp), (attempt, k, joins[k][2])
             assert as_set_checked(r.pairs) == exp, (attempt, k, joins[k][2])
+
+
+@pytest.mark.parametrize("tau", [0.6, 0.9])
+def test_autotuned_join_keeps_the_pairs(ctx, tau):
+    """AUTO with bitmap 0 on 80,000 probes: the autotuner times samples and
+    picks the signature width and the verification mode (a lane or the warp
+    per candidate); the choice is reported, reused from the context's cache
+    (also by the host-input join) and never changes the pairs."""
+    c = synth.generate(synth.C2, n_sets=80000, seed=71)
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, tau))
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    r1 = ctx.self_join(coll, threshold=tau)
+    r2 = ctx.self_join(coll, threshold=tau)
+    assert r1.bitmap_bits in (0, 128, 256, 512) and r1.verify_mode in (1, 2), (r1.bitmap_bits, r1.verify_mode)
+    assert (r2.bitmap_bits, r2.verify_mode) == (r1.bitmap_bits, r1.verify_mode)
+    assert as_set_checked(r1.pairs) == exp and as_set_checked(r2.pairs) == exp
+    r3 = ctx.self_join_host(c.tokens, c.sizes, c.starts, threshold=tau)
+    assert oracle.as_set(r3.pairs) == exp
+    for vm in (1, 2):
+        r = ctx.self_join(coll, threshold=tau, verify_mode=vm)
+        assert r.verify_mode == vm and as_set_checked(r.pairs) == exp
