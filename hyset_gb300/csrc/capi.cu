@@ -291,9 +291,15 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         CK(ctx->sc->gate.ensure(4, s));
         CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
         CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
+        // the list build's path is read back once per collection and prefix
+        // table (not while a batch is being captured into a graph)
+        cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+        CK(cudaStreamIsCapturing(s, &capturing));
+        int& path = c->list_path[d_pre];
         CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts, ix.list_off.as<uint32_t>(),
                        ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(), ctx->sc->gate.as<uint32_t>(),
-                       key_bits_for(U), scr, s));
+                       key_bits_for(U), scr, s, &path,
+                       capturing == cudaStreamCaptureStatusNone ? ctx->h_flags + 15 : nullptr));
         ix.sim = b->sim;
         ix.tau = b->tau;
         ix.kind = kind;

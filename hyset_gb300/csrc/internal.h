@@ -163,6 +163,7 @@ struct hyset_coll {
     hs::Index index_mid;  // R-S bands: midprefix entries, same layout as index
     hs::DevBuf g_off, g_set, g_ps, g_cursor;  // token groups of the prefix entries (token-major join)
     std::map<int, hs::DevBuf> bitmaps;  // by words
+    std::map<const uint32_t*, int> list_path;  // per prefix table: index lists built short (1) or by radix (2)
     hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, meta.as<uint2>(), n}; }
 };
 

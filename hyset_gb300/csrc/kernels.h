@@ -80,11 +80,16 @@ cudaError_t radix_sort_pairs(uint32_t* keys, uint32_t* vals, uint32_t* alt_keys,
 // values being increasing in emission order), otherwise the stable radix
 // passes on
 // the token sort them (each kernel checks the gate and returns early when it
-// is not its case).  counts, e_token, alt_* and scratch (max of
-// scan_scratch_words(U + 1) and radix_scratch_words(n) words) are clobbered.
+// is not its case).  *path (optional): 1 = only the short-list path (correct
+// for any lists, slow for long ones), 2 = only the radix passes, 0 = choose:
+// with h_gate (pinned) the longest list is read back once (a synchronisation)
+// and *path set, otherwise both paths launch and the gate picks on the device
+// (no host round trip: graph capture).  counts, e_token, alt_* and scratch
+// (max of scan_scratch_words(U + 1) and radix_scratch_words(n) words) are
+// clobbered.
 cudaError_t index_lists(uint32_t* e_token, uint32_t* e_val, uint64_t n, uint32_t U, uint32_t* counts,
                         uint32_t* list_off, uint32_t* alt_keys, uint32_t* alt_vals, uint32_t* gate, int key_bits,
-                        uint32_t* scratch, cudaStream_t s);
+                        uint32_t* scratch, cudaStream_t s, int* path = nullptr, uint32_t* h_gate = nullptr);
 
 // Prefix entries of sets [lo, hi): the first prefix_len(size) tokens of every
 // set (include/hyset/collection.hpp:128-135).  entry_off must hold the

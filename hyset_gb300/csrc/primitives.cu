@@ -361,7 +361,7 @@ constexpr int SCATTER_ITEMS = 8;  // entries per thread per step: eight atomics 
 __global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t* __restrict__ val, uint64_t n,
                                uint32_t U, uint32_t* __restrict__ cursor, uint32_t* __restrict__ out,
                                const uint32_t* gate, bool vec) {
-    if (*gate > LIST_SHORT) return;
+    if (gate && *gate > LIST_SHORT) return;  // gate == nullptr: run
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x * SCATTER_ITEMS;
     for (uint64_t i0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * SCATTER_ITEMS; i0 < n; i0 += stride) {
         uint32_t t[SCATTER_ITEMS], v[SCATTER_ITEMS], at[SCATTER_ITEMS];
@@ -398,7 +398,7 @@ __global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t*
 __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __restrict__ list_off, uint32_t U,
                                                            const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                            const uint32_t* gate) {
-    if (*gate > LIST_SHORT) return;
+    if (gate && *gate > LIST_SHORT) return;  // gate == nullptr: run
     __shared__ uint32_t stage_all[RANK_THREADS / 32][RANK_CAP];
     const int lane = threadIdx.x & 31;
     uint32_t* stage = stage_all[threadIdx.x >> 5];
@@ -722,26 +722,43 @@ cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uin
 
 cudaError_t index_lists(uint32_t* e_token, uint32_t* e_val, uint64_t n, uint32_t U, uint32_t* counts,
                         uint32_t* list_off, uint32_t* alt_keys, uint32_t* alt_vals, uint32_t* gate, int key_bits,
-                        uint32_t* scratch, cudaStream_t s) {
+                        uint32_t* scratch, cudaStream_t s, int* path, uint32_t* h_gate) {
     cudaError_t e = scan_exclusive(counts, list_off, (uint64_t)U + 1, scratch, s);
     if (e != cudaSuccess) return e;
     if (n == 0) return cudaSuccess;
-    e = cudaMemsetAsync(gate, 0, 4, s);
-    if (e != cudaSuccess) return e;
-    note_launches(3);
-    k_list_max<<<grid_for(U, 256, 4 * 152), 256, 0, s>>>(counts, U, gate);
-    // short lists: scatter into alt_vals (the counts become the cursors), rank
-    // back into e_val
-    e = cudaMemcpyAsync(counts, list_off, (size_t)U * 4, cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return e;
-    const bool vec = ((reinterpret_cast<uintptr_t>(e_token) | reinterpret_cast<uintptr_t>(e_val)) & 15u) == 0;
-    k_list_scatter<<<grid_for((n + SCATTER_ITEMS - 1) / SCATTER_ITEMS, 256), 256, 0, s>>>(
-        e_token, e_val, n, U, counts, alt_vals, gate, vec);
-    k_list_rank<<<grid_for(U, RANK_THREADS), RANK_THREADS, 0, s>>>(list_off, U, alt_vals, e_val, gate);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    // long lists: the radix passes (each of their kernels checks the gate)
-    return radix_sort_pairs(e_token, e_val, alt_keys, alt_vals, n, key_bits, scratch, s, false, gate);
+    int p = path ? *path : 0;
+    const uint32_t* g = nullptr;  // the kernels' device-side choice (p == 0 only)
+    if (p == 0) {
+        e = cudaMemsetAsync(gate, 0, 4, s);
+        if (e != cudaSuccess) return e;
+        note_launches();
+        k_list_max<<<grid_for(U, 256, 4 * 152), 256, 0, s>>>(counts, U, gate);
+        if (h_gate) {  // one host read settles the path for later builds
+            e = cudaMemcpyAsync(h_gate, gate, 4, cudaMemcpyDeviceToHost, s);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return e;
+            p = *h_gate <= LIST_SHORT ? 1 : 2;
+            if (path) *path = p;
+        } else {
+            g = gate;
+        }
+    }
+    if (p != 2) {
+        // short lists: scatter into alt_vals (the counts become the cursors),
+        // order back into e_val
+        e = cudaMemcpyAsync(counts, list_off, (size_t)U * 4, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+        const bool vec = ((reinterpret_cast<uintptr_t>(e_token) | reinterpret_cast<uintptr_t>(e_val)) & 15u) == 0;
+        note_launches(2);
+        k_list_scatter<<<grid_for((n + SCATTER_ITEMS - 1) / SCATTER_ITEMS, 256), 256, 0, s>>>(
+            e_token, e_val, n, U, counts, alt_vals, g, vec);
+        k_list_rank<<<grid_for(U, RANK_THREADS), RANK_THREADS, 0, s>>>(list_off, U, alt_vals, e_val, g);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    // long lists: the radix passes (gated when the choice is the device's)
+    if (p != 1) return radix_sort_pairs(e_token, e_val, alt_keys, alt_vals, n, key_bits, scratch, s, false, g);
+    return cudaSuccess;
 }
 
 cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, uint32_t limit, cudaStream_t s) {
