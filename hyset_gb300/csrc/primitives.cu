@@ -23,7 +23,7 @@ namespace {
 // ones go through the radix passes.
 constexpr uint32_t LIST_SHORT = 64;
 constexpr int RANK_THREADS = 256;
-constexpr uint32_t RANK_CAP = 1024;  // staged entries per warp (32 lists of 32; larger ranges from global memory)
+constexpr uint32_t RANK_CAP = 1024;  // staged entries per warp (16 lists of up to LIST_SHORT always fit)
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
@@ -392,9 +392,60 @@ __global__ void k_list_scatter(const uint32_t* __restrict__ tok, const uint32_t*
 // the warp stages them in shared memory, lane k orders list k there by
 // insertion sort (the scatter leaves lists nearly in emission order, since
 // earlier entries mostly take their slots first, so this is close to one pass
-// per list; at most LIST_SHORT^2/2 steps), and the warp writes the range back
-// with coalesced stores.  A range larger than the stage (32 lists averaging
-// more than 32 entries) is sorted in place in global memory, a lane per list.
+// per list), and the warp writes the range back with coalesced stores.  When
+// the 32 lists overflow the stage they go as two halves of 16 (16 lists of at
+// most LIST_SHORT entries always fit); a half that still overflows (lists
+// longer than LIST_SHORT) is sorted in place in global memory, a lane per list.
+__device__ __forceinline__ void order_lists(const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
+                                            uint32_t* stage, uint32_t ls, uint32_t le, int k0, int k1, int lane) {
+    const uint32_t a = __shfl_sync(FULL, ls, k0), b = __shfl_sync(FULL, le, k1 - 1), m = b - a;
+    const bool mine = lane >= k0 && lane < k1;
+    if (m <= RANK_CAP) {
+        for (uint32_t j0 = 0; j0 < m; j0 += 256) {  // eight loads in flight per lane
+            uint32_t x[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t j = j0 + 32u * u + lane;
+                x[u] = j < m ? in[a + j] : 0u;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const uint32_t j = j0 + 32u * u + lane;
+                if (j < m) stage[j] = x[u];
+            }
+        }
+        __syncwarp();
+        if (mine) {
+            const uint32_t lo = ls - a, hi = le - a;
+            for (uint32_t i = lo + 1; i < hi; ++i) {
+                const uint32_t x = stage[i];
+                uint32_t j = i;
+                for (; j > lo; --j) {
+                    const uint32_t y = stage[j - 1];
+                    if (y < x) break;
+                    stage[j] = y;
+                }
+                stage[j] = x;
+            }
+        }
+        __syncwarp();
+        for (uint32_t j = lane; j < m; j += 32) out[a + j] = stage[j];
+        __syncwarp();
+    } else if (mine) {
+        for (uint32_t i = ls; i < le; ++i) out[i] = in[i];
+        for (uint32_t i = ls + 1; i < le; ++i) {
+            const uint32_t x = out[i];
+            uint32_t j = i;
+            for (; j > ls; --j) {
+                const uint32_t y = out[j - 1];
+                if (y < x) break;
+                out[j] = y;
+            }
+            out[j] = x;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __restrict__ list_off, uint32_t U,
                                                            const uint32_t* __restrict__ in, uint32_t* __restrict__ out,
                                                            const uint32_t* gate) {
@@ -407,50 +458,12 @@ __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __re
         const uint64_t t = t0 + lane;
         const uint32_t ls = list_off[t < U ? t : U];
         const uint32_t le = list_off[t + 1 < U ? t + 1 : U];
-        const uint32_t a = __shfl_sync(FULL, ls, 0);
-        const uint32_t b = __shfl_sync(FULL, le, 31);
-        const uint32_t m = b - a;
-        if (m <= RANK_CAP) {
-            for (uint32_t j0 = 0; j0 < m; j0 += 256) {  // eight loads in flight per lane
-                uint32_t x[8];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const uint32_t j = j0 + 32u * u + lane;
-                    x[u] = j < m ? in[a + j] : 0u;
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    const uint32_t j = j0 + 32u * u + lane;
-                    if (j < m) stage[j] = x[u];
-                }
-            }
-            __syncwarp();
-            const uint32_t lo = ls - a, hi = le - a;
-            for (uint32_t i = lo + 1; i < hi; ++i) {
-                const uint32_t x = stage[i];
-                uint32_t j = i;
-                for (; j > lo; --j) {
-                    const uint32_t y = stage[j - 1];
-                    if (y < x) break;
-                    stage[j] = y;
-                }
-                stage[j] = x;
-            }
-            __syncwarp();
-            for (uint32_t j = lane; j < m; j += 32) out[a + j] = stage[j];
-            __syncwarp();
+        const uint32_t a = __shfl_sync(FULL, ls, 0), b = __shfl_sync(FULL, le, 31);
+        if (b - a <= RANK_CAP) {
+            order_lists(in, out, stage, ls, le, 0, 32, lane);
         } else {
-            for (uint32_t i = ls; i < le; ++i) out[i] = in[i];
-            for (uint32_t i = ls + 1; i < le; ++i) {
-                const uint32_t x = out[i];
-                uint32_t j = i;
-                for (; j > ls; --j) {
-                    const uint32_t y = out[j - 1];
-                    if (y < x) break;
-                    out[j] = y;
-                }
-                out[j] = x;
-            }
+            order_lists(in, out, stage, ls, le, 0, 16, lane);
+            order_lists(in, out, stage, ls, le, 16, 32, lane);
         }
     }
 }

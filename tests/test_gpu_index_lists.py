@@ -91,3 +91,30 @@ def test_short_lists_beyond_one_warp_stage(ctx):
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
     r = ctx.self_join(coll, threshold=0.8, technique="fgss", probe_major=True, bitmap=256, sort_pairs=True)
     assert r.count == len(exp) and oracle.as_set(r.pairs) == exp
+
+
+def test_remembered_short_path_with_lists_grown_in_place(ctx):
+    """The list path is read back once per collection and prefix table.  A
+    collection over caller memory can change afterwards: here token 0 is put
+    at the head of 1,500 sets in place (tokens stay sorted, the universe the
+    same), so one list far exceeds the short-list bound while the remembered
+    path is the short one; the lists must still come out in order."""
+    torch = pytest.importorskip("torch")
+    c = synth.generate(synth.C2, n_sets=20000, seed=63)
+    assert c.tokens.min() >= 1
+    dt = torch.from_numpy(c.tokens.view(np.int32)).cuda()
+    ds = torch.from_numpy(c.starts.view(np.int32)).cuda()
+    dz = torch.from_numpy(c.sizes.view(np.int32)).cuda()
+    coll = ctx.from_device(dt.data_ptr(), c.tokens.size, ds.data_ptr(), dz.data_ptr(), c.n, keep=(dt, ds, dz))
+    kw = dict(technique="fgss", probe_major=True, bitmap=256)
+    r = ctx.self_join(coll, threshold=0.8, **kw)
+    assert oracle.as_set(r.pairs) == oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.8))
+    grown = c.tokens.copy()
+    chosen = np.random.default_rng(9).choice(c.n, size=1500, replace=False)
+    grown[c.starts[chosen]] = 0
+    assert _longest_list(synth.Collection(grown, c.starts, c.sizes), 0.8) == 1500
+    dt.copy_(torch.from_numpy(grown.view(np.int32)).cuda())
+    torch.cuda.synchronize()
+    r = ctx.self_join(coll, threshold=0.8, **kw)
+    assert oracle.as_set(r.pairs) == oracle.as_set(oracle.join(grown, c.starts, c.sizes, 0.8))
+    coll.free()
