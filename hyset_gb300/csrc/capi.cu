@@ -1272,8 +1272,21 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
     CK(cudaMemcpyAsync(plan->unit_off.p, unit_off.data(), (n + 1) * 4, cudaMemcpyHostToDevice, s));
     CK(cudaStreamSynchronize(s));
     ctx->batch = std::move(plan);
-    // capture the device work once; later calls with the same batch replay it
     BatchPlan& bp = *ctx->batch;
+    // indexes whose list path is not known yet are built once here, outside
+    // the capture, so that the path is read back and remembered: the graph then
+    // holds only the kernels of the path each index takes
+    for (auto& bjp : bp.joins) {
+        BatchJoin& bj = *bjp;
+        if (bj.ktech != TECH_FGSS) continue;
+        const uint32_t* index_tab = bj.b->view.index_prefix;
+        const uint32_t* mid_tab = bj.b->view.mid_prefix;
+        if (!bj.R->list_path.count(index_tab)) ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix));
+        if (use_bands(bj.b, bj.self) && !bj.R->list_path.count(mid_tab))
+            ST(build_sorted_index(ctx, bj.R, bj.b, 2, bj.ix_mid, &bj.b->mid_prefix, bj.b->view.mid_prefix,
+                                  (int)bj.ix.pos_bits));
+    }
+    // capture the device work once; later calls with the same batch replay it
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     hyset_status st = batch_record(ctx, bp);
     cudaGraph_t g = nullptr;
