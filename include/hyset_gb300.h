@@ -66,9 +66,14 @@ typedef struct {
     hyset_sim sim;
     double threshold;          /* in (0, 1] */
     hyset_technique technique;
-    uint32_t bitmap_bits;      /* 0 = no signature filter; else 64, 128, 256 or 512 */
+    uint32_t bitmap_bits;      /* 64, 128, 256 or 512; 0 = chosen by the library with technique
+                                  AUTO (timed samples for joins of 60,000 probes or more, else
+                                  128 bits for mean set sizes <= 48 and 256 above), no signature
+                                  filter with an explicit technique */
     uint32_t count_only;       /* 1 = count result pairs, do not materialise them */
-    uint32_t verify_mode;      /* 0 = auto, 1 = one lane per candidate, 2 = one warp per candidate,
+    uint32_t verify_mode;      /* 0 = auto (a lane per candidate, or a warp per candidate where
+                                  the samples that choose the signature width show it faster),
+                                  1 = one lane per candidate, 2 = one warp per candidate,
                                   3 = one lane per candidate from staged prefixes (explicit candidate
                                   lists; joins treat it as 1) */
     uint32_t sort_pairs;       /* 1 = return pairs sorted by (first, second) */
