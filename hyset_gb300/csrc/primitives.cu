@@ -285,10 +285,10 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 // its set from one ballot (the sets ending before the round) and one OR of the
 // positions where sets start inside the round.  Every lane
 // carries an entry in every round (prefixes are far shorter than 32), the
-// stores coalesce, and the token loads of EMIT_ROUNDS rounds are issued before
+// stores coalesce, and the token loads of EMIT_ROUNDS (8) rounds are issued before
 // any of their stores.  Sets [lo, c.n): c, off and len are indexed by absolute
 // set id.  counts may be nullptr (no histogram).
-constexpr int EMIT_ROUNDS = 4;
+constexpr int EMIT_ROUNDS = 8;
 __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
                               uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit) {
