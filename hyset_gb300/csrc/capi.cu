@@ -239,8 +239,10 @@ int key_bits_for(uint32_t universe) {
 }
 
 // Global inverted index over the prefix entries of every set, lists ordered by
-// set id: histogram + scan give the list offsets, a stable radix sort by token
-// of the entries (emitted in set order) gives the order inside each list.
+// set id: histogram + scan give the list offsets; the entries (emitted in set
+// order) go into their lists by atomic slots and each list is put back in set
+// order in shared memory when every list is short, or by a stable radix sort
+// by token otherwise (index_lists).
 // pre / d_pre: the prefix length table (default: the bounds' index prefix);
 // force_pb >= 0 fixes the layout (0 = unpacked, > 0 = packed with that many
 // position bits) so that two indexes of one join share it.
