@@ -1,0 +1,464 @@
+// pipeline.cu — calls whose input arrives from host memory in chunks while
+// the device already works on the chunks that have landed: the text reader
+// (hyset_collection_parse) and the upload + self-join in one call
+// (hyset_self_join_host).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "host.h"
+
+namespace hs {
+
+namespace {
+constexpr uint64_t PIPE_CHUNK_TOKENS = 16ull << 20;  // 64 MB of tokens per copy chunk
+}  // namespace
+
+cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k) {
+    while (ctx->pipe_ev.size() <= k) {
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+        ctx->pipe_ev.push_back(e);
+    }
+    return ctx->pipe_ev[k];
+}
+
+}  // namespace hs
+
+using namespace hs;
+
+extern "C" {
+
+hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n_bytes, hyset_coll** out) {
+    if (!ctx || !out || (n_bytes && !text)) return fail(ctx, HYSET_E_INVALID, "null argument");
+    if (n_bytes >= (1ull << 33)) return fail(ctx, HYSET_E_UNSUPPORTED, "text of 2^33 bytes or more");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    // the text: used in place when it is device memory, else copied
+    const uint8_t* d_text = reinterpret_cast<const uint8_t*>(text);
+    DevBuf staged, counts, err;
+    struct Release {  // scratch goes back to the pool on every return path
+        DevBuf* b[3];
+        cudaStream_t s;
+        ~Release() {
+            for (DevBuf* d : b) d->release(s);
+        }
+    } rel{{&staged, &counts, &err}, s};
+    cudaPointerAttributes attr{};
+    if (cudaPointerGetAttributes(&attr, text) != cudaSuccess) cudaGetLastError();
+    // host text travels in 64 MB chunks on the auxiliary stream; the tiles of a
+    // chunk are counted once it and the next chunk (a tile reads one byte past
+    // its end) have landed, so counting overlaps the copy
+    constexpr uint64_t PARSE_CHUNK = 64ull << 20;  // a multiple of the 4 KiB tile
+    uint64_t n_chunks = 0;
+    if (n_bytes && attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged) {
+        CK(staged.ensure(n_bytes + 16, s));
+        CK(cudaEventRecord(ctx->ev_fork, s));
+        CK(cudaStreamWaitEvent(ctx->aux, ctx->ev_fork, 0));
+        n_chunks = (n_bytes + PARSE_CHUNK - 1) / PARSE_CHUNK;
+        for (uint64_t k = 0; k < n_chunks; ++k) {
+            const uint64_t b0 = k * PARSE_CHUNK, b1 = std::min(n_bytes, b0 + PARSE_CHUNK);
+            CK(cudaMemcpyAsync(staged.as<uint8_t>() + b0, text + b0, b1 - b0, cudaMemcpyHostToDevice, ctx->aux));
+            cudaEvent_t e = pipe_event(ctx, k);
+            if (!e) {
+                cudaStreamSynchronize(ctx->aux);
+                return fail(ctx, HYSET_E_CUDA, "event creation");
+            }
+            CK(cudaEventRecord(e, ctx->aux));
+        }
+        d_text = staged.as<uint8_t>();
+    }
+    if (n_bytes && (reinterpret_cast<uintptr_t>(d_text) & 15u)) {  // tiles load 16-byte words
+        DevBuf aligned;
+        CK(aligned.ensure(n_bytes + 16, s));
+        CK(cudaMemcpyAsync(aligned.p, d_text, n_bytes, cudaMemcpyDeviceToDevice, s));
+        staged.release(s);
+        staged = aligned;
+        aligned.p = nullptr;
+        d_text = staged.as<uint8_t>();
+    }
+    const uint64_t tiles = parse_tiles(n_bytes);
+    CK(counts.ensure((2 * tiles + 2) * 4 + (2 * n_chunks + 2) * 4, s));
+    CK(err.ensure(16, s));
+    uint32_t* tile_toks = counts.as<uint32_t>();
+    uint32_t* tile_lines = tile_toks + tiles + 1;
+    uint32_t* carry = tile_lines + tiles + 1;  // per chunk: tokens and lines before it
+    uint32_t* flags = err.as<uint32_t>();
+    unsigned long long* first_bad = reinterpret_cast<unsigned long long*>(err.as<uint8_t>() + 8);
+    CK(cudaMemsetAsync(flags, 0, 8, s));
+    CK(cudaMemsetAsync(first_bad, 0xFF, 8, s));
+    CK(cudaMemsetAsync(tile_toks, 0, (2 * tiles + 2) * 4 + (2 * n_chunks + 2) * 4, s));
+    uint32_t* h = ctx->h_flags + 8;  // [0] flags, [2..3] first bad offset, [4] tokens, [5] lines
+    auto parse_error = [&](uint32_t f, unsigned long long at) {
+        char msg[160];
+        const char* what = (f & PARSE_E_CHAR) ? "unexpected byte"
+                           : (f & PARSE_E_EMPTY_ITEM) ? "empty item (two spaces, a leading space or a space before CR)"
+                           : (f & PARSE_E_LINE_END) ? "CR not ending a line, or a line of only CR"
+                                                    : "number of more than 10 digits or >= 2^32";
+        std::snprintf(msg, sizeof msg, "parse error at byte %llu: %s", at, what);
+        return fail(ctx, HYSET_E_INVALID, msg);
+    };
+    auto c = std::make_unique<hyset_coll>();
+    c->ctx = ctx;
+    struct CollGuard {  // the collection's buffers go back on every early return
+        hyset_ctx* ctx;
+        std::unique_ptr<hyset_coll>& c;
+        ~CollGuard() {
+            if (c) hyset_collection_free(ctx, c.release());
+        }
+    } cguard{ctx, c};
+    uint32_t n_tokens = 0, n_lines = 0;
+    if (n_chunks) {
+        // each chunk is counted, scanned on top of the previous chunks' totals
+        // and emitted as soon as it and the next chunk have landed, so the
+        // whole parse overlaps the copy.  The output is sized from the first
+        // chunk's density (one wait); a text denser further on overflows that
+        // estimate and is emitted again at its exact size.
+        const uint64_t per = PARSE_CHUNK / 4096;  // tiles per chunk
+        uint32_t tok_cap = 0, line_cap = 0;
+        for (uint64_t k = 0; k < n_chunks; ++k) {
+            CK(cudaStreamWaitEvent(s, pipe_event(ctx, std::min(k + 1, n_chunks - 1)), 0));
+            CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s, k * per, (k + 1) * per));
+            CK(parse_chunk_scan(tile_toks, tile_lines, k * per, std::min(tiles, (k + 1) * per), carry, k, s));
+            if (k == 0) {
+                CK(cudaMemcpyAsync(h + 4, carry + 2, 8, cudaMemcpyDeviceToHost, s));
+                CK(cudaStreamSynchronize(s));
+                const double scale = (double)n_bytes / (double)std::min<uint64_t>(n_bytes, PARSE_CHUNK);
+                const double bound = (double)(n_bytes / 2 + 2);  // a token or a line takes two bytes
+                tok_cap = (uint32_t)std::min({bound, 1.25 * scale * h[4] + 4096.0, 4294967295.0});
+                line_cap = (uint32_t)std::min({bound, 1.25 * scale * h[5] + 4096.0, 4294967295.0});
+                CK(c->tokens.ensure((size_t)tok_cap * 4 + 4, s));
+                CK(c->starts.ensure((size_t)line_cap * 4 + 4, s));
+            }
+            CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(),
+                          flags, first_bad, s, k * per, (k + 1) * per, tok_cap, line_cap));
+        }
+        CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 4, carry + 2 * n_chunks, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h[0] & ~PARSE_E_CAPACITY) return parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        n_tokens = h[4];
+        n_lines = h[5];
+        if (h[0] & PARSE_E_CAPACITY) {  // the estimate was short: every tile again, exact sizes
+            CK(c->tokens.ensure((size_t)n_tokens * 4 + 4, s));
+            CK(c->starts.ensure((size_t)n_lines * 4 + 4, s));
+            CK(cudaMemsetAsync(flags, 0, 4, s));
+            CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(),
+                          flags, first_bad, s));
+        }
+        c->n = n_lines;
+        c->n_tokens = n_tokens;
+        CK(c->sizes.ensure((size_t)n_lines * 4 + 4, s));
+    } else {
+        CK(parse_count(d_text, n_bytes, tile_toks, tile_lines, flags, first_bad, s));
+        CK(ctx->sc->scan.ensure(scan_scratch_words(tiles + 1) * 4, s));
+        CK(scan_exclusive(tile_toks, tile_toks, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+        CK(scan_exclusive(tile_lines, tile_lines, tiles + 1, ctx->sc->scan.as<uint32_t>(), s));
+        CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 4, tile_toks + tiles, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + 5, tile_lines + tiles, 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if (h[0]) return parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        n_tokens = h[4];
+        n_lines = h[5];
+        c->n = n_lines;
+        c->n_tokens = n_tokens;
+        CK(c->tokens.ensure((size_t)n_tokens * 4 + 4, s));
+        CK(c->starts.ensure((size_t)n_lines * 4 + 4, s));
+        CK(c->sizes.ensure((size_t)n_lines * 4 + 4, s));
+        CK(parse_emit(d_text, n_bytes, tile_toks, tile_lines, c->tokens.as<uint32_t>(), c->starts.as<uint32_t>(),
+                      flags, first_bad, s));
+    }
+    CK(parse_line_sizes(c->starts.as<uint32_t>(), n_lines, n_tokens, c->starts.as<uint32_t>(),
+                        c->sizes.as<uint32_t>(), s));
+    CK(cudaMemcpyAsync(h, err.p, 16, cudaMemcpyDeviceToHost, s));
+    c->d_tokens = c->tokens.as<uint32_t>();
+    c->d_starts = c->starts.as<uint32_t>();
+    c->d_sizes = c->sizes.as<uint32_t>();
+    // the collection checks go behind the parse on the stream: one synchronisation
+    hyset_status stt = enqueue_collection_checks(ctx, c.get(), nullptr);
+    if (stt == HYSET_OK) {
+        CK(cudaStreamSynchronize(s));
+        if (h[0]) stt = parse_error(h[0], *reinterpret_cast<unsigned long long*>(h + 2));
+        else stt = finish_collection_checks(ctx, c.get(), nullptr);
+    }
+    if (stt != HYSET_OK) {
+        hyset_collection_free(ctx, c.release());
+        return stt;
+    }
+    *out = c.release();
+    return HYSET_OK;
+}
+
+// The upload and the self-join in one call.  The tokens go to the device in
+// 64 MB chunks on the auxiliary stream; while the later chunks are in flight,
+// the sets of the chunks already on the device are checked, their prefix
+// entries emitted and their signatures generated on the context's stream.
+// After the last chunk only the index sort and the join launch remain.  The
+// pipeline needs the join's configuration before the tokens arrive: an explicit
+// probe-major prefix-index join, or one whose technique and signature width
+// the context has already chosen for a collection with the same size profile;
+// every other join runs as hyset_collection_upload + hyset_self_join.
+hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64_t n_tokens, const uint32_t* starts,
+                                  const uint32_t* sizes, uint32_t n_sets, const hyset_join_opts* opts,
+                                  hyset_coll** coll_out, hyset_result** out) {
+    if (!ctx || !out || !opts || (n_sets && (!sizes || (!tokens && n_tokens))))
+        return fail(ctx, HYSET_E_INVALID, "null argument");
+    *out = nullptr;
+    if (coll_out) *coll_out = nullptr;
+    ST(check_opts(ctx, opts));
+    if (n_tokens >= (1ull << 32)) return fail(ctx, HYSET_E_INVALID, "n_tokens must be < 2^32");
+    if (opts->probe_end) return fail(ctx, HYSET_E_INVALID, "probe ranges need an uploaded collection");
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream, cp = ctx->aux;
+    auto res = std::make_unique<hyset_result>();
+    auto c = std::make_unique<hyset_coll>();
+    c->ctx = ctx;
+    c->n = n_sets;
+    c->n_tokens = n_tokens;
+    hyset_coll* C = c.get();
+    auto bail = [&](hyset_status st) {
+        cudaStreamSynchronize(cp);
+        hyset_collection_free(ctx, c.release());
+        return st;
+    };
+    const unsigned long long launches0 = launches();
+    CK(cudaEventRecord(ctx->ev0, s));
+    if (C->tokens.ensure(n_tokens * 4 + 4, s) != cudaSuccess || C->starts.ensure((size_t)n_sets * 4 + 4, s) ||
+        C->sizes.ensure((size_t)n_sets * 4 + 4, s) || C->meta.ensure((size_t)n_sets * sizeof(uint2) + 8, s))
+        return bail(fail(ctx, HYSET_E_NOMEM, "device allocation"));
+    C->d_tokens = C->tokens.as<uint32_t>();
+    C->d_starts = C->starts.as<uint32_t>();
+    C->d_sizes = C->sizes.as<uint32_t>();
+    // 1. on the copy stream: the sizes (and starts, when given) first, then every
+    //    token chunk with an event after each; the sizes go first so the
+    //    per-set work is not queued behind the tokens on the copy engine
+    CK(cudaEventRecord(ctx->ev_fork, s));
+    CK(cudaStreamWaitEvent(cp, ctx->ev_fork, 0));
+    const bool starts_given = starts != nullptr;
+    if (n_sets) {
+        CK(cudaMemcpyAsync(C->sizes.p, sizes, (size_t)n_sets * 4, cudaMemcpyHostToDevice, cp));
+        if (starts_given) CK(cudaMemcpyAsync(C->starts.p, starts, (size_t)n_sets * 4, cudaMemcpyHostToDevice, cp));
+    }
+    CK(cudaEventRecord(ctx->ev_join, cp));
+    CK(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+    if (!starts_given && n_sets) {  // contiguous sets: starts are the exclusive scan of the sizes
+        CK(ctx->sc->scan.ensure(scan_scratch_words(n_sets) * 4, s));
+        CK(scan_exclusive(C->d_sizes, C->starts.as<uint32_t>(), n_sets, ctx->sc->scan.as<uint32_t>(), s));
+    }
+    const uint64_t n_chunks = n_tokens ? (n_tokens + PIPE_CHUNK_TOKENS - 1) / PIPE_CHUNK_TOKENS : 0;
+    for (uint64_t k = 0; k < n_chunks; ++k) {
+        const uint64_t t0 = k * PIPE_CHUNK_TOKENS, t1 = std::min(n_tokens, t0 + PIPE_CHUNK_TOKENS);
+        CK(cudaMemcpyAsync(C->tokens.as<uint32_t>() + t0, tokens + t0, (t1 - t0) * 4, cudaMemcpyHostToDevice, cp));
+        cudaEvent_t e = pipe_event(ctx, k);
+        if (!e) return bail(fail(ctx, HYSET_E_CUDA, "event creation"));
+        CK(cudaEventRecord(e, cp));
+    }
+    // 2. on the host meanwhile, one pass over the sizes: contiguity of the given
+    //    starts, size order, and for every chunk the first set that ends past it
+    //    (sets before it are complete once the chunk has landed)
+    bool contiguous = true, ordered = true;
+    std::vector<uint32_t> chunk_hi(n_chunks, n_sets);
+    {
+        uint64_t run = 0, bound = PIPE_CHUNK_TOKENS, k = 0;
+        uint32_t prev = 0;
+        for (uint32_t i = 0; i < n_sets; ++i) {
+            const uint32_t z = sizes[i];
+            if (starts_given) contiguous &= starts[i] == run;
+            ordered &= z >= prev;
+            prev = z;
+            const uint64_t end = run + z;
+            while (k < n_chunks && end > bound) {
+                chunk_hi[k++] = i;
+                bound += PIPE_CHUNK_TOKENS;
+            }
+            run = end;
+        }
+        if (!starts_given && run > n_tokens) return bail(fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens"));
+    }
+    if (!ordered) return bail(fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size"));
+    ST(build_size_meta(ctx, C, sizes));
+    // 3. the configuration, from the options or the context's earlier choices
+    const hyset_join_opts* o = opts;
+    bool pipelined = contiguous && n_sets > 0;
+    hyset_technique selected = HYSET_TECH_AUTO;
+    int selector = -1;
+    const std::string key = join_key(C, C, o);
+    if (o->technique == HYSET_TECH_AUTO) {
+        auto it = ctx->select_cache.find(key);
+        if (it == ctx->select_cache.end()) pipelined = false;
+        else {
+            selected = it->second.first;
+            selector = it->second.second;
+        }
+    }
+    Tuned tn = tune(C, C, o, selected);
+    if (tn.tech != HYSET_TECH_FGSS || !tn.probe_major) pipelined = false;
+    if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && n_sets >= TUNE_MIN_PROBES) {
+        auto it = ctx->bits_cache.find(key);
+        if (it == ctx->bits_cache.end()) pipelined = false;
+        else {
+            tn.bits = it->second & 0xFFFFu;
+            if (!o->verify_mode && (it->second >> 16)) tn.vmode = (int)(it->second >> 16);
+        }
+    }
+    Bounds* b = nullptr;
+    ST(get_bounds(ctx, o->sim, o->threshold, C->max_size, 0, &b));
+    uint32_t max_pre = 1;
+    for (size_t l = 0; l < C->size_hist.size(); ++l)
+        if (C->size_hist[l]) max_pre = std::max(max_pre, b->index_prefix[l]);
+    const uint32_t pb = bits_for(max_pre);
+    const uint64_t E = prefix_entries(C, b->index_prefix);
+    if (pb + bits_for(n_sets) > 32 || E >= (1ull << 32)) pipelined = false;  // packed layout only
+    if (!pipelined) {
+        // the plain sequence: all tokens, the checks, then the join
+        CK(cudaStreamWaitEvent(s, pipe_event(ctx, n_chunks ? n_chunks - 1 : 0), 0));
+        hyset_status stt = enqueue_collection_checks(ctx, C, sizes);
+        if (stt == HYSET_OK) {
+            CK(cudaStreamSynchronize(s));
+            stt = finish_collection_checks(ctx, C, sizes);
+        }
+        if (stt == HYSET_OK) stt = do_join(ctx, C, C, o, res.get());
+        if (stt != HYSET_OK) return bail(stt);
+    } else {
+        // 4. per chunk: checks, prefix entries (no histogram yet) and signatures
+        const uint32_t n = n_sets;
+        CK(ctx->sc->len.ensure((size_t)n * 4 + 4, s));
+        CK(ctx->sc->off.ensure((size_t)n * 4 + 4, s));
+        CK(ctx->sc->tok.ensure(E ? E * 4 : 4, s));
+        CK(ctx->sc->altk.ensure(E ? E * 4 : 4, s));
+        CK(ctx->sc->altv.ensure(E ? E * 4 : 4, s));
+        CK(ctx->sc->gate.ensure(4, s));
+        Index& ix = C->index;
+        CK(ix.set.ensure(E ? E * 4 : 4, s));
+        CK(ix.pos.ensure(4, s));
+        CK(ctx->s_flags.ensure(16, s));
+        CK(cudaMemsetAsync(ctx->s_flags.p, 0, 16, s));
+        const size_t scan_words = std::max(scan_scratch_words(n), radix_scratch_words(E ? E : 1));
+        CK(ctx->sc->scan.ensure(scan_words * 4, s));
+        uint32_t* len = ctx->sc->len.as<uint32_t>();
+        uint32_t* off = ctx->sc->off.as<uint32_t>();
+        CollView v = C->view();
+        CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
+        CK(scan_exclusive(len, off, n, ctx->sc->scan.as<uint32_t>(), s));
+        const int words = (int)(tn.bits / 64);
+        DevBuf& bits = C->bitmaps[words];
+        if (words) CK(bits.ensure((size_t)n * words * 8 + 8, s));
+        // A collection with the same size profile joined before: its universe
+        // is assumed, so the token histogram is counted as the chunks land and
+        // the checks are read after the join (one synchronisation); a larger
+        // token than assumed means the index is built again and the join re-run.
+        const std::string ukey = coll_signature(C);
+        auto uit = ctx->universe_cache.find(ukey);
+        bool assumed = uit != ctx->universe_cache.end();
+        uint32_t U = assumed ? uit->second : 0;
+        uint32_t* counts = nullptr;
+        if (assumed) {
+            CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
+            counts = ctx->sc->counts.as<uint32_t>();
+            CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+        }
+        uint32_t lo = 0;
+        for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
+            // sets whose tokens end inside the chunks copied so far
+            const uint32_t hi = k + 1 == n_chunks ? n : std::max(lo, chunk_hi[k]);
+            CK(cudaStreamWaitEvent(s, pipe_event(ctx, k), 0));
+            if (hi <= lo) continue;
+            CollView part = v;
+            part.sizes += lo;
+            part.starts += lo;
+            part.meta += lo;
+            part.n = hi - lo;
+            CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
+            CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s, lo,
+                                   hi, U + 1));
+            if (words) CK(generate_bitmaps(part, words, bits.as<uint64_t>() + (size_t)lo * words, s));
+            lo = hi;
+        }
+        if (n_chunks) CK(cudaStreamWaitEvent(s, pipe_event(ctx, n_chunks - 1), 0));  // every copy has landed
+        // 5. the index and the join.  The universe (largest token + 1) sizes the
+        //    list offsets: assumed (above), or read with the checks.
+        uint32_t* f = ctx->h_flags;
+        auto verdict = [&]() -> hyset_status {
+            if (f[0] & 8) return fail(ctx, HYSET_E_INVALID, "a set reaches past the end of the token array");
+            if (f[0] & 1) return fail(ctx, HYSET_E_INVALID, "empty set in collection");
+            if (f[0] & 2) return fail(ctx, HYSET_E_INVALID, "set tokens must be strictly ascending");
+            if (f[1] == 0xFFFFFFFFu) return fail(ctx, HYSET_E_INVALID, "token 0xFFFFFFFF is reserved");
+            return HYSET_OK;
+        };
+        if (!assumed) {
+            CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            const hyset_status vs = verdict();
+            if (vs != HYSET_OK) return bail(vs);
+            U = f[1] + 1;
+        }
+        JoinParams P{};
+        for (int attempt = 0; attempt < 2; ++attempt) {
+            C->universe = U;
+            CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
+            CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
+            CK(ctx->sc->scan.ensure(std::max(scan_words, scan_scratch_words((uint64_t)U + 1)) * 4, s));
+            if (attempt > 0)  // the list build reordered the entries: emit them again
+                CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr, s));
+            counts = ctx->sc->counts.as<uint32_t>();
+            if (!(assumed && attempt == 0)) {  // not counted while the chunks landed
+                CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+                CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
+            }
+            CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts,
+                           ix.list_off.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(),
+                           ctx->sc->gate.as<uint32_t>(), key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));
+            ix.sim = b->sim;
+            ix.tau = b->tau;
+            ix.kind = 0;
+            ix.universe = U;
+            ix.entries = E;
+            ix.pos_bits = pb;
+            P = JoinParams{};
+            P.R = C->view();
+            P.S = P.R;
+            P.B = b->view;
+            P.first_ge = C->first_ge.as<uint32_t>();
+            P.R_L = C->max_size;
+            P.self = 1;
+            P.grab = std::min<uint32_t>(tn.batch, 32);
+            P.p_lo = 0;
+            P.p_hi = n;
+            P.r_lo = 0;
+            P.r_hi = n;
+            P.X = ix.view();
+            if (words) {
+                P.bits_R = P.bits_S = bits.as<uint64_t>();
+                P.words = words;
+            }
+            if (assumed) CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+            const hyset_status js = run_join(ctx, P, TECH_FGSS, tn.vmode, o, res.get(), true);  // synchronises
+            if (js != HYSET_OK) return bail(js);
+            if (!assumed) break;
+            const hyset_status vs = verdict();
+            if (vs != HYSET_OK) return bail(vs);
+            if (f[1] + 1 <= U) break;  // every token was indexed: the join stands
+            U = f[1] + 1;              // a larger token: index and join again
+            assumed = false;
+        }
+        C->universe = f[1] + 1;
+        ctx->universe_cache[ukey] = C->universe;
+        res->technique = HYSET_TECH_FGSS;
+        res->bitmap_bits = tn.bits;
+        res->verify_mode = (uint32_t)tn.vmode;
+        res->selector = selector;
+        if (o->collect_stats) res->stats[3] = E;
+        res->launches = launches() - launches0;
+    }
+    if (coll_out) *coll_out = c.release();
+    else hyset_collection_free(ctx, c.release());
+    *out = res.release();
+    return HYSET_OK;
+}
+
+}  // extern "C"
