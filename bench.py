@@ -177,6 +177,30 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def check_parity(ctx, coll, c, kw, p_lo, p_hi, sim):
+    """One untimed join with its pairs copied back, compared as a set with the
+    oracle's pairs of the same probe range; returns the parity record."""
+    import numpy as np
+    import oracle
+    q = dict(kw)
+    q["device_pairs"] = False
+    r = ctx.self_join(coll, **q)
+    threads = os.cpu_count() or 1
+    if (p_lo, p_hi) == (0, c.n):
+        exp = oracle.join_multi(c.tokens, c.starts, c.sizes, THRESHOLD, threads, sim=sim)
+    else:
+        exp = oracle.join_multi_range(c.tokens, c.starts, c.sizes, THRESHOLD, threads, (p_lo, p_hi - 1), sim=sim)
+
+    def keys(p):
+        p = np.asarray(p, np.uint64).reshape(-1, 2)
+        return np.sort((p[:, 0] << np.uint64(32)) | p[:, 1])
+
+    got, want = keys(r.pairs), keys(exp)
+    ok = bool(got.size == r.count and np.array_equal(got, want))
+    return {"parity": ok, "pairs": int(r.count), "oracle_pairs": int(want.size),
+            "checked_against": f"oracle restatement of host::allpairs, probes [{p_lo}, {p_hi}), {threads} threads"}
+
+
 def shard(n, ws, rank):
     """Probe range of this rank: sqrt split (later probes have longer candidate windows)."""
     import math
@@ -209,8 +233,10 @@ def run_ours(args, ws, rank, local):
         if dist is not None:
             dist.barrier()
 
-    # untimed: work counters for the roofline, and a parity spot check of the shard
+    # untimed: work counters for the roofline, and the shard's pair set against
+    # the oracle (the reference's host::allpairs restated, all host threads)
     st_run = ctx.self_join(coll, collect_stats=True, **kw)
+    parity = check_parity(ctx, coll, c, kw, p_lo, p_hi, args.sim)
     for _ in range(args.warmup):
         ctx.self_join(coll, **kw)
     barrier()
@@ -272,6 +298,24 @@ def run_ours(args, ws, rank, local):
         e2e_mean = float(t[0])
     e2e_value = total_pairs / e2e_mean
 
+    # attribution of the headline (collection resident, L2 flushed, median of
+    # five): the plain single-launch path (probe-major prefix filter, no
+    # signatures, a lane per candidate, one probe per warp batch: no tuning at
+    # all) and the autotuner's configuration (signature width, verification
+    # mode, probe batch) forced explicitly, beside AUTO (selector + autotuner)
+    def leg_ms(q, reps=5):
+        ms = []
+        for _ in range(reps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            ms.append(ctx.self_join(coll, **q).device_ms)
+        return statistics.median(ms)
+
+    plain_kw = dict(kw, technique="fgss", probe_major=True, bitmap=0, verify_mode=1, fgss_batch=1)
+    tuned_kw = dict(kw, technique="fgss", probe_major=True, bitmap=r.bitmap_bits, verify_mode=r.verify_mode,
+                    fgss_batch=r.probe_batch or 0)
+    legs = {"plain_single_launch_ms": leg_ms(plain_kw), "autotuned_ms": leg_ms(tuned_kw), "auto_ms": leg_ms(kw)}
+
     out = None
     if rank == 0:
         # the plain reference-shaped path: block pairs of 10,000 sets, one launch each
@@ -308,9 +352,13 @@ def run_ours(args, ws, rank, local):
                           "result_pairs": total_pairs,
                           "parallelism": f"probe shards x{ws}" if ws > 1 else "single GPU",
                           "l2": "512 MB buffer written between timed steps; tokens 449 MB > L2",
+                          "probe_batch": r.probe_batch, "selector": r.selector,
                           "plain_block_pair_ms": plain_ms,
-                          "speedup_vs_plain": plain_ms / step_ms if plain_ms else None,
+                          "speedup_vs_block_pair": plain_ms / step_ms if plain_ms else None,
+                          **legs,
+                          "speedup_vs_plain_single_launch": legs["plain_single_launch_ms"] / legs["auto_ms"],
                           "kernel_ms": kms},
+               "parity": parity["parity"], "parity_detail": parity,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                             "algorithmic_bytes_per_launch": alg, "kernel": "k_join (probe-major FGSS filter + verify, persistent)"},
@@ -320,45 +368,11 @@ def run_ours(args, ws, rank, local):
                "clocks": clocks, "gpu_launches": launches}
         print(json.dumps(out), flush=True)
     coll.free()
+    if not parity["parity"]:
+        sys.exit(f"parity failure: {parity}")
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
-    return out
-
-
-def batch_workload(n_joins=256, seed=0x5E7B):
-    """R-S joins of uneven sizes: |R|, |S| log-uniform in [1e3, 2e5], Zipf s in
-    [0.7, 1.3], mean set size log-uniform in [8, 300], universe 5e4..5e5,
-    threshold in [0.5, 0.95], similarity Jaccard / cosine / dice in turn.  R and
-    S of a join are a random split of one generated collection, so near-duplicate
-    sets fall on both sides."""
-    import math
-    import numpy as np
-    from hyset_gb300 import synth
-    rng = np.random.default_rng(seed)
-    sims = ["jaccard", "cosine", "dice"]
-    out = []
-    for j in range(n_joins):
-        nr = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
-        ns = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
-        mean = math.exp(rng.uniform(math.log(8), math.log(300)))
-        c = synth.generate(synth.C2, n_sets=nr + ns, universe=int(rng.uniform(5e4, 5e5)),
-                           zipf_s=float(rng.uniform(0.7, 1.3)), size_dist=synth.LOGNORMAL,
-                           size_a=math.log(mean) - 0.125, size_b=0.5, size_min=2,
-                           size_max=min(2000, max(16, int(mean * 6))), dup_frac=0.05, dup_edit_lo=0.02,
-                           dup_edit_hi=0.12, seed=int(rng.integers(1, 2**31)))
-        side = rng.random(c.n) < nr / (nr + ns)
-        parts = []
-        for mask in (side, ~side):
-            ids = np.nonzero(mask)[0]
-            sizes = c.sizes[ids]
-            starts = np.zeros(len(ids), np.uint32)
-            if len(ids):
-                starts[1:] = np.cumsum(sizes[:-1])
-            sz64 = sizes.astype(np.int64)
-            src = np.repeat(c.starts[ids].astype(np.int64) - starts.astype(np.int64), sz64) + np.arange(sz64.sum())
-            parts.append((c.tokens[src], starts, sizes))
-        out.append((parts[0], parts[1], dict(threshold=float(rng.uniform(0.5, 0.95)), sim=sims[j % 3])))
     return out
 
 
@@ -366,7 +380,8 @@ def run_batch(args):
     import torch
     import hyset_gb300 as hs
     t0 = time.time()
-    work = batch_workload(args.joins)
+    from hyset_gb300 import synth
+    work = synth.batch_workload(args.joins)
     gen_s = time.time() - t0
     ctx = hs.Context(0)
     joins, colls = [], []

@@ -89,9 +89,10 @@ def build_synth(force: bool = False) -> str:
 def build_oracle(force: bool = False) -> None:
     odir = os.path.join(ROOT, "oracle")
     _run(["make", "-C", odir] + (["-B"] if force else []) + ["liboracle.so"])
-    ref = os.environ.get("HYSET_REFERENCE_ROOT", "/root/reference")
-    if os.path.isdir(os.path.join(ref, "include", "hyset")):
-        _run(["make", "-C", odir, f"REFROOT={ref}", "ref"])
+    # the reference's own host join, where its source tree exists (the recipe
+    # in oracle/Makefile knows where it lies; HYSET_REFERENCE_ROOT overrides)
+    ref = os.environ.get("HYSET_REFERENCE_ROOT")
+    _run(["make", "-C", odir] + ([f"REFROOT={ref}"] if ref else []) + ["ref-if-present"])
 
 
 def build_all(force: bool = False, verbose: bool = False) -> None:

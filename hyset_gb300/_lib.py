@@ -58,6 +58,7 @@ PROTOTYPES = {
     "hyset_destroy": (None, [C.c_void_p]),
     "hyset_last_error": (C.c_char_p, [C.c_void_p]),
     "hyset_default_opts": (None, [C.POINTER(JoinOpts)]),
+    "hyset_device_bytes": (C.c_uint64, []),
     "hyset_collection_upload": (C.c_int, [C.c_void_p, U32P, C.c_uint64, U32P, U32P, C.c_uint32,
                                           C.POINTER(C.c_void_p)]),
     "hyset_collection_from_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
@@ -79,6 +80,7 @@ PROTOTYPES = {
     "hyset_result_technique": (C.c_int, [C.c_void_p]),
     "hyset_result_bitmap_bits": (C.c_uint32, [C.c_void_p]),
     "hyset_result_verify_mode": (C.c_uint32, [C.c_void_p]),
+    "hyset_result_probe_batch": (C.c_uint32, [C.c_void_p]),
     "hyset_result_split": (C.c_uint32, [C.c_void_p, C.POINTER(C.c_int)]),
     "hyset_result_device_ms": (C.c_double, [C.c_void_p]),
     "hyset_result_kernel_ms": (C.c_double, [C.c_void_p]),

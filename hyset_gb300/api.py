@@ -34,6 +34,7 @@ class JoinResult:
     split_at: int = 0           # partition split: first probe id of the high range (0 = none)
     split_low: str = ""         # the low range's technique when split
     verify_mode: int = 0        # 1 lane per candidate, 2 warp per candidate, 3 staged (candidate lists)
+    probe_batch: int = 0        # probes per warp batch of the probe-major prefix kernel (0: another kernel)
 
 
 # R-S joins: which collection is indexed (hyset_join_opts.orientation)
@@ -79,7 +80,7 @@ def _take_result(lib, r) -> JoinResult:
                           [int(st[i]) for i in range(k)], int(lib.hyset_result_device_pairs(r) or 0),
                           int(lib.hyset_result_launches(r)), SELECTOR_NAMES.get(lib.hyset_result_selector(r), "?"),
                           int(lib.hyset_result_bitmap_bits(r)), *_split(lib, r),
-                          int(lib.hyset_result_verify_mode(r)))
+                          int(lib.hyset_result_verify_mode(r)), int(lib.hyset_result_probe_batch(r)))
     finally:
         lib.hyset_result_free(r)
 
@@ -135,7 +136,11 @@ class Context:
         self.selector_info = None
         if selector:
             from . import selector as _sel
-            self.selector_info = _sel.install_shipped(self)
+            try:
+                self.selector_info = _sel.install_shipped(self)
+            except Exception:
+                self.close()
+                raise
 
     def close(self):
         if self.handle:

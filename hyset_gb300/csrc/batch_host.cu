@@ -22,9 +22,9 @@ std::string opts_key(const hyset_join_desc& d) {
 }
 }  // namespace
 
-void batch_release(hyset_ctx* ctx) {
-    if (!ctx->batch) return;
-    BatchPlan& bp = *ctx->batch;
+namespace {
+// Gives back every buffer and graph of a plan (installed or not).
+void release_plan(hyset_ctx* ctx, BatchPlan& bp) {
     cudaStream_t s = ctx->stream;
     if (bp.exec) cudaGraphExecDestroy(bp.exec);
     if (bp.graph) cudaGraphDestroy(bp.graph);
@@ -37,6 +37,12 @@ void batch_release(hyset_ctx* ctx) {
     for (DevBuf* d : bufs) d->release(s);
     bp.sc.release(s);
     cudaStreamSynchronize(s);
+}
+}  // namespace
+
+void batch_release(hyset_ctx* ctx) {
+    if (!ctx->batch) return;
+    release_plan(ctx, *ctx->batch);
     ctx->batch.reset();
 }
 
@@ -72,6 +78,9 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
     if (ctx->batch && ctx->batch->sig == sig) return HYSET_OK;  // same batch: replay its graph
     batch_release(ctx);
     auto plan = std::make_unique<BatchPlan>();
+    auto guard = on_exit([&] {  // a plan that failed before it was installed gives its memory back
+        if (plan) release_plan(ctx, *plan);
+    });
     plan->sig = sig;
     // index builds of the batch use the plan's own scratch, so later joins that
     // grow the context's scratch cannot free memory the graph still addresses
@@ -111,7 +120,8 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
             const uint32_t a_lo = o->probe_end ? o->probe_begin : 0, a_hi = o->probe_end ? o->probe_end : S->n;
             if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && tn.tech == HYSET_TECH_FGSS &&
                 a_hi - a_lo >= TUNE_MIN_PROBES)
-                ST(autotune_bits(ctx, R, S, o, bj->b, bj->self, a_lo, a_hi, &tn.bits));
+                ST(autotune_bits(ctx, R, S, o, bj->b, bj->self, a_lo, a_hi, &tn.bits, nullptr,
+                                 o->fgss_batch ? nullptr : &tn.batch));
         }
         bj->tech = tn.tech;
         bj->ktech = tn.tech == HYSET_TECH_FGSS ? TECH_FGSS : (tn.tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
@@ -168,6 +178,7 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         desc[j].tech = (uint32_t)bj->ktech;
         desc[j].words = (uint32_t)bj->words;
         desc[j].unit_probes = bj->ktech == TECH_FGSS ? std::min<uint32_t>(tn.batch, P.X2.set ? 16 : 32) : 1;
+        bj->unit_probes = bj->ktech == TECH_FGSS ? desc[j].unit_probes : 0;
         const uint32_t np = P.p_hi - P.p_lo;
         bj->units = (np + desc[j].unit_probes - 1) / desc[j].unit_probes;
         cost[j] = (double)np * (double)(R->n_tokens / std::max<uint32_t>(R->n, 1) + 1) *
@@ -277,6 +288,7 @@ hyset_status hyset_batch_join(hyset_ctx* ctx, const hyset_join_desc* joins, uint
         hyset_result* r = out[j].get();
         r->technique = bj.tech;
         r->bitmap_bits = (uint32_t)bj.words * 64u;
+        r->probe_batch = bj.unit_probes;
         r->device_ms = ms;  // the whole batch: one launch sequence
         r->count = counts[j];
         if (!bj.o.count_only && counts[j] > bj.cap) {

@@ -54,6 +54,9 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
         return HYSET_OK;
     }
     auto b = std::make_unique<Bounds>();
+    auto guard = on_exit([&] {  // tables that failed to upload give their memory back
+        if (b) b->dev.release(ctx->stream);
+    });
     b->sim = sim;
     b->tau = tau;
     b->L = L;

@@ -3,15 +3,39 @@
 // they drive: collection.cu, join_host.cu, pipeline.cu, batch_host.cu,
 // plan.cu, handlers.cu, verifier.cu, noalloc.cu.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
 #include "host.h"
 
 namespace hs {
+
+namespace {
+std::atomic<long long> g_device_bytes{0};
+std::mutex g_fault_mu;
+std::string g_fault_value;  // the HYSET_FAULT_ALLOC value the count started from
+long long g_fault_count = 0;
+}  // namespace
+
+unsigned long long device_bytes() { return (unsigned long long)g_device_bytes.load(); }
+void add_device_bytes(long long delta) { g_device_bytes += delta; }
+
+bool inject_alloc_failure() {
+    const char* v = std::getenv("HYSET_FAULT_ALLOC");
+    if (!v || !*v) return false;
+    std::lock_guard<std::mutex> lock(g_fault_mu);
+    if (g_fault_value != v) {
+        g_fault_value = v;
+        g_fault_count = 0;
+    }
+    return ++g_fault_count == std::atoll(v);
+}
 
 hyset_status fail(hyset_ctx* ctx, hyset_status st, const char* what, cudaError_t e) {
     if (ctx) {
@@ -111,6 +135,8 @@ void hyset_destroy(hyset_ctx* ctx) {
 
 const char* hyset_last_error(const hyset_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
 
+uint64_t hyset_device_bytes(void) { return device_bytes(); }
+
 uint64_t hyset_result_count(const hyset_result* r) { return r ? r->count : 0; }
 const hyset_pair* hyset_result_pairs(const hyset_result* r) {
     static const hyset_pair none = {0, 0};
@@ -121,6 +147,7 @@ uint64_t hyset_result_launches(const hyset_result* r) { return r ? r->launches :
 hyset_technique hyset_result_technique(const hyset_result* r) { return r ? r->technique : HYSET_TECH_AUTO; }
 uint32_t hyset_result_bitmap_bits(const hyset_result* r) { return r ? r->bitmap_bits : 0; }
 uint32_t hyset_result_verify_mode(const hyset_result* r) { return r ? r->verify_mode : 0; }
+uint32_t hyset_result_probe_batch(const hyset_result* r) { return r ? r->probe_batch : 0; }
 uint32_t hyset_result_split(const hyset_result* r, hyset_technique* low_technique) {
     if (low_technique) *low_technique = r ? r->split_low : HYSET_TECH_AUTO;
     return r ? r->split_at : 0;

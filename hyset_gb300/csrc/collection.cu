@@ -89,6 +89,9 @@ hyset_status hyset_collection_upload(hyset_ctx* ctx, const uint32_t* tokens, uin
     *out = nullptr;
     CK(cudaSetDevice(ctx->device));
     auto c = std::make_unique<hyset_coll>();
+    auto guard = on_exit([&] {  // a failed upload releases what it allocated
+        if (c) hyset_collection_free(ctx, c.release());
+    });
     c->ctx = ctx;
     c->n = n_sets;
     c->n_tokens = n_tokens;
@@ -115,11 +118,7 @@ hyset_status hyset_collection_upload(hyset_ctx* ctx, const uint32_t* tokens, uin
     c->d_tokens = c->tokens.as<uint32_t>();
     c->d_starts = c->starts.as<uint32_t>();
     c->d_sizes = c->sizes.as<uint32_t>();
-    hyset_status stt = make_collection(ctx, c.get(), sizes);
-    if (stt != HYSET_OK) {
-        hyset_collection_free(ctx, c.release());
-        return stt;
-    }
+    ST(make_collection(ctx, c.get(), sizes));
     *out = c.release();
     return HYSET_OK;
 }

@@ -32,6 +32,9 @@ hyset_status hyset_handler_create(hyset_ctx* ctx, const hyset_coll* coll, hyset_
         return fail(ctx, HYSET_E_INVALID, "bitmap size must be 64, 128, 256 or 512");
     CK(cudaSetDevice(ctx->device));
     auto h = std::make_unique<hyset_handler>();
+    auto guard = on_exit([&] {  // a failed creation releases what it allocated
+        if (h) hyset_handler_destroy(h.release());
+    });
     h->ctx = ctx;
     h->coll = coll;
     h->technique = technique;

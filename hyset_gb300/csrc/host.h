@@ -11,6 +11,18 @@
 
 namespace hs {
 
+// Runs f when the scope ends (cleanup of partially built objects on every
+// early return).
+template <typename F>
+struct OnExit {
+    F f;
+    ~OnExit() { f(); }
+};
+template <typename F>
+OnExit<F> on_exit(F f) {
+    return OnExit<F>{f};
+}
+
 // ---- errors (capi.cu) -------------------------------------------------------
 // Records `what` (and the CUDA error) as the context's last error; returns st.
 hyset_status fail(hyset_ctx* ctx, hyset_status st, const char* what, cudaError_t e = cudaSuccess);
@@ -65,6 +77,7 @@ hyset_status get_bitmaps(hyset_ctx* ctx, hyset_coll* c, int words, const uint64_
 
 // ---- configuration, selector, autotuner (plan.cu) ---------------------------
 constexpr uint32_t TUNE_MIN_PROBES = 60000;  // joins this large time samples to pick their configuration
+constexpr uint32_t DEFAULT_PROBE_BATCH = 3;  // probes per warp batch of the probe-major kernel, untuned
 hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o);
 struct Tuned {
     hyset_technique tech;
@@ -83,8 +96,11 @@ hyset_status select_technique(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, cons
                               hyset_technique* out, int* selector);
 hyset_status plan_split(hyset_ctx* ctx, hyset_coll* R, const hyset_join_opts* o, uint32_t* split_at,
                         hyset_technique* low, hyset_technique* high);
+// The autotuner: signature width (always), verification mode (vmode != NULL)
+// and probe batch (batch != NULL) of a prefix-index join from timed samples.
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
-                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode = nullptr);
+                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode = nullptr,
+                           uint32_t* batch = nullptr);
 
 // ---- joins (join_host.cu) -----------------------------------------------------
 hyset_status sort_device_pairs(hyset_ctx* ctx, uint2* pairs, uint64_t n, uint32_t n_probe, uint32_t n_indexed);

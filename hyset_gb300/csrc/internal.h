@@ -14,21 +14,41 @@
 
 namespace hs {
 
+// Device bytes held by the library's buffers (every DevBuf of every context).
+unsigned long long device_bytes();
+void add_device_bytes(long long delta);
+// Allocation-failure injection for tests: while the environment variable
+// HYSET_FAULT_ALLOC holds N, the N-th device allocation attempt counted from
+// when that value was first seen fails as cudaErrorMemoryAllocation.
+bool inject_alloc_failure();
+
 // Device allocation from the stream-ordered pool; grows, never shrinks.
 struct DevBuf {
     void* p = nullptr;
     size_t bytes = 0;
     cudaError_t ensure(size_t b, cudaStream_t s) {
         if (b <= bytes && p) return cudaSuccess;
-        if (p) cudaFreeAsync(p, s);
+        if (inject_alloc_failure()) return cudaErrorMemoryAllocation;
+        if (p) {
+            cudaFreeAsync(p, s);
+            add_device_bytes(-(long long)bytes);
+        }
         p = nullptr;
         bytes = 0;
         cudaError_t e = cudaMallocAsync(&p, b ? b : 16, s);
-        if (e == cudaSuccess) bytes = b ? b : 16;
+        if (e == cudaSuccess) {
+            bytes = b ? b : 16;
+            add_device_bytes((long long)bytes);
+        } else {
+            p = nullptr;
+        }
         return e;
     }
     void release(cudaStream_t s) {
-        if (p) cudaFreeAsync(p, s);
+        if (p) {
+            cudaFreeAsync(p, s);
+            add_device_bytes(-(long long)bytes);
+        }
         p = nullptr;
         bytes = 0;
     }
@@ -86,6 +106,7 @@ struct BatchJoin {
     int ktech = 0;
     hyset_technique tech = HYSET_TECH_AUTO;
     uint32_t units = 0;
+    uint32_t unit_probes = 0;  // probes per work unit of the prefix-index kernel (0: window technique)
 };
 
 // Scratch of an index build (prefix lengths and offsets, entries, radix sort
@@ -137,7 +158,12 @@ struct hyset_ctx {
     double cost[3][9] = {};                   // per technique (bitmap, fgss, direct)
     hs::DevBuf d_mlp, d_feat, d_moments, d_hist;
     std::map<std::string, std::pair<hyset_technique, int>> select_cache;  // decision, selector
-    std::map<std::string, uint32_t> bits_cache;  // autotuned signature width per join
+    struct TuneChoice {
+        uint32_t bits = 0;   // signature width
+        int vmode = 0;       // verification mode (0: not tuned)
+        uint32_t batch = 0;  // probes per warp batch of the probe-major kernel (0: not tuned)
+    };
+    std::map<std::string, TuneChoice> tune_cache;  // the autotuner's choices per join
     std::map<std::string, uint32_t> universe_cache;  // universe by collection size profile (host-input joins)
     struct SplitPlan {
         uint32_t at;  // first probe id of the high range; 0 = no split
@@ -175,6 +201,7 @@ struct hyset_result {
     hyset_technique technique = HYSET_TECH_AUTO;
     uint32_t bitmap_bits = 0;  // signature width the join ran with
     uint32_t verify_mode = 0;  // verification mode the join ran with
+    uint32_t probe_batch = 0;  // probes per warp batch of the probe-major kernel (0: not that kernel)
     uint32_t split_at = 0;     // partition split: first probe id of the high range (0 = none)
     hyset_technique split_low = HYSET_TECH_AUTO;  // the low range's technique
     double device_ms = 0;

@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
                 const uint2 cm = R.meta[c];
                 cs = cm.x;
                 lc = cm.y;
-                // verification.hpp:346-348 / hybrid_kernels.hpp:50: minoverlap(probe, candidate),
+                // hybrid_kernels.hpp:50: minoverlap(probe, candidate),
                 // for any pair (an incompatible length pair gets min(lp, lc)).
                 const uint32_t big = max(lp, lc), small = min(lp, lc);
                 if (small >= B.minsize[big]) mo = minoverlap(B, big, small);

@@ -138,6 +138,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
             res->technique = part[1].technique;
             res->bitmap_bits = part[1].bitmap_bits;
             res->verify_mode = part[1].verify_mode;
+            res->probe_batch = part[1].probe_batch;
             res->selector = 2;
             res->split_at = split_at;
             res->split_low = part[0].technique;
@@ -156,7 +157,8 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
         const uint32_t a_lo = o->probe_end ? o->probe_begin : 0, a_hi = o->probe_end ? o->probe_end : S->n;
         if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && tech == HYSET_TECH_FGSS && tn.probe_major &&
             a_hi - a_lo >= TUNE_MIN_PROBES)
-            ST(autotune_bits(ctx, R, S, o, b, self, a_lo, a_hi, &tn.bits, o->verify_mode ? nullptr : &tn.vmode));
+            ST(autotune_bits(ctx, R, S, o, b, self, a_lo, a_hi, &tn.bits, o->verify_mode ? nullptr : &tn.vmode,
+                             o->fgss_batch ? nullptr : &tn.batch));
     }
     const int vmode = tn.vmode;
     res->verify_mode = (uint32_t)vmode;
@@ -173,6 +175,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     P.R_L = R->max_size;
     P.self = self ? 1 : 0;
     P.grab = tech == HYSET_TECH_FGSS ? std::min<uint32_t>(tn.batch, 32) : 1;
+    res->probe_batch = tech == HYSET_TECH_FGSS && tn.probe_major ? P.grab : 0;
     P.p_lo = o->probe_end ? o->probe_begin : 0;
     P.p_hi = o->probe_end ? o->probe_end : S->n;
     P.r_lo = 0;

@@ -2,22 +2,22 @@
 //
 // Some callers of this library cannot allocate device memory at the moment
 // they need a join step: a host engine that owns every byte of GPU memory
-// through its own pool, code that runs while another component is capturing
-// the stream into a CUDA graph (cudaMalloc is not capturable), or a latency-
-// critical path where cudaMalloc's implicit device synchronisation is not
-// acceptable.  hyset_verify_candidates_noalloc serves them: the caller passes
-// device inputs and outputs, and the kernel's scratch (work counter, pair
-// counter, minoverlap table) lives in one file-scope __device__ array.
+// through its own pool (a database or serving process that sizes its pool at
+// start-up and forbids allocations afterwards), or a latency-critical path
+// where cudaMalloc's implicit device synchronisation is not acceptable.
+// hyset_verify_candidates_noalloc serves them: the caller passes device inputs
+// and outputs, and the kernel's scratch (work counter, pair counter,
+// minoverlap table) lives in one file-scope __device__ array.  The call
+// enqueues a set-up kernel, the verification kernel and two device-to-device
+// copies on the caller's stream; it never waits for the stream.
 //
 // The array is HYSET_NOALLOC_SCRATCH_BYTES (64 KiB); every GPU that loads the
 // library holds it until the process exits.  All calls share it and it keeps
-// the last call's contents: each call clears its counters and rewrites the
-// table first, so calls that overlap on the GPU (different streams, or
-// different host threads without ordering) race on it and must be serialised
-// by the caller.
-#include <cmath>
+// the last call's contents: each call's set-up kernel clears the counters and
+// rewrites the table first, so calls that overlap on the GPU (different
+// streams, or different host threads without ordering) race on it and must be
+// serialised by the caller.
 #include <cstddef>
-#include <cstring>
 #include <mutex>
 
 #include "../../include/hyset_gb300.h"
@@ -96,6 +96,28 @@ __global__ void __launch_bounds__(256) k_verify_noalloc(
     }
 }
 
+// Set-up of one call: clears the counters and writes the raw minoverlap by
+// |a| + |b| for sums 0..entries-1.  The reference's double expression
+// (include/hyset/similarity.hpp:40-42, jaccard: ceil(sum * t / (1 + t)); dice
+// in the same style: ceil(t * sum / 2)) is evaluated with explicitly rounded
+// IEEE operations, so no multiply-add contraction can change a value: each
+// entry is the double the host computes.
+__global__ void __launch_bounds__(256) k_noalloc_setup(unsigned char* scratch, uint32_t entries, int sim, double t) {
+    ScratchHeader* hdr = reinterpret_cast<ScratchHeader*>(scratch);
+    uint32_t* mo_sum = reinterpret_cast<uint32_t*>(scratch + TABLE_OFFSET);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        hdr->count = 0;
+        hdr->work = 0;
+        hdr->skipped = 0;
+    }
+    for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < entries; k += gridDim.x * blockDim.x) {
+        const double sum = (double)k;
+        const double v = sim == SIM_DICE ? __ddiv_rn(__dmul_rn(t, sum), 2.0)
+                                         : __ddiv_rn(__dmul_rn(sum, t), __dadd_rn(1.0, t));
+        mo_sum[k] = (uint32_t)ceil(v);
+    }
+}
+
 // Device address of g_noalloc_scratch per device, looked up once per device
 // (with that device current) on the first call made on it.
 std::mutex g_mu;
@@ -113,12 +135,6 @@ hyset_status scratch_for_current_device(void** out) {
     }
     *out = g_scratch_ptr[dev];
     return HYSET_OK;
-}
-
-uint32_t raw_minoverlap(int sim, uint32_t sum, double t) {
-    // similarity.hpp:40-42 (jaccard); dice in the same style
-    if (sim == SIM_DICE) return (uint32_t)(std::ceil(t * (double)sum / 2.0));
-    return (uint32_t)(std::ceil((double)sum * t / (1 + t)));
 }
 
 }  // namespace
@@ -143,18 +159,12 @@ extern "C" hyset_status hyset_verify_candidates_noalloc(
     void* scratch = nullptr;
     hyset_status st = scratch_for_current_device(&scratch);
     if (st != HYSET_OK) return st;
-    // minoverlap by |a| + |b| for every pair of lengths <= max_set_size, computed
-    // on the host with the reference's double expression (no multiply-add
-    // contraction in this translation unit)
-    uint32_t table[2 * NOALLOC_MAX_LEN + 1];
-    const uint32_t entries = 2 * max_set_size + 1;
-    for (uint32_t k = 0; k < entries; ++k) table[k] = raw_minoverlap((int)sim, k, threshold);
+    // counters cleared and the minoverlap table for lengths <= max_set_size
+    // written by a set-up kernel on the same stream (no host copy)
     unsigned char* base = static_cast<unsigned char*>(scratch);
-    if (cudaMemsetAsync(base, 0, sizeof(ScratchHeader), s) != cudaSuccess) return HYSET_E_CUDA;
-    // pageable source: the copy is staged before the call returns, so `table` may go out of scope
-    if (cudaMemcpyAsync(base + TABLE_OFFSET, table, entries * sizeof(uint32_t), cudaMemcpyHostToDevice, s) !=
-        cudaSuccess)
-        return HYSET_E_CUDA;
+    const uint32_t entries = 2 * max_set_size + 1;
+    k_noalloc_setup<<<(entries + 255) / 256, 256, 0, s>>>(base, entries, (int)sim, threshold);
+    if (cudaGetLastError() != cudaSuccess) return HYSET_E_CUDA;
     if (n_probes) {
         int dev = 0, sms = 0;
         if (cudaGetDevice(&dev) != cudaSuccess ||

@@ -221,6 +221,12 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
     c->n = n_sets;
     c->n_tokens = n_tokens;
     hyset_coll* C = c.get();
+    auto guard = on_exit([&] {  // every early return releases the collection (copies finished first)
+        if (c) {
+            cudaStreamSynchronize(cp);
+            hyset_collection_free(ctx, c.release());
+        }
+    });
     auto bail = [&](hyset_status st) {
         cudaStreamSynchronize(cp);
         hyset_collection_free(ctx, c.release());
@@ -299,11 +305,12 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
     Tuned tn = tune(C, C, o, selected);
     if (tn.tech != HYSET_TECH_FGSS || !tn.probe_major) pipelined = false;
     if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && n_sets >= TUNE_MIN_PROBES) {
-        auto it = ctx->bits_cache.find(key);
-        if (it == ctx->bits_cache.end()) pipelined = false;
+        auto it = ctx->tune_cache.find(key);
+        if (it == ctx->tune_cache.end()) pipelined = false;
         else {
-            tn.bits = it->second & 0xFFFFu;
-            if (!o->verify_mode && (it->second >> 16)) tn.vmode = (int)(it->second >> 16);
+            tn.bits = it->second.bits;
+            if (!o->verify_mode && it->second.vmode) tn.vmode = it->second.vmode;
+            if (!o->fgss_batch && it->second.batch) tn.batch = it->second.batch;
         }
     }
     Bounds* b = nullptr;
@@ -451,6 +458,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         res->technique = HYSET_TECH_FGSS;
         res->bitmap_bits = tn.bits;
         res->verify_mode = (uint32_t)tn.vmode;
+        res->probe_batch = P.grab;
         res->selector = selector;
         if (o->collect_stats) res->stats[3] = E;
         res->launches = launches() - launches0;

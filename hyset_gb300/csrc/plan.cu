@@ -44,7 +44,7 @@ Tuned tune(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o, h
     if (t.tech == HYSET_TECH_AUTO) t.tech = (pairs_window <= 4000000ull) ? HYSET_TECH_BITMAP : HYSET_TECH_FGSS;
     // explicit FGSS defaults to the token-major kernel; AUTO to probe-major
     t.probe_major = (o->technique == HYSET_TECH_FGSS && !o->probe_major) ? 0 : 1;
-    t.batch = o->fgss_batch ? o->fgss_batch : 3;
+    t.batch = o->fgss_batch ? o->fgss_batch : DEFAULT_PROBE_BATCH;
     t.bits = o->bitmap_bits;
     if (o->technique == HYSET_TECH_AUTO && t.bits == 0) t.bits = avg <= 48.0 ? 128 : 256;
     if (t.tech == HYSET_TECH_BITMAP && t.bits == 0) t.bits = 64;
@@ -292,18 +292,24 @@ namespace {
 constexpr uint32_t TUNE_SAMPLE = 16384;  // a sample fills the GPU for about two waves
 constexpr float TUNE_MARGIN = 0.92f;  // leave the rule's width only for an estimated gain of 8 % or more
 constexpr float TUNE_VMODE_MARGIN = 0.97f;  // warp verification only for an estimated gain of 3 % or more
+constexpr float TUNE_BATCH_MARGIN = 0.97f;  // a probe batch other than the default only for a gain of 3 % or more
+constexpr uint32_t TUNE_BATCHES[] = {1, 2, 3, 4, 6};  // probe batches the autotuner times
 }  // namespace
 
-// The signature width (and, when vmode is given, the verification mode) of a
-// prefix-index join, from timed samples of its probe range; cached per join
-// key as bits | vmode << 16.
+// The signature width (and, when requested, the verification mode and the
+// probe batch) of a prefix-index join, from timed samples of its probe range;
+// cached per join key.  The batch is the tile of the probe-major kernel: the
+// probes one warp filters together (its slot and item rounds are shared by
+// the batch, so a larger batch keeps more loads in flight per warp but
+// balances worse across warps).
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
-                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode) {
+                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode, uint32_t* batch) {
     const std::string key = join_key(R, S, o);
-    auto it = ctx->bits_cache.find(key);
-    if (it != ctx->bits_cache.end() && (!vmode || (it->second >> 16))) {
-        *bits = it->second & 0xFFFFu;
-        if (vmode) *vmode = (int)(it->second >> 16);
+    auto it = ctx->tune_cache.find(key);
+    if (it != ctx->tune_cache.end() && (!vmode || it->second.vmode) && (!batch || it->second.batch)) {
+        *bits = it->second.bits;
+        if (vmode) *vmode = it->second.vmode;
+        if (batch) *batch = it->second.batch;
         return HYSET_OK;
     }
     cudaStream_t s = ctx->stream;
@@ -317,7 +323,9 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     P.self = self ? 1 : 0;
     P.r_lo = 0;
     P.r_hi = R->n;
-    P.grab = 4;
+    const uint32_t grab_cap = P.X2.set ? 16u : 32u;  // banded R-S joins: two lanes per probe
+    const uint32_t base_batch = std::min(o->fgss_batch ? o->fgss_batch : DEFAULT_PROBE_BATCH, grab_cap);
+    P.grab = base_batch;
     CK(ctx->s_count.ensure(16, s));
     CK(ctx->s_work.ensure(16, s));
     P.out = Sink{nullptr, ctx->s_count.as<unsigned long long>(), 0, 1};
@@ -347,6 +355,20 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
             total += ms;
         }
         *out = total * (float)(p_hi - p_lo) / (float)(sampled ? sampled : 1);
+        return HYSET_OK;
+    };
+    auto use_width = [&](uint32_t width) -> hyset_status {
+        const int words = (int)(width / 64);
+        P.words = words;
+        P.bits_R = P.bits_S = nullptr;
+        if (words) {
+            const uint64_t *br = nullptr, *bs = nullptr;
+            ST(get_bitmaps(ctx, R, words, &br));
+            if (self) bs = br;
+            else ST(get_bitmaps(ctx, S, words, &bs));
+            P.bits_R = br;
+            P.bits_S = bs;
+        }
         return HYSET_OK;
     };
     for (int k = 0; k < 4; ++k) {
@@ -380,29 +402,47 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     const uint32_t rule = (double)R->n_tokens / (double)std::max<uint32_t>(R->n, 1) <= 48.0 ? 128u : 256u;
     const float rule_ms = est[rule == 128u ? 1 : 2];
     if (best != rule && best_ms > TUNE_MARGIN * rule_ms) best = rule;
+    const int kb = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
+    float cur_ms = kern_est[kb];  // the chosen configuration's estimated kernel time
     // verification: a lane per surviving item, or the warp per item when the
     // samples show it faster at the chosen width (long merges: low thresholds,
-    // cosine)
-    int vm = 1;
+    // cosine); an explicit mode is kept
+    int vm = o->verify_mode == 2 ? 2 : 1;
+    ST(use_width(best));
     if (vmode) {
-        const int kb = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
-        const int words = (int)(best / 64);
-        P.words = words;
-        P.bits_R = P.bits_S = nullptr;
-        if (words) {
-            const uint64_t *br = nullptr, *bs = nullptr;
-            ST(get_bitmaps(ctx, R, words, &br));
-            if (self) bs = br;
-            else ST(get_bitmaps(ctx, S, words, &bs));
-            P.bits_R = br;
-            P.bits_S = bs;
-        }
         float warp_ms = 0;
         ST(sample(2, &warp_ms));
-        if (warp_ms < TUNE_VMODE_MARGIN * kern_est[kb]) vm = 2;
+        if (warp_ms < TUNE_VMODE_MARGIN * kern_est[kb]) {
+            vm = 2;
+            cur_ms = warp_ms;
+        }
         *vmode = vm;
+    } else if (vm == 2) {
+        ST(sample(2, &cur_ms));
     }
-    ctx->bits_cache[key] = best | (vmode ? (uint32_t)vm << 16 : 0u);
+    // probe batch: the other tile widths at the chosen width and mode; a
+    // width other than the default only for an estimated gain of 3 % or more
+    uint32_t tb = base_batch;
+    if (batch) {
+        float tb_ms = cur_ms;
+        for (uint32_t cand_b : TUNE_BATCHES) {
+            const uint32_t g = std::min(cand_b, grab_cap);
+            if (g == base_batch) continue;
+            P.grab = g;
+            float ms = 0;
+            ST(sample(vm, &ms));
+            if (ms < TUNE_BATCH_MARGIN * tb_ms && ms < TUNE_BATCH_MARGIN * cur_ms) {
+                tb = g;
+                tb_ms = ms;
+            }
+        }
+        P.grab = base_batch;
+        *batch = tb;
+    }
+    hyset_ctx::TuneChoice& ch = ctx->tune_cache[key];
+    ch.bits = best;
+    if (vmode) ch.vmode = vm;
+    if (batch) ch.batch = tb;
     *bits = best;
     return HYSET_OK;
 }

@@ -28,6 +28,9 @@ hyset_status hyset_verifier_create(hyset_ctx* ctx, const hyset_coll* indexed, co
     ST(check_opts(ctx, &o));
     CK(cudaSetDevice(ctx->device));
     auto v = std::make_unique<hyset_verifier>();
+    auto guard = on_exit([&] {  // a failed creation releases what it allocated
+        if (v) hyset_verifier_destroy(v.release());
+    });
     v->ctx = ctx;
     v->indexed = indexed;
     v->probe = probe;

@@ -131,3 +131,39 @@ def generate(spec: SynthSpec, threads: int = 0, **overrides) -> Collection:
     finally:
         lib.hyset_synth_free(h)
     return Collection(tok, st, sz)
+
+
+def batch_workload(n_joins: int = 256, seed: int = 0x5E7B):
+    """The batched workload: `n_joins` independent R-S joins of uneven sizes:
+    |R|, |S| log-uniform in [1e3, 2e5], Zipf s in [0.7, 1.3], mean set size
+    log-uniform in [8, 300], universe 5e4..5e5,
+    threshold in [0.5, 0.95], similarity Jaccard / cosine / dice in turn.  R and
+    S of a join are a random split of one generated collection, so near-duplicate
+    sets fall on both sides.  Returns [((r_tokens, r_starts, r_sizes),
+    (s_tokens, s_starts, s_sizes), {"threshold": t, "sim": name}), ...]."""
+    import math
+    rng = np.random.default_rng(seed)
+    sims = ["jaccard", "cosine", "dice"]
+    out = []
+    for j in range(n_joins):
+        nr = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
+        ns = int(math.exp(rng.uniform(math.log(1e3), math.log(2e5))))
+        mean = math.exp(rng.uniform(math.log(8), math.log(300)))
+        c = generate(C2, n_sets=nr + ns, universe=int(rng.uniform(5e4, 5e5)),
+                     zipf_s=float(rng.uniform(0.7, 1.3)), size_dist=LOGNORMAL,
+                     size_a=math.log(mean) - 0.125, size_b=0.5, size_min=2,
+                     size_max=min(2000, max(16, int(mean * 6))), dup_frac=0.05, dup_edit_lo=0.02,
+                     dup_edit_hi=0.12, seed=int(rng.integers(1, 2**31)))
+        side = rng.random(c.n) < nr / (nr + ns)
+        parts = []
+        for mask in (side, ~side):
+            ids = np.nonzero(mask)[0]
+            sizes = c.sizes[ids]
+            starts = np.zeros(len(ids), np.uint32)
+            if len(ids):
+                starts[1:] = np.cumsum(sizes[:-1])
+            sz64 = sizes.astype(np.int64)
+            src = np.repeat(c.starts[ids].astype(np.int64) - starts.astype(np.int64), sz64) + np.arange(sz64.sum())
+            parts.append((c.tokens[src], starts, sizes))
+        out.append((parts[0], parts[1], dict(threshold=float(rng.uniform(0.5, 0.95)), sim=sims[j % 3])))
+    return out

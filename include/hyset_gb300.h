@@ -13,7 +13,7 @@
  *   - Results are owned by the library until hyset_result_free.
  *   - Pairs are (probe set id, indexed set id).  In a self-join the ids are the
  *     positions in the size-sorted collection and first > second, exactly as the
- *     reference emits them (include/hyset/verification.hpp:120-122).
+ *     reference emits them (include/hyset/verification.hpp:128-129).
  *   - The output pair SET is bit-exact to the reference's host::allpairs on the
  *     same input; the ORDER of pairs is unspecified unless sorted on request.
  *   - The library never falls back to a CPU implementation: without a usable
@@ -85,7 +85,8 @@ typedef struct {
     uint32_t probe_major;      /* technique FGSS: 1 = probe-major kernel (set-id-sorted index, one warp
                                   per probe batch), 0 = token-major kernel (token groups in shared
                                   memory).  AUTO always uses probe-major; probe ranges need it */
-    uint32_t fgss_batch;       /* probe-major FGSS: probes per warp batch (1..32); 0 = tuned default */
+    uint32_t fgss_batch;       /* probe-major FGSS: probes per warp batch (1..32); 0 = the default (3),
+                                  or the autotuner's choice with technique AUTO */
     uint32_t orientation;      /* R-S joins: 0 = automatic (index the smaller collection, probe the
                                   larger), 1 = as given, 2 = swapped.  The result is the same pair
                                   set in every orientation, pairs always (probe id, indexed id) of
@@ -105,6 +106,13 @@ hyset_status hyset_create(int device, hyset_ctx** out);
 void hyset_destroy(hyset_ctx* ctx);
 const char* hyset_last_error(const hyset_ctx* ctx);
 void hyset_default_opts(hyset_join_opts* opts);
+/* No counterpart in the reference (its handlers own raw device arrays).
+ * Device memory held by the library's buffers, summed over every context,
+ * collection, handler and verifier alive (capacity planning, leak checks).
+ * Allocation failures return HYSET_E_NOMEM and leave every object valid;
+ * for tests, while the environment variable HYSET_FAULT_ALLOC holds N the
+ * N-th device allocation counted from when that value was first seen fails. */
+uint64_t hyset_device_bytes(void);
 
 /* ---- collections ----------------------------------------------------- */
 /* hyset::collection::device_collection(host_collection&) (include/hyset/collection.hpp:54-71):
@@ -178,6 +186,12 @@ const hyset_pair* hyset_result_pairs(const hyset_result* r); /* NULL when count_
 hyset_technique hyset_result_technique(const hyset_result* r);
 uint32_t hyset_result_bitmap_bits(const hyset_result* r);   /* signature width used (0 = none) */
 uint32_t hyset_result_verify_mode(const hyset_result* r);   /* verification mode used (1 lane, 2 warp, 3 staged) */
+/* Probes per warp batch of the probe-major prefix-filter kernel (the tile the
+ * reference sizes with --block for its block-pair launches, src/fgss.cu and
+ * device_algorithms.hpp:147-148); 0 when the join ran another kernel.  With
+ * fgss_batch 0 and technique AUTO the autotuner picks it from timed samples
+ * (joins of 60,000 probes or more). */
+uint32_t hyset_result_probe_batch(const hyset_result* r);
 /* Partition split chosen by the learned selector for an AUTO self-join: the
  * first probe id of the high range (0 = the join ran as one range) and, in
  * *low_technique (may be NULL), the low range's technique (the high range's is
@@ -289,31 +303,33 @@ int hyset_result_selector(const hyset_result* r);
 /* ---- verification without allocation ------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory when they verify: a host engine that owns all GPU memory through its
- * own pool, code running while the stream is being captured into a CUDA graph
- * (cudaMalloc cannot be captured), or a latency-critical path that cannot
- * afford cudaMalloc's implicit device synchronisation.
+ * own pool and forbids allocations after start-up, or a latency-critical path
+ * that cannot afford cudaMalloc's implicit device synchronisation.
  *
  * Verifies explicit candidate lists exactly like hyset_verifier (scenario 1:
  * one lane per candidate, 2: one warp per candidate): probe d_probes[i] of the
  * probe collection S owns candidates [d_offsets[i-1] (0 for i = 0),
  * d_offsets[i]) of the indexed collection R; (probe, candidate) is appended to
  * d_pairs when |probe ∩ candidate| >= minoverlap(|probe|, |candidate|).  All
- * inputs and outputs are device pointers; nothing is allocated and the call is
- * asynchronous on `stream` (a cudaStream_t, NULL = legacy default stream, on
- * the current device).  *d_count receives the number of result pairs (pairs
- * past pair_capacity are counted but not written); *d_skipped (optional)
- * receives the number of candidates skipped because a set is longer than
- * max_set_size.
+ * inputs and outputs are device pointers; nothing is allocated and nothing is
+ * copied from host memory: the call enqueues two kernels and two
+ * device-to-device copies on `stream` (a cudaStream_t, NULL = legacy default
+ * stream, on the current device) and returns without waiting.  *d_count
+ * receives the number of result pairs (pairs past pair_capacity are counted
+ * but not written); *d_skipped (optional) receives the number of candidates
+ * skipped because a set is longer than max_set_size.  Both, and d_pairs, are
+ * valid once the stream has reached the end of the call's work (for example
+ * after cudaStreamSynchronize).
  *
  * Limits: Jaccard and dice only (HYSET_E_UNSUPPORTED for cosine); sets of at
  * most HYSET_NOALLOC_MAX_SET_SIZE tokens (larger max_set_size is rejected with
  * HYSET_E_UNSUPPORTED).  The scratch (counters and the minoverlap table) is one
  * HYSET_NOALLOC_SCRATCH_BYTES array in device memory that every GPU loading
  * the library keeps until exit.  All calls share it and it keeps the last
- * call's contents; each call clears and rewrites it first, so calls that
- * overlap on the GPU race and must be serialised by the caller.  The first
- * call on a device looks up the array's device address (with that device
- * current); make that first call before any stream capture. */
+ * call's contents; each call's first kernel clears and rewrites it, so calls
+ * that overlap on the GPU race and must be serialised by the caller.  The
+ * first call on a device looks up the array's device address with that device
+ * current (cudaGetSymbolAddress, once per device). */
 #define HYSET_NOALLOC_SCRATCH_BYTES 65536
 #define HYSET_NOALLOC_MAX_SET_SIZE 4096
 hyset_status hyset_verify_candidates_noalloc(

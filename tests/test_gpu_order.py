@@ -2,7 +2,8 @@
 
 `sort_pairs` orders a result by (probe id, indexed id) with a device radix
 sort, so the pair list is the same array on every run (the reference's append
-order is nondeterministic, include/hyset/verification.hpp:385-386).  The batch
+order is nondeterministic: each pair takes the next slot of an atomicAdd,
+include/hyset/verification.hpp:125-130).  The batch
 tests check that a captured batch stays correct when later joins grow the
 context's scratch memory, and that freeing a collection drops a captured batch
 that reads it."""
