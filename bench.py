@@ -559,6 +559,106 @@ def run_verify(args):
           flush=True)
 
 
+def run_configs(args):
+    """--workload c1 / c2: the two smaller self-join configurations, each leg
+    timed with the collection resident (CUDA events, L2 flushed, median of
+    --steps after --warmup), every leg's pair set checked against the oracle.
+
+    c1: 10,000 sets, Jaccard 0.8: the plain single-launch GPU path and AUTO
+    against the reference algorithm on one host core (cpu_single) and on all
+    of them (cpu_multi).
+    c2: 200,000 sets, Jaccard 0.5 / 0.7 / 0.9: the reference's two GPU
+    techniques, bitmap signatures of 64 and 256 bits and the prefix filter,
+    beside AUTO."""
+    import numpy as np
+    import torch
+    import hyset_gb300 as hs
+    import oracle
+    from hyset_gb300 import synth
+
+    spec, taus = (synth.C1, [0.8]) if args.workload == "c1" else (synth.C2, [0.5, 0.7, 0.9])
+    c = synth.generate(spec)
+    ctx = hs.Context(0)
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    threads = os.cpu_count() or 1
+    peak, peak_kind = measured_peaks()
+
+    def keys(p):
+        p = np.asarray(p, np.uint64).reshape(-1, 2)
+        return np.sort((p[:, 0] << np.uint64(32)) | p[:, 1])
+
+    if args.workload == "c1":
+        legs = {"plain_single_launch": dict(technique="fgss", probe_major=True, bitmap=0, verify_mode=1, fgss_batch=1),
+                "auto": dict(technique="auto")}
+    else:
+        legs = {"bitmap64": dict(technique="bitmap", bitmap=64), "bitmap256": dict(technique="bitmap", bitmap=256),
+                "fgss": dict(technique="fgss", probe_major=True), "auto": dict(technique="auto")}
+    rows, launches, parity, headline = [], 0, True, None
+    for tau in taus:
+        exp = keys(oracle.join(c.tokens, c.starts, c.sizes, tau))
+        idx_s, join_s = oracle.last_timing()
+        cpu1_s = idx_s + join_s
+        oracle.join_multi(c.tokens, c.starts, c.sizes, tau, threads)
+        idx_s, join_s = oracle.last_timing(multi=True)
+        cpun_s = idx_s + join_s
+        row = {"threshold": tau, "result_pairs": int(exp.size), "cpu_single_ms": 1000 * cpu1_s,
+               "cpu_multi_ms": 1000 * cpun_s, "cpu_threads": threads}
+        for name, q in legs.items():
+            kw = dict(threshold=tau, device_pairs=True, **q)
+            r = ctx.self_join(coll, **dict(kw, device_pairs=False))
+            ok = bool(np.array_equal(keys(r.pairs), exp))
+            parity &= ok
+            st = ctx.self_join(coll, collect_stats=True, **kw)
+            for _ in range(args.warmup):
+                ctx.self_join(coll, **kw)
+            dev, kern = [], []
+            for _ in range(args.steps):
+                flush.fill_(1)
+                torch.cuda.synchronize()
+                x = ctx.self_join(coll, **kw)
+                dev.append(x.device_ms)
+                kern.append(x.kernel_ms)
+                launches += x.launches
+            leg = {"ms": statistics.median(dev), "kernel_ms": statistics.median(kern), "parity": ok,
+                   "technique": st.technique, "bitmap_bits": st.bitmap_bits, "verify_mode": st.verify_mode,
+                   "probe_batch": st.probe_batch}
+            if st.technique == "fgss":
+                alg = algorithmic_bytes(st.stats, st.count, st.bitmap_bits // 64, c.n)
+                leg["roofline_frac"] = alg / (leg["kernel_ms"] / 1000.0) / 1e9 / peak
+                leg["algorithmic_bytes"] = alg
+            else:
+                leg["window_pairs_per_s"] = st.stats[0] / (leg["kernel_ms"] / 1000.0)
+            row[name] = leg
+        rows.append(row)
+        if headline is None or tau == 0.7:
+            headline = (tau, row)
+    tau, row = headline
+    auto = row["auto"]
+    line = {"metric": f"self-join ms & verified pairs/s, {args.workload} configuration, 1 GB300",
+            "value": row["result_pairs"] / (auto["ms"] / 1000.0), "unit": "pairs/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": auto["ms"], "higher_is_better": True,
+            "dtype": "u32", "data": "synthetic (seeded generator)",
+            "config": {"workload": ("10,000 sets, sizes U[5,50], universe 5,000, Zipf 1.0, Jaccard 0.8"
+                                    if args.workload == "c1" else
+                                    "200,000 sets, lognormal(3.2,0.6) sizes in [2,500], universe 100,000, "
+                                    "Zipf 1.1, 3% near-duplicates; Jaccard 0.5 / 0.7 / 0.9"),
+                       "headline_threshold": tau, "thresholds": rows,
+                       "l2": "512 MB buffer written between timed steps"},
+            "roofline": {"bound": "hbm", "frac": auto.get("roofline_frac"), "peak": peak, "unit": "GB/s",
+                         "peak_kind": peak_kind, "traffic": None,
+                         "kernel": "AUTO leg's filter+verify launch"},
+            "cpu_baseline": {"value": row["result_pairs"] / (row["cpu_single_ms"] / 1000.0), "unit": "pairs/s",
+                             "cores": 1, "kind": "port",
+                             "sample": "whole workload (index + join), oracle restatement of host::allpairs"},
+            "parity": parity, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    coll.free()
+    ctx.close()
+    if not parity:
+        sys.exit("parity failure")
+
+
 def hs_text_bytes(c):
     from hyset_gb300 import synth
     lib = synth._load()
@@ -584,9 +684,10 @@ def main():
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
     ap.add_argument("--vmode", type=int, default=0,
                     help="verification: 0 auto (the autotuner's samples choose), 1 lane, 2 warp per candidate")
-    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse", "verify"],
+    ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse", "verify", "c1", "c2"],
                     help="batch: the batched R-S workload; parse: the collection text reader; verify: the "
-                         "candidate verifier alone (separate measurements, not the headline)")
+                         "candidate verifier alone; c1 / c2: the 10K-set and 200K-set configurations "
+                         "(separate measurements, not the headline)")
     ap.add_argument("--joins", type=int, default=256)
     args = ap.parse_args()
     ws, rank, local = dist_env()
@@ -598,6 +699,9 @@ def main():
         return
     if args.workload == "verify":
         run_verify(args)
+        return
+    if args.workload in ("c1", "c2"):
+        run_configs(args)
         return
     if args.impl == "reference":
         run_reference(args, ws, rank)

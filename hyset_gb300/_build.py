@@ -25,7 +25,7 @@ SYNTH = os.path.join(PKG, "libhyset_synth.so")
 CUDA_SOURCES = ["primitives.cu", "join.cu", "join_tm.cu", "batch.cu", "mlp.cu", "stats.cu", "parse.cu", "noalloc.cu",
                 # host side of the C ABI
                 "capi.cu", "collection.cu", "bounds.cu", "index_host.cu", "plan.cu", "join_host.cu", "pipeline.cu",
-                "batch_host.cu", "handlers.cu", "verifier.cu"]
+                "batch_host.cu", "handlers.cu", "verifier.cu", "ring.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17",

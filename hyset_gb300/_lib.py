@@ -100,6 +100,8 @@ PROTOTYPES = {
                                         C.c_int, C.c_uint32, C.c_uint32, C.c_double, C.POINTER(C.c_void_p)]),
     "hyset_verifier_add_candidates": (C.c_int, [C.c_void_p, C.c_uint32, U32P, C.c_uint32]),
     "hyset_verifier_flush": (C.c_int, [C.c_void_p]),
+    "hyset_verifier_set_wait": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "hyset_verifier_status": (C.c_int, [C.c_void_p]),
     "hyset_verifier_output": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint64), C.POINTER(C.c_void_p)]),
     "hyset_verifier_destroy": (None, [C.c_void_p]),
     "hyset_join_features": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(JoinOpts),

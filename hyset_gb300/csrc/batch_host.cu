@@ -96,7 +96,9 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
     for (uint32_t j = 0; j < n; ++j) {
         const hyset_join_desc& d = joins[j];
         if (!d.indexed) return fail(ctx, HYSET_E_INVALID, "batch join without an indexed collection");
-        auto bj = std::make_unique<BatchJoin>();
+        // owned by the plan from the start: a failure below releases its buffers
+        plan->joins.push_back(std::make_unique<BatchJoin>());
+        BatchJoin* bj = plan->joins.back().get();
         bj->R = const_cast<hyset_coll*>(d.indexed);
         bj->S = const_cast<hyset_coll*>(d.probe ? d.probe : d.indexed);
         bj->self = bj->S == bj->R;
@@ -183,7 +185,6 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         bj->units = (np + desc[j].unit_probes - 1) / desc[j].unit_probes;
         cost[j] = (double)np * (double)(R->n_tokens / std::max<uint32_t>(R->n, 1) + 1) *
                   (bj->ktech == TECH_FGSS ? 1.0 : (double)R->n);
-        plan->joins.push_back(std::move(bj));
     }
     // scratch for the largest index build, sized before capture
     CK(ctx->sc->len.ensure((size_t)maxN * 4 + 4, s));

@@ -238,8 +238,22 @@ struct hyset_verifier {
     uint32_t scenario = 1;
     int aggregate = 0;
     uint32_t max_probes = 0, max_candidates = 0;
-    std::vector<uint32_t> h_probes, h_offsets, h_cands;
-    hs::DevBuf d_probes, d_offsets, d_cands, pairs, count, work;
+    // the candidate ring (ring.cu): records and candidate ids in device rings,
+    // staged in pinned host rings of the same layout
+    uint64_t rec_cap = 0, cand_cap = 0, pair_cap = 0;
+    hs::DevBuf d_recs, d_cands, d_done, d_ctl, pairs;
+    hs::RingRec* h_recs = nullptr;
+    uint32_t* h_cands = nullptr;
+    unsigned long long* h_ctl = nullptr;  // pinned read-back of the control words
+    uint64_t pushed = 0, published = 0;   // records staged / published (absolute counts)
+    uint64_t cand_pushed = 0, cand_published = 0;
+    uint64_t head = 0;       // records verified, as last read back
+    uint64_t undrained = 0;  // candidates published since the pairs were last drained
+    uint64_t wait_ns = 0;    // the consumer's wait limit for published records
+    cudaStream_t pub = nullptr, cons = nullptr;  // publication copies / the persistent consumer
+    cudaEvent_t ev_pub = nullptr, ev_cons = nullptr;
+    bool consumer_live = false;
+    unsigned int last_status = 0;  // exit status of the last consumer launch that ended
     uint64_t out_count = 0;
     std::vector<hyset_pair> out_pairs;
 };

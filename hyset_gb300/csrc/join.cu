@@ -24,6 +24,7 @@
 // item at its smallest common token verifies it (the other items stop at the
 // first common token they see).  No dense B x B filter matrix exists.
 #include "join_impl.cuh"
+#include "verify_impl.cuh"
 
 namespace hs {
 
@@ -56,30 +57,6 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     }
 }
 
-// Staged lane-serial merge: b's first VSTAGE tokens are in `head` (shared
-// memory), the rest in global memory; same early-exit bounds as verify_serial.
-constexpr uint32_t VSTAGE = 16;            // candidate tokens staged per candidate
-constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fall in distinct banks
-__device__ __forceinline__ bool verify_staged(const uint32_t* a, uint32_t na, const uint32_t* head,
-                                              const uint32_t* __restrict__ b, uint32_t nb, uint32_t thr) {
-    uint32_t i = 0, k = 0, found = 0, maxa = na, maxb = nb;
-    while (maxa >= thr && maxb >= thr && found < thr) {
-        const uint32_t x = a[i], y = k < VSTAGE ? head[k] : __ldg(b + k);
-        if (x == y) {
-            ++i;
-            ++k;
-            ++found;
-        } else if (x < y) {
-            ++i;
-            --maxa;
-        } else {
-            ++k;
-            --maxb;
-        }
-    }
-    return found >= thr;
-}
-
 // Explicit candidate lists: probes[i] owns candidates [offsets[i-1], offsets[i]).
 template <int VMODE>
 __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, CollView S, BoundsView B,
@@ -89,73 +66,16 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
                                                                     uint32_t n_probes, Sink out, unsigned int* work) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* sbuf = smem + warp * (MAXP + (VMODE == 3 ? 32 * VSTRIDE : 0));
+    uint32_t* sbuf = smem + warp * verify_smem_words(VMODE);
     for (;;) {
         uint32_t i = 0;
         if (lane == 0) i = atomicAdd(work, 1u);
         i = __shfl_sync(FULL, i, 0);
         if (i >= n_probes) break;
-        const uint32_t p = probes[i];
-        const uint2 pm = S.meta[p];
-        const uint32_t lp = pm.y;
         const uint32_t cb = i ? offsets[i - 1] : 0, ce = offsets[i];
-        const uint32_t* pg = S.tokens + pm.x;
-        const uint32_t* a = pg;
-        if (lp <= MAXP) {
-            for (uint32_t k = lane; k < lp; k += 32) sbuf[k] = pg[k];
-            __syncwarp();
-            a = sbuf;
-        }
-        for (uint32_t k0 = cb; k0 < ce; k0 += 32) {
-            const uint32_t k = k0 + lane;
-            bool keep = k < ce;
-            uint32_t c = 0, lc = 0, mo = 0, cs = 0;
-            if (keep) {
-                c = cands[k];
-                const uint2 cm = R.meta[c];
-                cs = cm.x;
-                lc = cm.y;
-                // hybrid_kernels.hpp:50: minoverlap(probe, candidate),
-                // for any pair (an incompatible length pair gets min(lp, lc)).
-                const uint32_t big = max(lp, lc), small = min(lp, lc);
-                if (small >= B.minsize[big]) mo = minoverlap(B, big, small);
-                else mo = small;
-            }
-            if constexpr (VMODE == 1) {
-                bool ok = keep && verify_serial(a, lp, R.tokens + cs, lc, mo, NOWN);
-                emit(out, ok, p, c, lane);
-            } else if constexpr (VMODE == 3) {
-                // the first VSTAGE tokens of the round's 32 candidates arrive with
-                // 16 coalesced loads (two candidates per load, one per half-warp);
-                // each lane then merges its candidate out of shared memory and
-                // reads global memory only past the staged prefix
-                uint32_t* tile = sbuf + MAXP;
-                const uint32_t t = lane & (VSTAGE - 1);
-#pragma unroll
-                for (int r = 0; r < 16; ++r) {
-                    const int j = 2 * r + (lane >> 4);
-                    const uint32_t cj = __shfl_sync(FULL, cs, j), lj = __shfl_sync(FULL, keep ? lc : 0u, j);
-                    if (t < lj) tile[j * VSTRIDE + t] = __ldg(R.tokens + cj + t);
-                }
-                __syncwarp();
-                const bool ok = keep && verify_staged(a, lp, tile + lane * VSTRIDE, R.tokens + cs, lc, mo);
-                __syncwarp();
-                emit(out, ok, p, c, lane);
-            } else {
-                unsigned m = __ballot_sync(FULL, keep);
-                while (m) {
-                    int src = __ffs(m) - 1;
-                    m &= m - 1;
-                    uint32_t cc = __shfl_sync(FULL, c, src);
-                    uint32_t c2 = __shfl_sync(FULL, cs, src);
-                    uint32_t ll = __shfl_sync(FULL, lc, src);
-                    uint32_t mm = __shfl_sync(FULL, mo, src);
-                    bool ok = verify_warp(a, lp, R.tokens + c2, ll, mm, NOWN, lane);
-                    emit(out, ok && lane == 0, p, cc, lane);
-                }
-            }
-        }
-        __syncwarp();
+        const uint32_t* list = cands + cb;
+        verify_probe_list<VMODE>(R, S, B, probes[i], [list](uint32_t k) { return list[k]; }, ce - cb, out, sbuf,
+                                 lane);
     }
 }
 
@@ -206,7 +126,7 @@ cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const
                                      Sink out, unsigned int* work, int sm_count, cudaStream_t s) {
     if (n_probes == 0) return cudaSuccess;
     note_launches();
-    const size_t smem = JOIN_WARPS * (MAXP + (vmode == 3 ? 32 * VSTRIDE : 0)) * sizeof(uint32_t);
+    const size_t smem = JOIN_WARPS * verify_smem_words(vmode) * sizeof(uint32_t);
     int per_sm = 0;
     cudaError_t e;
     if (vmode == 3) {

@@ -242,6 +242,34 @@ cudaError_t mlp_train(float* w, float* mom, float* vel, float* g, const float* x
                       int n, float denom, int steps, float lr, float weight_decay, float* loss_trace,
                       cudaStream_t s);
 
+// ---- ring.cu ---------------------------------------------------------------
+// The candidate ring: records (probe, n, begin) and candidate ids in device
+// rings the host fills; see ring.cu.
+struct RingRec {
+    uint32_t probe;       // probe set id (of S)
+    uint32_t n;           // candidates of this record
+    unsigned long long begin;  // absolute position of its first candidate (mod cand_cap)
+};
+enum RingStatus : unsigned int { RING_RUNNING = 0, RING_CLOSED = 1, RING_TIMEOUT = 2 };
+struct RingView {
+    const unsigned long long* tail;   // records published by the host
+    const unsigned long long* close;  // non-zero: stop once the published records are verified
+    unsigned long long* claim;        // next record to verify
+    unsigned long long* head;         // records verified: a contiguous prefix
+    unsigned long long* done;         // [rec_cap] record index + 1 once that record is verified
+    unsigned int* status;             // the launch's exit status (RingStatus, atomicMax)
+    const RingRec* recs;              // [rec_cap]
+    const uint32_t* cands;            // [cand_cap]
+    unsigned long long rec_cap, cand_cap;  // powers of two
+    unsigned long long wait_ns;       // a warp waits this long for a published record, then gives up
+};
+// One persistent launch (a block per SM) consuming the ring until close or
+// the wait limit; vmode 2 = a warp per candidate, otherwise the staged lane mode.
+cudaError_t launch_ring_consumer(CollView R, CollView S, BoundsView B, const RingView& V, int vmode, Sink out,
+                                 int sm_count, cudaStream_t s);
+// *word = value, ordered on stream s (publishes the ring's tail and close words).
+cudaError_t ring_store(unsigned long long* word, unsigned long long value, cudaStream_t s);
+
 // Explicit candidate lists (hybrid::device_handler): probes[i] owns candidates
 // [i ? offsets[i-1] : 0, offsets[i]).
 cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const uint32_t* probes,

@@ -75,10 +75,10 @@ hyset_status hyset_collection_parse(hyset_ctx* ctx, const char* text, uint64_t n
     if (n_bytes && (reinterpret_cast<uintptr_t>(d_text) & 15u)) {  // tiles load 16-byte words
         DevBuf aligned;
         CK(aligned.ensure(n_bytes + 16, s));
-        CK(cudaMemcpyAsync(aligned.p, d_text, n_bytes, cudaMemcpyDeviceToDevice, s));
-        staged.release(s);
-        staged = aligned;
-        aligned.p = nullptr;
+        std::swap(staged, aligned);  // staged (released by the guard on every return): the aligned copy
+        const cudaError_t e = cudaMemcpyAsync(staged.p, d_text, n_bytes, cudaMemcpyDeviceToDevice, s);
+        aligned.release(s);
+        CK(e);
         d_text = staged.as<uint8_t>();
     }
     const uint64_t tiles = parse_tiles(n_bytes);

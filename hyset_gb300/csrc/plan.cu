@@ -294,6 +294,7 @@ constexpr float TUNE_MARGIN = 0.92f;  // leave the rule's width only for an esti
 constexpr float TUNE_VMODE_MARGIN = 0.97f;  // warp verification only for an estimated gain of 3 % or more
 constexpr float TUNE_BATCH_MARGIN = 0.97f;  // a probe batch other than the default only for a gain of 3 % or more
 constexpr uint32_t TUNE_BATCHES[] = {1, 2, 3, 4, 6};  // probe batches the autotuner times
+constexpr float TUNE_BATCH_FULL_MS = 40.0f;  // batches are timed over the whole range up to this estimate
 }  // namespace
 
 // The signature width (and, when requested, the verification mode and the
@@ -420,20 +421,40 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     } else if (vm == 2) {
         ST(sample(2, &cur_ms));
     }
-    // probe batch: the other tile widths at the chosen width and mode; a
-    // width other than the default only for an estimated gain of 3 % or more
+    // probe batch: it trades loads in flight per warp against balance across
+    // warps, which samples of a few thousand batches cannot show (they do not
+    // fill the persistent launch), so the candidates run over the whole probe
+    // range, when the range's estimated kernel time makes that cheap; a batch
+    // other than the default only for a gain of 3 % or more
     uint32_t tb = base_batch;
     if (batch) {
-        float tb_ms = cur_ms;
-        for (uint32_t cand_b : TUNE_BATCHES) {
-            const uint32_t g = std::min(cand_b, grab_cap);
-            if (g == base_batch) continue;
-            P.grab = g;
-            float ms = 0;
-            ST(sample(vm, &ms));
-            if (ms < TUNE_BATCH_MARGIN * tb_ms && ms < TUNE_BATCH_MARGIN * cur_ms) {
-                tb = g;
-                tb_ms = ms;
+        if (cur_ms <= TUNE_BATCH_FULL_MS) {
+            auto whole = [&](uint32_t g, float* out) -> hyset_status {
+                P.grab = g;
+                P.p_lo = p_lo;
+                P.p_hi = p_hi;
+                CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+                CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
+                CK(cudaEventRecord(ctx->ek0, s));
+                CK(launch_join(P, TECH_FGSS, vm, ctx->sm_count, s));
+                CK(cudaEventRecord(ctx->ek1, s));
+                CK(cudaEventSynchronize(ctx->ek1));
+                CK(cudaEventElapsedTime(out, ctx->ek0, ctx->ek1));
+                return HYSET_OK;
+            };
+            float base_ms = 0;
+            ST(whole(base_batch, &base_ms));  // warms the caches the other runs find warm too
+            ST(whole(base_batch, &base_ms));
+            float tb_ms = base_ms;
+            for (uint32_t cand_b : TUNE_BATCHES) {
+                const uint32_t g = std::min(cand_b, grab_cap);
+                if (g == base_batch) continue;
+                float ms = 0;
+                ST(whole(g, &ms));
+                if (ms < TUNE_BATCH_MARGIN * base_ms && ms < tb_ms) {
+                    tb = g;
+                    tb_ms = ms;
+                }
             }
         }
         P.grab = base_batch;

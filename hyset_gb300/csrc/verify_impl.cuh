@@ -1,0 +1,115 @@
+// verify_impl.cuh — verification of explicit candidate lists
+// (hybrid::kernels::scenario_1 / scenario_2, include/hyset/hybrid_kernels.hpp:14-165):
+// one warp takes a probe and its candidates, 32 at a time.  Shared by the
+// batch verifier (k_verify_candidates, join.cu) and the persistent consumer of
+// the candidate ring (ring.cu).
+#pragma once
+#include "join_impl.cuh"
+
+namespace hs {
+namespace {
+
+// Staged lane-serial merge: b's first VSTAGE tokens are in `head` (shared
+// memory), the rest in global memory; same early-exit bounds as verify_serial.
+constexpr uint32_t VSTAGE = 16;            // candidate tokens staged per candidate
+constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fall in distinct banks
+
+// Shared-memory words one warp needs: the probe, plus the staged candidate
+// prefixes in mode 3.
+__host__ __device__ constexpr uint32_t verify_smem_words(int vmode) {
+    return MAXP + (vmode == 3 ? 32 * VSTRIDE : 0);
+}
+
+__device__ __forceinline__ bool verify_staged(const uint32_t* a, uint32_t na, const uint32_t* head,
+                                              const uint32_t* __restrict__ b, uint32_t nb, uint32_t thr) {
+    uint32_t i = 0, k = 0, found = 0, maxa = na, maxb = nb;
+    while (maxa >= thr && maxb >= thr && found < thr) {
+        const uint32_t x = a[i], y = k < VSTAGE ? head[k] : __ldg(b + k);
+        if (x == y) {
+            ++i;
+            ++k;
+            ++found;
+        } else if (x < y) {
+            ++i;
+            --maxa;
+        } else {
+            ++k;
+            --maxb;
+        }
+    }
+    return found >= thr;
+}
+
+// Verifies probe p of S against the n candidates cand_at(0..n-1) of R and
+// appends (p, c) for every pair with overlap >= minoverlap.  VMODE 1: a lane
+// per candidate; 2: the warp per candidate (merge-path steps of 32 tokens);
+// 3: a lane per candidate, merging from 16-token prefixes staged with
+// coalesced loads.  sbuf: this warp's verify_smem_words(VMODE) words.  All 32
+// lanes call it with the same arguments.
+template <int VMODE, typename CandAt>
+__device__ __forceinline__ void verify_probe_list(const CollView& R, const CollView& S, const BoundsView& B,
+                                                  uint32_t p, CandAt cand_at, uint32_t n, const Sink& out,
+                                                  uint32_t* sbuf, int lane) {
+    const uint2 pm = S.meta[p];
+    const uint32_t lp = pm.y;
+    const uint32_t* pg = S.tokens + pm.x;
+    const uint32_t* a = pg;
+    if (lp <= MAXP) {
+        for (uint32_t k = lane; k < lp; k += 32) sbuf[k] = pg[k];
+        __syncwarp();
+        a = sbuf;
+    }
+    for (uint32_t k0 = 0; k0 < n; k0 += 32) {
+        const uint32_t k = k0 + lane;
+        bool keep = k < n;
+        uint32_t c = 0, lc = 0, mo = 0, cs = 0;
+        if (keep) {
+            c = cand_at(k);
+            const uint2 cm = R.meta[c];
+            cs = cm.x;
+            lc = cm.y;
+            // hybrid_kernels.hpp:50: minoverlap(probe, candidate), for any pair
+            // (an incompatible length pair gets min(lp, lc)).
+            const uint32_t big = max(lp, lc), small = min(lp, lc);
+            if (small >= B.minsize[big]) mo = minoverlap(B, big, small);
+            else mo = small;
+        }
+        if constexpr (VMODE == 1) {
+            bool ok = keep && verify_serial(a, lp, R.tokens + cs, lc, mo, NOWN);
+            emit(out, ok, p, c, lane);
+        } else if constexpr (VMODE == 3) {
+            // the first VSTAGE tokens of the round's 32 candidates arrive with
+            // 16 coalesced loads (two candidates per load, one per half-warp);
+            // each lane then merges its candidate out of shared memory and
+            // reads global memory only past the staged prefix
+            uint32_t* tile = sbuf + MAXP;
+            const uint32_t t = lane & (VSTAGE - 1);
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const int j = 2 * r + (lane >> 4);
+                const uint32_t cj = __shfl_sync(FULL, cs, j), lj = __shfl_sync(FULL, keep ? lc : 0u, j);
+                if (t < lj) tile[j * VSTRIDE + t] = __ldg(R.tokens + cj + t);
+            }
+            __syncwarp();
+            const bool ok = keep && verify_staged(a, lp, tile + lane * VSTRIDE, R.tokens + cs, lc, mo);
+            __syncwarp();
+            emit(out, ok, p, c, lane);
+        } else {
+            unsigned m = __ballot_sync(FULL, keep);
+            while (m) {
+                int src = __ffs(m) - 1;
+                m &= m - 1;
+                uint32_t cc = __shfl_sync(FULL, c, src);
+                uint32_t c2 = __shfl_sync(FULL, cs, src);
+                uint32_t ll = __shfl_sync(FULL, lc, src);
+                uint32_t mm = __shfl_sync(FULL, mo, src);
+                bool ok = verify_warp(a, lp, R.tokens + c2, ll, mm, NOWN, lane);
+                emit(out, ok && lane == 0, p, cc, lane);
+            }
+        }
+    }
+    __syncwarp();
+}
+
+}  // namespace
+}  // namespace hs

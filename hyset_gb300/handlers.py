@@ -126,6 +126,16 @@ class DeviceHandler:
     def set_max_set_size(self, size: int) -> None:
         """Kept for interface parity; probes longer than the shared-memory stage are read from HBM."""
 
+    def set_wait_limit(self, microseconds: int) -> None:
+        """How long the persistent verifier kernel waits for published
+        candidates before it ends (the next publication starts it again)."""
+        check(self._lib.hyset_verifier_set_wait(self.handle, int(microseconds)), self._ctx.handle)
+
+    def status(self) -> int:
+        """0, or 5 (HYSET_E_TIMEOUT) when the last verifier kernel ended
+        because no candidates arrived within the wait limit."""
+        return int(self._lib.hyset_verifier_status(self.handle))
+
     def set_output_handler(self, output: OutputHandler) -> None:
         self.output = output
 

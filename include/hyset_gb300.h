@@ -239,7 +239,16 @@ void hyset_handler_destroy(hyset_handler* h);
 /* ---- candidate verifier (hybrid::device_handler) ------------------- */
 /* hybrid::device_handler(indexed, probe, threads, scenario, aggregate, maxProbes,
  * maxCandidates, threshold)   include/hyset/hybrid_algorithms.hpp:41-62.
- * scenario 1 = one lane per candidate, 2 = one warp per candidate (merge-path). */
+ * scenario 1 = one lane per candidate, 2 = one warp per candidate (merge-path).
+ * The reference copies a host batch synchronously and verifies it on a
+ * worker thread (hybrid_algorithms.hpp:107-193).  Here candidates stream
+ * through device-resident rings (records: max_probes rounded up to a power of
+ * two; candidate ids: max_candidates rounded up) that a persistent kernel,
+ * started at creation, verifies as they are published: adding candidates
+ * copies them asynchronously and returns, waiting only when the rings are
+ * full or the pair buffer (max_candidates pairs) must be drained.  The kernel
+ * waits for the producer at most the wait limit (default 100 ms) and then ends
+ * (the next publication starts it again); every device wait is bounded. */
 hyset_status hyset_verifier_create(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
                                    hyset_sim sim, uint32_t threads, uint32_t scenario, int aggregate,
                                    uint32_t max_probes, uint32_t max_candidates, double threshold,
@@ -247,8 +256,17 @@ hyset_status hyset_verifier_create(hyset_ctx* ctx, const hyset_coll* indexed, co
 /* device_handler::addCandidates(probeID, candidate_set&)  hybrid_algorithms.hpp:71-105 */
 hyset_status hyset_verifier_add_candidates(hyset_verifier* v, uint32_t probe_id, const uint32_t* candidates,
                                            uint32_t n_candidates);
-/* device_handler::flush()  hybrid_algorithms.hpp:195-200 */
+/* device_handler::flush()  hybrid_algorithms.hpp:195-200: verifies everything
+ * added so far and appends its pairs (or count) to the output.  Returns
+ * HYSET_E_TIMEOUT if the device made no progress for 60 s. */
 hyset_status hyset_verifier_flush(hyset_verifier* v);
+/* No counterpart in the reference.  How long the persistent verifier kernel
+ * waits for published candidates before it ends (from its next start on). */
+hyset_status hyset_verifier_set_wait(hyset_verifier* v, uint64_t microseconds);
+/* No counterpart in the reference.  HYSET_E_TIMEOUT when the last verifier
+ * kernel ended because the producer published nothing within the wait limit
+ * (the next publication starts a new one), else HYSET_OK. */
+hyset_status hyset_verifier_status(hyset_verifier* v);
 hyset_status hyset_verifier_output(const hyset_verifier* v, uint64_t* count, const hyset_pair** pairs);
 void hyset_verifier_destroy(hyset_verifier* v);
 /* Device-resident candidate lists (the input of hybrid::device_handler's
