@@ -21,6 +21,12 @@ constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per
 #ifndef HS_SHORT_LIST
 #define HS_SHORT_LIST 8
 #endif
+#ifndef HS_SIGVEC
+#define HS_SIGVEC 0  // signatures read 16 bytes at a time (even widths)
+#endif
+#ifndef HS_WSEARCH
+#define HS_WSEARCH 1  // list window search: 1 = one round of loads up to SHORT_LIST, else bisection
+#endif
 constexpr uint32_t SHORT_LIST = HS_SHORT_LIST;  // inverted lists this short are windowed without bisection
 
 struct Window {
@@ -131,6 +137,28 @@ __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p,
     count_stat<ST>(P, 6, used, lane);
 }
 
+// Hamming distance of two W-word signatures.  A set's signature starts on a
+// multiple of 8 W bytes (the array is 256-byte aligned), so for even W the
+// words are read 16 bytes at a time.
+template <int W>
+__device__ __forceinline__ uint32_t sig_distance(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b) {
+    uint32_t pop = 0;
+#if HS_SIGVEC
+    if constexpr (W % 2 == 0) {
+#pragma unroll
+        for (int w = 0; w < W; w += 2) {
+            const ulonglong2 x = __ldg(reinterpret_cast<const ulonglong2*>(a + w));
+            const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2*>(b + w));
+            pop += __popcll(x.x ^ y.x) + __popcll(x.y ^ y.y);
+        }
+        return pop;
+    }
+#endif
+#pragma unroll
+    for (int w = 0; w < W; ++w) pop += __popcll(__ldg(a + w) ^ __ldg(b + w));
+    return pop;
+}
+
 // Lane k of the warp holds the k-th value of a non-decreasing inclusive scan;
 // returns the first lane whose value exceeds q (q < the warp total).
 __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
@@ -199,6 +227,40 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 if (P.X.sorted) {
                     const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
                     const uint32_t len = b1 - b0;
+#if HS_WSEARCH == 2
+                    if (len <= 4 * SHORT_LIST) {
+                        // two rounds of independent loads: three samples cut the
+                        // list in quarters of q <= SHORT_LIST entries, then the
+                        // quarter holding each bound is read whole (one quarter
+                        // when both bounds fall in it)
+                        const uint32_t q = len > SHORT_LIST ? (len + 3) >> 2 : len;
+                        uint32_t clo = 0, chi = 0;
+                        if (len > SHORT_LIST) {
+                            const uint32_t s1 = __ldg(x_set + b0 + q), s2 = __ldg(x_set + b0 + 2 * q);
+                            const uint32_t s3 = 3 * q < len ? __ldg(x_set + b0 + 3 * q) : 0xFFFFFFFFu;
+                            clo = (s1 < klo) + (s2 < klo) + (s3 < klo);
+                            chi = (s1 < khi) + (s2 < khi) + (s3 < khi);
+                        }
+                        const uint32_t lo0 = clo * q, hi0 = chi * q;
+                        uint32_t vl[SHORT_LIST], vh[SHORT_LIST];
+#pragma unroll
+                        for (int k = 0; k < (int)SHORT_LIST; ++k) {
+                            vl[k] = (uint32_t)k < q && lo0 + k < len ? __ldg(x_set + b0 + lo0 + k) : 0xFFFFFFFFu;
+                            vh[k] = chi != clo && (uint32_t)k < q && hi0 + k < len ? __ldg(x_set + b0 + hi0 + k)
+                                                                                  : 0xFFFFFFFFu;
+                        }
+                        uint32_t nlo = lo0, nhi = hi0;
+#pragma unroll
+                        for (int k = 0; k < (int)SHORT_LIST; ++k) {
+                            nlo += vl[k] < klo;
+                            nhi += (chi != clo ? vh[k] : vl[k]) < khi;
+                        }
+                        b1 = b0 + nhi;
+                        b0 = b0 + nlo;
+                    } else {
+                        lower_bound2_u32(x_set, b0, b1, klo, khi, b0, b1);
+                    }
+#else
                     if (len <= SHORT_LIST) {
                         // one round trip: independent loads instead of dependent bisection
                         uint32_t v[SHORT_LIST];
@@ -216,6 +278,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                     } else {
                         lower_bound2_u32(x_set, b0, b1, klo, khi, b0, b1);
                     }
+#endif
                 }
                 first = b0;
                 cnt = b1 - b0;
@@ -258,10 +321,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             if (keep) {
                 const uint2 cm = P.R.meta[c];
                 if constexpr (early_sig) {
-                    const uint64_t* bs = P.bits_S + (uint64_t)ip * W;
-                    const uint64_t* bc = P.bits_R + (uint64_t)c * W;
-#pragma unroll
-                    for (int w = 0; w < W; ++w) pop += __popcll(__ldg(bs + w) ^ __ldg(bc + w));
+                    pop = sig_distance<W>(P.bits_S + (uint64_t)ip * W, P.bits_R + (uint64_t)c * W);
                 }
                 cstart = cm.x;
                 lc = cm.y;
@@ -272,12 +332,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             count_stat<ST>(P, 0, q < total ? 1u : 0u, lane);
             count_stat<ST>(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
             if constexpr (W > 4) {
-                if (keep) {
-                    const uint64_t* bs = P.bits_S + (uint64_t)ip * W;
-                    const uint64_t* bc = P.bits_R + (uint64_t)c * W;
-#pragma unroll
-                    for (int w = 0; w < W; ++w) pop += __popcll(__ldg(bs + w) ^ __ldg(bc + w));
-                }
+                if (keep) pop = sig_distance<W>(P.bits_S + (uint64_t)ip * W, P.bits_R + (uint64_t)c * W);
             }
             if constexpr (W > 0) keep = keep && ilp + lc - pop >= 2u * mo;
             count_stat<ST>(P, 1, keep ? 1u : 0u, lane);
