@@ -21,8 +21,14 @@ constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per
 #ifndef HS_SHORT_LIST
 #define HS_SHORT_LIST 8
 #endif
+#ifndef HS_SPECIALIZE
+#define HS_SPECIALIZE 0  // the probe-major kernel carries a second copy of the filter for plain indexes
+#endif
+#ifndef HS_GUIDED
+#define HS_GUIDED 0  // work counters claimed in guided chunks instead of one batch per atomic
+#endif
 #ifndef HS_SIGVEC
-#define HS_SIGVEC 0  // signatures read 16 bytes at a time (even widths)
+#define HS_SIGVEC 1  // signatures read 16 bytes at a time (even widths)
 #endif
 #ifndef HS_WSEARCH
 #define HS_WSEARCH 1  // list window search: 1 = one round of loads up to SHORT_LIST, else bisection
@@ -180,11 +186,17 @@ __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
 // candidates of probe t at least as long as the probe (its midprefix tokens
 // against the maxprefix index X), lane k + t the shorter ones (its maxprefix
 // tokens against the midprefix index X2).
-template <int VMODE, int W, bool ST>
+//
+// PLAIN (compile time): one packed, set-id-sorted index and no bands (every
+// self-join, and R-S joins whose bounds do not allow bands); the general form
+// also serves unsorted block indexes, unpacked entries and banded joins.
+// Leaving their branches and shuffles out of the common case saves issue
+// slots, which bound this kernel.
+template <int VMODE, int W, bool ST, bool PLAIN>
 __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
     // lane t < k: probe t of the batch (largest sets first)
     uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
-    const bool banded = P.X2.set != nullptr;
+    const bool banded = !PLAIN && P.X2.set != nullptr;
     const uint32_t t_probe = banded && (uint32_t)lane >= k ? (uint32_t)lane - k : (uint32_t)lane;
     if (t_probe < k && (banded || (uint32_t)lane < k)) {
         band = (uint32_t)lane >= k ? 1u : 0u;
@@ -216,7 +228,8 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
         const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp);
         const uint32_t t_pst = __shfl_sync(FULL, pst, t);
         const uint32_t t_lo = __shfl_sync(FULL, lo, t), t_hi = __shfl_sync(FULL, hi, t);
-        const uint32_t t_band = __shfl_sync(FULL, band, t);
+        uint32_t t_band = 0;
+        if constexpr (!PLAIN) t_band = __shfl_sync(FULL, band, t);
         const uint32_t* __restrict__ x_off = t_band ? P.X2.list_off : P.X.list_off;
         const uint32_t* __restrict__ x_set = t_band ? P.X2.set : P.X.set;
         uint32_t first = 0, cnt = 0;
@@ -224,7 +237,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             const uint32_t tok = __ldg(P.S.tokens + t_pst + j);
             if (tok < P.X.universe) {
                 uint32_t b0 = x_off[tok], b1 = x_off[tok + 1];
-                if (P.X.sorted) {
+                if (PLAIN || P.X.sorted) {
                     const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
                     const uint32_t len = b1 - b0;
 #if HS_WSEARCH == 2
@@ -299,20 +312,24 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             const uint32_t ip = __shfl_sync(FULL, p, it);
             const uint32_t ilp = __shfl_sync(FULL, lp, it);
             const uint32_t ipst = __shfl_sync(FULL, pst, it);
-            const uint32_t ilo = __shfl_sync(FULL, lo, it), ihi = __shfl_sync(FULL, hi, it);
-            const uint32_t iband = __shfl_sync(FULL, band, it);
+            uint32_t ilo = 0, ihi = 0, iband = 0;
+            if constexpr (!PLAIN) {
+                ilo = __shfl_sync(FULL, lo, it);
+                ihi = __shfl_sync(FULL, hi, it);
+                iband = __shfl_sync(FULL, band, it);
+            }
             const uint32_t e = f_jj + ((keep ? q : 0) - (i_jj - c_jj));
             uint32_t c = 0, pc = 0, lc = 0, mo = 0, cstart = 0, pop = 0;
             if (keep) {
                 const uint32_t v = (iband ? P.X2.set : P.X.set)[e];
-                if (P.X.pos) {
+                if (!PLAIN && P.X.pos) {
                     c = v;
                     pc = (iband ? P.X2.pos : P.X.pos)[e];
                 } else {
                     c = v >> P.X.pos_bits;
                     pc = v & ((1u << P.X.pos_bits) - 1u);
                 }
-                if (!P.X.sorted) keep = c >= ilo && c < ihi;
+                if (!PLAIN && !P.X.sorted) keep = c >= ilo && c < ihi;
             }
             // Signatures up to 256 bits are loaded with the candidate's meta (one
             // round trip); wider ones only for items that pass the positional
