@@ -37,46 +37,19 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     uint32_t* sbuf = smem + warp * MAXP;
     const uint32_t nprobe = P.p_hi - P.p_lo;
     const uint32_t grab = P.grab ? P.grab : 1;
-    const bool plain = P.X2.set == nullptr && P.X.sorted && P.X.pos == nullptr;  // see fgss_batch
     uint32_t i = 0, i_end = 0;
-#if HS_GUIDED
-    // guided self-scheduling: a warp takes about 1/(8 warps) of the work it
-    // saw remaining at its last claim (whole batches, 1..16 of them), so the
-    // shared counter sees several times fewer atomics early on and single
-    // batches at the end
-    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
-    uint32_t seen = 0;
-#endif
     for (;;) {
         if (i >= i_end) {
-#if HS_GUIDED
-            uint32_t want = grab;
-            if (lane == 0) {
-                const uint32_t rem = nprobe > seen ? nprobe - seen : 0u;
-                want = min(max(rem / (warps_total * 8u) / grab, 1u), 16u) * grab;
-                i = atomicAdd(P.work, want);
-                seen = i + want;
-            }
-            i = __shfl_sync(FULL, i, 0);
-            want = __shfl_sync(FULL, want, 0);
-            i_end = min(nprobe, i + want);
-#else
             const uint32_t steal = grab * HS_JOIN_STEAL;  // probes per atomic on the shared counter
             if (lane == 0) i = atomicAdd(P.work, steal);
             i = __shfl_sync(FULL, i, 0);
             i_end = min(nprobe, i + steal);
-#endif
         }
         if (i >= nprobe) break;
         const uint32_t end = min(i_end, i + grab);
         // largest sets first: the heaviest probes start early, the tail is light
         if constexpr (TECH == TECH_FGSS) {
-#if HS_SPECIALIZE
-            if (plain) fgss_batch<VMODE, W, ST, true>(P, i, end - i, lane);
-            else fgss_batch<VMODE, W, ST, false>(P, i, end - i, lane);
-#else
-            fgss_batch<VMODE, W, ST, false>(P, i, end - i, lane);
-#endif
+            fgss_batch<VMODE, W, ST>(P, i, end - i, lane);
         } else {
             for (uint32_t q = i; q < end; ++q) enum_probe<VMODE, W, ST>(P, P.p_hi - 1 - q, sbuf, lane);
         }
@@ -93,34 +66,16 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
                                                                     uint32_t n_probes, Sink out, unsigned int* work) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t* sbuf = smem + warp * verify_smem_words(VMODE);
-#if HS_GUIDED
-    const uint32_t warps_total = gridDim.x * (blockDim.x >> 5);
-    uint32_t seen = 0, i = 0, i_end = 0;
-    for (;; ++i) {
-        if (i >= i_end) {  // guided self-scheduling, as in k_join
-            uint32_t want = 1;
-            if (lane == 0) {
-                const uint32_t rem = n_probes > seen ? n_probes - seen : 0u;
-                want = min(max(rem / (warps_total * 8u), 1u), 16u);
-                i = atomicAdd(work, want);
-                seen = i + want;
-            }
-            i = __shfl_sync(FULL, i, 0);
-            i_end = min(n_probes, i + __shfl_sync(FULL, want, 0));
-        }
-        if (i >= n_probes) break;
-#else
+    uint32_t* sbuf = smem + warp * verify_smem_words(VMODE, VMAXP);
     for (;;) {
         uint32_t i = 0;
         if (lane == 0) i = atomicAdd(work, 1u);
         i = __shfl_sync(FULL, i, 0);
         if (i >= n_probes) break;
-#endif
         const uint32_t cb = i ? offsets[i - 1] : 0, ce = offsets[i];
         const uint32_t* list = cands + cb;
-        verify_probe_list<VMODE>(R, S, B, probes[i], [list](uint32_t k) { return list[k]; }, ce - cb, out, sbuf,
-                                 lane);
+        verify_probe_list<VMODE, VMAXP>(R, S, B, probes[i], [list](uint32_t k) { return list[k]; }, ce - cb, out,
+                                        sbuf, lane);
     }
 }
 
@@ -171,7 +126,7 @@ cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const
                                      Sink out, unsigned int* work, int sm_count, cudaStream_t s) {
     if (n_probes == 0) return cudaSuccess;
     note_launches();
-    const size_t smem = JOIN_WARPS * verify_smem_words(vmode) * sizeof(uint32_t);
+    const size_t smem = JOIN_WARPS * verify_smem_words(vmode, VMAXP) * sizeof(uint32_t);
     int per_sm = 0;
     cudaError_t e;
     if (vmode == 3) {

@@ -21,18 +21,7 @@ constexpr uint32_t MAXP = 768;       // probe tokens staged in shared memory per
 #ifndef HS_SHORT_LIST
 #define HS_SHORT_LIST 8
 #endif
-#ifndef HS_SPECIALIZE
-#define HS_SPECIALIZE 0  // the probe-major kernel carries a second copy of the filter for plain indexes
-#endif
-#ifndef HS_GUIDED
-#define HS_GUIDED 0  // work counters claimed in guided chunks instead of one batch per atomic
-#endif
-#ifndef HS_SIGVEC
-#define HS_SIGVEC 1  // signatures read 16 bytes at a time (even widths)
-#endif
-#ifndef HS_WSEARCH
-#define HS_WSEARCH 1  // list window search: 1 = one round of loads up to SHORT_LIST, else bisection
-#endif
+
 constexpr uint32_t SHORT_LIST = HS_SHORT_LIST;  // inverted lists this short are windowed without bisection
 
 struct Window {
@@ -149,7 +138,6 @@ __device__ __forceinline__ void verify_and_emit(const JoinParams& P, uint32_t p,
 template <int W>
 __device__ __forceinline__ uint32_t sig_distance(const uint64_t* __restrict__ a, const uint64_t* __restrict__ b) {
     uint32_t pop = 0;
-#if HS_SIGVEC
     if constexpr (W % 2 == 0) {
 #pragma unroll
         for (int w = 0; w < W; w += 2) {
@@ -157,11 +145,10 @@ __device__ __forceinline__ uint32_t sig_distance(const uint64_t* __restrict__ a,
             const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2*>(b + w));
             pop += __popcll(x.x ^ y.x) + __popcll(x.y ^ y.y);
         }
-        return pop;
-    }
-#endif
+    } else {
 #pragma unroll
-    for (int w = 0; w < W; ++w) pop += __popcll(__ldg(a + w) ^ __ldg(b + w));
+        for (int w = 0; w < W; ++w) pop += __popcll(__ldg(a + w) ^ __ldg(b + w));
+    }
     return pop;
 }
 
@@ -186,17 +173,11 @@ __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
 // candidates of probe t at least as long as the probe (its midprefix tokens
 // against the maxprefix index X), lane k + t the shorter ones (its maxprefix
 // tokens against the midprefix index X2).
-//
-// PLAIN (compile time): one packed, set-id-sorted index and no bands (every
-// self-join, and R-S joins whose bounds do not allow bands); the general form
-// also serves unsorted block indexes, unpacked entries and banded joins.
-// Leaving their branches and shuffles out of the common case saves issue
-// slots, which bound this kernel.
-template <int VMODE, int W, bool ST, bool PLAIN>
+template <int VMODE, int W, bool ST>
 __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
     // lane t < k: probe t of the batch (largest sets first)
     uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
-    const bool banded = !PLAIN && P.X2.set != nullptr;
+    const bool banded = P.X2.set != nullptr;
     const uint32_t t_probe = banded && (uint32_t)lane >= k ? (uint32_t)lane - k : (uint32_t)lane;
     if (t_probe < k && (banded || (uint32_t)lane < k)) {
         band = (uint32_t)lane >= k ? 1u : 0u;
@@ -228,8 +209,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
         const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp);
         const uint32_t t_pst = __shfl_sync(FULL, pst, t);
         const uint32_t t_lo = __shfl_sync(FULL, lo, t), t_hi = __shfl_sync(FULL, hi, t);
-        uint32_t t_band = 0;
-        if constexpr (!PLAIN) t_band = __shfl_sync(FULL, band, t);
+        const uint32_t t_band = __shfl_sync(FULL, band, t);
         const uint32_t* __restrict__ x_off = t_band ? P.X2.list_off : P.X.list_off;
         const uint32_t* __restrict__ x_set = t_band ? P.X2.set : P.X.set;
         uint32_t first = 0, cnt = 0;
@@ -237,43 +217,9 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             const uint32_t tok = __ldg(P.S.tokens + t_pst + j);
             if (tok < P.X.universe) {
                 uint32_t b0 = x_off[tok], b1 = x_off[tok + 1];
-                if (PLAIN || P.X.sorted) {
+                if (P.X.sorted) {
                     const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
                     const uint32_t len = b1 - b0;
-#if HS_WSEARCH == 2
-                    if (len <= 4 * SHORT_LIST) {
-                        // two rounds of independent loads: three samples cut the
-                        // list in quarters of q <= SHORT_LIST entries, then the
-                        // quarter holding each bound is read whole (one quarter
-                        // when both bounds fall in it)
-                        const uint32_t q = len > SHORT_LIST ? (len + 3) >> 2 : len;
-                        uint32_t clo = 0, chi = 0;
-                        if (len > SHORT_LIST) {
-                            const uint32_t s1 = __ldg(x_set + b0 + q), s2 = __ldg(x_set + b0 + 2 * q);
-                            const uint32_t s3 = 3 * q < len ? __ldg(x_set + b0 + 3 * q) : 0xFFFFFFFFu;
-                            clo = (s1 < klo) + (s2 < klo) + (s3 < klo);
-                            chi = (s1 < khi) + (s2 < khi) + (s3 < khi);
-                        }
-                        const uint32_t lo0 = clo * q, hi0 = chi * q;
-                        uint32_t vl[SHORT_LIST], vh[SHORT_LIST];
-#pragma unroll
-                        for (int k = 0; k < (int)SHORT_LIST; ++k) {
-                            vl[k] = (uint32_t)k < q && lo0 + k < len ? __ldg(x_set + b0 + lo0 + k) : 0xFFFFFFFFu;
-                            vh[k] = chi != clo && (uint32_t)k < q && hi0 + k < len ? __ldg(x_set + b0 + hi0 + k)
-                                                                                  : 0xFFFFFFFFu;
-                        }
-                        uint32_t nlo = lo0, nhi = hi0;
-#pragma unroll
-                        for (int k = 0; k < (int)SHORT_LIST; ++k) {
-                            nlo += vl[k] < klo;
-                            nhi += (chi != clo ? vh[k] : vl[k]) < khi;
-                        }
-                        b1 = b0 + nhi;
-                        b0 = b0 + nlo;
-                    } else {
-                        lower_bound2_u32(x_set, b0, b1, klo, khi, b0, b1);
-                    }
-#else
                     if (len <= SHORT_LIST) {
                         // one round trip: independent loads instead of dependent bisection
                         uint32_t v[SHORT_LIST];
@@ -291,7 +237,6 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                     } else {
                         lower_bound2_u32(x_set, b0, b1, klo, khi, b0, b1);
                     }
-#endif
                 }
                 first = b0;
                 cnt = b1 - b0;
@@ -312,24 +257,20 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             const uint32_t ip = __shfl_sync(FULL, p, it);
             const uint32_t ilp = __shfl_sync(FULL, lp, it);
             const uint32_t ipst = __shfl_sync(FULL, pst, it);
-            uint32_t ilo = 0, ihi = 0, iband = 0;
-            if constexpr (!PLAIN) {
-                ilo = __shfl_sync(FULL, lo, it);
-                ihi = __shfl_sync(FULL, hi, it);
-                iband = __shfl_sync(FULL, band, it);
-            }
+            const uint32_t ilo = __shfl_sync(FULL, lo, it), ihi = __shfl_sync(FULL, hi, it);
+            const uint32_t iband = __shfl_sync(FULL, band, it);
             const uint32_t e = f_jj + ((keep ? q : 0) - (i_jj - c_jj));
             uint32_t c = 0, pc = 0, lc = 0, mo = 0, cstart = 0, pop = 0;
             if (keep) {
                 const uint32_t v = (iband ? P.X2.set : P.X.set)[e];
-                if (!PLAIN && P.X.pos) {
+                if (P.X.pos) {
                     c = v;
                     pc = (iband ? P.X2.pos : P.X.pos)[e];
                 } else {
                     c = v >> P.X.pos_bits;
                     pc = v & ((1u << P.X.pos_bits) - 1u);
                 }
-                if (!PLAIN && !P.X.sorted) keep = c >= ilo && c < ihi;
+                if (!P.X.sorted) keep = c >= ilo && c < ihi;
             }
             // Signatures up to 256 bits are loaded with the candidate's meta (one
             // round trip); wider ones only for items that pass the positional

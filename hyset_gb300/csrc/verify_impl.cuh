@@ -14,10 +14,18 @@ namespace {
 constexpr uint32_t VSTAGE = 16;            // candidate tokens staged per candidate
 constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fall in distinct banks
 
-// Shared-memory words one warp needs: the probe, plus the staged candidate
-// prefixes in mode 3.
-__host__ __device__ constexpr uint32_t verify_smem_words(int vmode) {
-    return MAXP + (vmode == 3 ? 32 * VSTRIDE : 0);
+#ifndef HS_VMAXP
+#define HS_VMAXP 768
+#endif
+// Probe tokens the batch verifier stages in shared memory (longer probes are
+// merged from L1/L2).  Smaller than the join kernels' stage so that more warps
+// fit an SM: the verifier waits on gathers, and more resident warps hide them.
+constexpr uint32_t VMAXP = HS_VMAXP;
+
+// Shared-memory words one warp needs: the probe (pmax tokens), plus the
+// staged candidate prefixes in mode 3.
+__host__ __device__ constexpr uint32_t verify_smem_words(int vmode, uint32_t pmax = MAXP) {
+    return pmax + (vmode == 3 ? 32 * VSTRIDE : 0);
 }
 
 __device__ __forceinline__ bool verify_staged(const uint32_t* a, uint32_t na, const uint32_t* head,
@@ -44,9 +52,9 @@ __device__ __forceinline__ bool verify_staged(const uint32_t* a, uint32_t na, co
 // appends (p, c) for every pair with overlap >= minoverlap.  VMODE 1: a lane
 // per candidate; 2: the warp per candidate (merge-path steps of 32 tokens);
 // 3: a lane per candidate, merging from 16-token prefixes staged with
-// coalesced loads.  sbuf: this warp's verify_smem_words(VMODE) words.  All 32
-// lanes call it with the same arguments.
-template <int VMODE, typename CandAt>
+// coalesced loads.  sbuf: this warp's verify_smem_words(VMODE, PMAX) words.
+// All 32 lanes call it with the same arguments.
+template <int VMODE, uint32_t PMAX, typename CandAt>
 __device__ __forceinline__ void verify_probe_list(const CollView& R, const CollView& S, const BoundsView& B,
                                                   uint32_t p, CandAt cand_at, uint32_t n, const Sink& out,
                                                   uint32_t* sbuf, int lane) {
@@ -54,7 +62,7 @@ __device__ __forceinline__ void verify_probe_list(const CollView& R, const CollV
     const uint32_t lp = pm.y;
     const uint32_t* pg = S.tokens + pm.x;
     const uint32_t* a = pg;
-    if (lp <= MAXP) {
+    if (lp <= PMAX) {
         for (uint32_t k = lane; k < lp; k += 32) sbuf[k] = pg[k];
         __syncwarp();
         a = sbuf;
@@ -82,7 +90,7 @@ __device__ __forceinline__ void verify_probe_list(const CollView& R, const CollV
             // 16 coalesced loads (two candidates per load, one per half-warp);
             // each lane then merges its candidate out of shared memory and
             // reads global memory only past the staged prefix
-            uint32_t* tile = sbuf + MAXP;
+            uint32_t* tile = sbuf + PMAX;
             const uint32_t t = lane & (VSTAGE - 1);
 #pragma unroll
             for (int r = 0; r < 16; ++r) {
