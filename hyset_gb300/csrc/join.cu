@@ -58,8 +58,10 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
 }
 
 // Explicit candidate lists: probes[i] owns candidates [offsets[i-1], offsets[i]).
-template <int VMODE>
+template <int VMODE, int W>
 __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, CollView S, BoundsView B,
+                                                                    const uint64_t* __restrict__ sig_R,
+                                                                    const uint64_t* __restrict__ sig_S,
                                                                     const uint32_t* __restrict__ probes,
                                                                     const uint32_t* __restrict__ offsets,
                                                                     const uint32_t* __restrict__ cands,
@@ -74,8 +76,37 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
         if (i >= n_probes) break;
         const uint32_t cb = i ? offsets[i - 1] : 0, ce = offsets[i];
         const uint32_t* list = cands + cb;
-        verify_probe_list<VMODE, VMAXP>(R, S, B, probes[i], [list](uint32_t k) { return list[k]; }, ce - cb, out,
-                                        sbuf, lane);
+        verify_probe_list<VMODE, W, VMAXP>(R, S, B, sig_R, sig_S, probes[i], [list](uint32_t k) { return list[k]; },
+                                           ce - cb, out, sbuf, lane);
+    }
+}
+
+template <int VMODE, int W>
+cudaError_t launch_verify_w(CollView R, CollView S, BoundsView B, const uint64_t* sig_R, const uint64_t* sig_S,
+                            const uint32_t* probes, const uint32_t* offsets, const uint32_t* cands, uint32_t n_probes,
+                            Sink out, unsigned int* work, int sm_count, cudaStream_t s) {
+    const size_t smem = JOIN_WARPS * verify_smem_words(VMODE, VMAXP) * sizeof(uint32_t);
+    int per_sm = 0;
+    const cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verify_candidates<VMODE, W>, JOIN_THREADS, smem);
+    if (e != cudaSuccess) return e;
+    k_verify_candidates<VMODE, W><<<sm_count * (per_sm ? per_sm : 1), JOIN_THREADS, smem, s>>>(
+        R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work);
+    return cudaGetLastError();
+}
+
+template <int VMODE>
+cudaError_t launch_verify_v(int words, CollView R, CollView S, BoundsView B, const uint64_t* sig_R,
+                            const uint64_t* sig_S, const uint32_t* probes, const uint32_t* offsets,
+                            const uint32_t* cands, uint32_t n_probes, Sink out, unsigned int* work, int sm_count,
+                            cudaStream_t s) {
+    switch (sig_R && sig_S ? words : 0) {
+    case 0: return launch_verify_w<VMODE, 0>(R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    case 1: return launch_verify_w<VMODE, 1>(R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    case 2: return launch_verify_w<VMODE, 2>(R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    case 4: return launch_verify_w<VMODE, 4>(R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    case 8: return launch_verify_w<VMODE, 8>(R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    default: return cudaErrorInvalidValue;
     }
 }
 
@@ -123,29 +154,15 @@ cudaError_t launch_join(const JoinParams& P, int technique, int vmode, int sm_co
 
 cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const uint32_t* probes,
                                      const uint32_t* offsets, const uint32_t* cands, uint32_t n_probes, int vmode,
-                                     Sink out, unsigned int* work, int sm_count, cudaStream_t s) {
+                                     Sink out, unsigned int* work, int sm_count, cudaStream_t s, const uint64_t* sig_R,
+                                     const uint64_t* sig_S, int words) {
     if (n_probes == 0) return cudaSuccess;
     note_launches();
-    const size_t smem = JOIN_WARPS * verify_smem_words(vmode, VMAXP) * sizeof(uint32_t);
-    int per_sm = 0;
-    cudaError_t e;
-    if (vmode == 3) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verify_candidates<3>, JOIN_THREADS, smem);
-        if (e != cudaSuccess) return e;
-        k_verify_candidates<3><<<sm_count * (per_sm ? per_sm : 1), JOIN_THREADS, smem, s>>>(
-            R, S, B, probes, offsets, cands, n_probes, out, work);
-    } else if (vmode == 2) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verify_candidates<2>, JOIN_THREADS, smem);
-        if (e != cudaSuccess) return e;
-        k_verify_candidates<2><<<sm_count * (per_sm ? per_sm : 1), JOIN_THREADS, smem, s>>>(
-            R, S, B, probes, offsets, cands, n_probes, out, work);
-    } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_verify_candidates<1>, JOIN_THREADS, smem);
-        if (e != cudaSuccess) return e;
-        k_verify_candidates<1><<<sm_count * (per_sm ? per_sm : 1), JOIN_THREADS, smem, s>>>(
-            R, S, B, probes, offsets, cands, n_probes, out, work);
-    }
-    return cudaGetLastError();
+    if (vmode == 3)
+        return launch_verify_v<3>(words, R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    if (vmode == 2)
+        return launch_verify_v<2>(words, R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
+    return launch_verify_v<1>(words, R, S, B, sig_R, sig_S, probes, offsets, cands, n_probes, out, work, sm_count, s);
 }
 
 }  // namespace hs

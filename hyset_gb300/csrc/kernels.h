@@ -272,8 +272,12 @@ cudaError_t ring_store(unsigned long long* word, unsigned long long value, cudaS
 
 // Explicit candidate lists (hybrid::device_handler): probes[i] owns candidates
 // [i ? offsets[i-1] : 0, offsets[i]).
+// sig_R / sig_S (words per signature, 0 = none): the XOR-signature bound drops
+// candidates before any merge (the pairs do not change).
 cudaError_t launch_verify_candidates(CollView R, CollView S, BoundsView B, const uint32_t* probes,
                                      const uint32_t* offsets, const uint32_t* cands, uint32_t n_probes,
-                                     int vmode, Sink out, unsigned int* work, int sm_count, cudaStream_t s);
+                                     int vmode, Sink out, unsigned int* work, int sm_count, cudaStream_t s,
+                                     const uint64_t* sig_R = nullptr, const uint64_t* sig_S = nullptr,
+                                     int words = 0);
 
 }  // namespace hs

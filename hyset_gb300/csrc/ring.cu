@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(RING_THREADS) k_ring_consume(CollView R, CollV
         const uint4 rec = __ldcg(reinterpret_cast<const uint4*>(V.recs) + (c & rec_mask));
         const uint32_t* ring = V.cands;
         const unsigned long long base = (unsigned long long)rec.z | ((unsigned long long)rec.w << 32);
-        verify_probe_list<VMODE, MAXP>(R, S, B, rec.x,
+        verify_probe_list<VMODE, 0, MAXP>(R, S, B, nullptr, nullptr, rec.x,
                                  [ring, base, cand_mask](uint32_t k) { return __ldcg(ring + ((base + k) & cand_mask)); },
                                  rec.y, out, sbuf, lane);
         // the record is done: its pairs are written, then the flag, then the

@@ -274,13 +274,29 @@ hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, cons
     *out = nullptr;
     ST(check_opts(ctx, opts));
     CK(cudaSetDevice(ctx->device));
-    const hyset_coll* R = indexed;
-    const hyset_coll* S = probe ? probe : indexed;
+    hyset_coll* R = const_cast<hyset_coll*>(indexed);  // signature buffers live in the collections
+    hyset_coll* S = const_cast<hyset_coll*>(probe ? probe : indexed);
     Bounds* b = nullptr;
     ST(get_bounds(ctx, opts->sim, opts->threshold, std::max(R->max_size, S->max_size), 0, &b));
     auto res = std::make_unique<hyset_result>();
     cudaStream_t s = ctx->stream;
     const int vmode = opts->verify_mode ? (int)opts->verify_mode : 3;
+    // the signature bound first (technique AUTO or BITMAP; DIRECT merges every
+    // candidate, as the reference does): width from bitmap_bits, else 128 bits
+    // for mean set sizes up to 48 and 256 above; the signatures are generated
+    // here, inside the call's device time
+    int words = 0;
+    if (opts->technique != HYSET_TECH_DIRECT && opts->technique != HYSET_TECH_FGSS) {
+        const double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
+        words = opts->bitmap_bits ? (int)(opts->bitmap_bits / 64) : (avg <= 48.0 ? 2 : 4);
+    }
+    CK(cudaEventRecord(ctx->ev0, s));
+    const uint64_t *sig_r = nullptr, *sig_s = nullptr;
+    if (words && n_probes) {
+        ST(get_bitmaps(ctx, R, words, &sig_r));
+        if (S == R) sig_s = sig_r;
+        else ST(get_bitmaps(ctx, S, words, &sig_s));
+    }
     const int count_only = opts->count_only ? 1 : 0;
     uint64_t cap = opts->pair_capacity ? opts->pair_capacity : (1u << 20);
     CK(ctx->s_count.ensure(16, s));
@@ -293,15 +309,18 @@ hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, cons
         CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
         CK(cudaEventRecord(ctx->ek0, s));
         CK(launch_verify_candidates(R->view(), S->view(), b->view, d_probes, d_offsets, d_candidates, n_probes, vmode,
-                                    sk, ctx->s_work.as<unsigned int>(), ctx->sm_count, s));
+                                    sk, ctx->s_work.as<unsigned int>(), ctx->sm_count, s, sig_r, sig_s, words));
         CK(cudaEventRecord(ctx->ek1, s));
         unsigned long long count = 0;
         CK(cudaMemcpyAsync(&count, ctx->s_count.p, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
-        float kms = 0;
+        float kms = 0, dms = 0;
         CK(cudaEventElapsedTime(&kms, ctx->ek0, ctx->ek1));
-        res->kernel_ms = res->device_ms = kms;
+        CK(cudaEventElapsedTime(&dms, ctx->ev0, ctx->ek1));
+        res->kernel_ms = kms;
+        res->device_ms = dms;  // signatures (first attempt) and the verification
         res->verify_mode = (uint32_t)vmode;
+        res->bitmap_bits = (uint32_t)words * 64u;
         res->count = count;
         if (count_only || count <= cap) break;
         cap = count + count / 8 + 1024;
@@ -317,7 +336,7 @@ hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, cons
         CK(cudaStreamSynchronize(s));
         res->has_pairs = 1;
     }
-    res->technique = HYSET_TECH_DIRECT;
+    res->technique = words ? HYSET_TECH_BITMAP : HYSET_TECH_DIRECT;
     *out = res.release();
     return HYSET_OK;
 }

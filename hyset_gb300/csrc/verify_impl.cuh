@@ -15,7 +15,7 @@ constexpr uint32_t VSTAGE = 16;            // candidate tokens staged per candid
 constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fall in distinct banks
 
 #ifndef HS_VMAXP
-#define HS_VMAXP 768
+#define HS_VMAXP 384
 #endif
 // Probe tokens the batch verifier stages in shared memory (longer probes are
 // merged from L1/L2).  Smaller than the join kernels' stage so that more warps
@@ -52,20 +52,28 @@ __device__ __forceinline__ bool verify_staged(const uint32_t* a, uint32_t na, co
 // appends (p, c) for every pair with overlap >= minoverlap.  VMODE 1: a lane
 // per candidate; 2: the warp per candidate (merge-path steps of 32 tokens);
 // 3: a lane per candidate, merging from 16-token prefixes staged with
-// coalesced loads.  sbuf: this warp's verify_smem_words(VMODE, PMAX) words.
+// coalesced loads.  W > 0: before any merge, the XOR-signature bound of the
+// reference's bitmap filter (|r ∩ s| <= (|r| + |s| - popc(b_r ^ b_s)) / 2,
+// include/hyset/device_algorithms.hpp:104-113) drops candidates that cannot
+// reach minoverlap (W words per signature in sig_R / sig_S); a round whose
+// candidates all fail it stages and merges nothing, and the probe's tokens are
+// staged only when a round first needs them.  The bound is sound, so the pairs
+// do not change.  sbuf: this warp's verify_smem_words(VMODE, PMAX) words.
 // All 32 lanes call it with the same arguments.
-template <int VMODE, uint32_t PMAX, typename CandAt>
+template <int VMODE, int W, uint32_t PMAX, typename CandAt>
 __device__ __forceinline__ void verify_probe_list(const CollView& R, const CollView& S, const BoundsView& B,
-                                                  uint32_t p, CandAt cand_at, uint32_t n, const Sink& out,
-                                                  uint32_t* sbuf, int lane) {
+                                                  const uint64_t* __restrict__ sig_R,
+                                                  const uint64_t* __restrict__ sig_S, uint32_t p, CandAt cand_at,
+                                                  uint32_t n, const Sink& out, uint32_t* sbuf, int lane) {
     const uint2 pm = S.meta[p];
     const uint32_t lp = pm.y;
     const uint32_t* pg = S.tokens + pm.x;
     const uint32_t* a = pg;
-    if (lp <= PMAX) {
-        for (uint32_t k = lane; k < lp; k += 32) sbuf[k] = pg[k];
-        __syncwarp();
-        a = sbuf;
+    bool staged = false;
+    uint64_t ps[W > 0 ? W : 1];
+    if constexpr (W > 0) {
+#pragma unroll
+        for (int w = 0; w < W; ++w) ps[w] = __ldg(sig_S + (uint64_t)p * W + w);
     }
     for (uint32_t k0 = 0; k0 < n; k0 += 32) {
         const uint32_t k = k0 + lane;
@@ -81,6 +89,32 @@ __device__ __forceinline__ void verify_probe_list(const CollView& R, const CollV
             const uint32_t big = max(lp, lc), small = min(lp, lc);
             if (small >= B.minsize[big]) mo = minoverlap(B, big, small);
             else mo = small;
+            if constexpr (W > 0) {
+                uint32_t pop = 0;
+                const uint64_t* bc = sig_R + (uint64_t)c * W;
+                if constexpr (W % 2 == 0) {
+#pragma unroll
+                    for (int w = 0; w < W; w += 2) {
+                        const ulonglong2 y = __ldg(reinterpret_cast<const ulonglong2*>(bc + w));
+                        pop += __popcll(ps[w] ^ y.x) + __popcll(ps[w + 1] ^ y.y);
+                    }
+                } else {
+#pragma unroll
+                    for (int w = 0; w < W; ++w) pop += __popcll(ps[w] ^ __ldg(bc + w));
+                }
+                keep = lp + lc - pop >= 2u * mo;
+            }
+        }
+        if constexpr (W > 0) {
+            if (!__ballot_sync(FULL, keep)) continue;  // no candidate of the round can reach minoverlap
+        }
+        if (!staged) {  // the probe's tokens, once, when a round first merges
+            if (lp <= PMAX) {
+                for (uint32_t q = lane; q < lp; q += 32) sbuf[q] = pg[q];
+                __syncwarp();
+                a = sbuf;
+            }
+            staged = true;
         }
         if constexpr (VMODE == 1) {
             bool ok = keep && verify_serial(a, lp, R.tokens + cs, lc, mo, NOWN);

@@ -273,9 +273,14 @@ void hyset_verifier_destroy(hyset_verifier* v);
  * kernels, hybrid_kernels.hpp:14-165, already on the device): probe
  * d_probes[i] of `probe` (NULL = indexed) owns candidates [d_offsets[i-1]
  * (0 for i = 0), d_offsets[i]) of `indexed`; pairs with overlap >= minoverlap
- * are returned as a join result (kernel_ms = the verification launch).  Uses
- * opts->sim, threshold, verify_mode (0 = 3: one lane per candidate merging from
- * a staged 16-token prefix), count_only, pair_capacity and device_pairs. */
+ * are returned as a join result (kernel_ms = the verification launch,
+ * device_ms = the signatures and the launch).  Uses opts->sim, threshold,
+ * verify_mode (0 = 3: one lane per candidate merging from a staged 16-token
+ * prefix), count_only, pair_capacity, device_pairs, and technique: DIRECT
+ * merges every candidate (the reference's scenario kernels); AUTO or BITMAP
+ * first drops the candidates whose XOR signatures rule out minoverlap (the
+ * bound of device_algorithms.hpp:104-113; bitmap_bits wide, 0 = 128 bits for
+ * mean set sizes up to 48, else 256), which never changes the pairs. */
 hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, const hyset_coll* probe,
                                  const uint32_t* d_probes, const uint32_t* d_offsets, const uint32_t* d_candidates,
                                  uint32_t n_probes, const hyset_join_opts* opts, hyset_result** out);

@@ -187,15 +187,18 @@ def read_text(text: bytes):
     return tok[:nt.value].copy(), siz[:ns].copy(), int(ne.value)
 
 
-def verify_csr(coll, probes, offsets, cands, threshold, sim="jaccard"):
-    """(pairs, tokens read) of explicit candidate lists over one collection
-    (tokens, starts, sizes), verified as hybrid::device_handler's kernels do."""
+def verify_csr(coll, probes, offsets, cands, threshold, sim="jaccard", probe=None):
+    """(pairs, tokens read) of explicit candidate lists, verified as
+    hybrid::device_handler's kernels do: probes of `probe` (default: coll)
+    against candidates of coll, each a (tokens, starts, sizes) triple."""
     lib = _load()
     fn = lib.oracle_verify_csr
     fn.restype = C.c_void_p
     fn.argtypes = [U32P] * 9 + [C.c_uint32, C.c_int, C.c_double, C.POINTER(C.c_uint64)]
     t, tp = _p(coll[0]); s_, sp = _p(coll[1]); z, zp = _p(coll[2])
+    pc = probe if probe is not None else coll
+    t2, tp2 = _p(pc[0]); s2, sp2 = _p(pc[1]); z2, zp2 = _p(pc[2])
     pr, prp = _p(probes); of, ofp = _p(offsets); ca, cap = _p(cands)
     read = C.c_uint64()
-    out = _take(fn(tp, sp, zp, tp, sp, zp, prp, ofp, cap, len(pr), SIM[sim], float(threshold), C.byref(read)))
+    out = _take(fn(tp, sp, zp, tp2, sp2, zp2, prp, ofp, cap, len(pr), SIM[sim], float(threshold), C.byref(read)))
     return out, int(read.value)
