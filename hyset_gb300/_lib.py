@@ -110,6 +110,7 @@ PROTOTYPES = {
     "hyset_mlp_grad": (C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_void_p, C.c_void_p]),
     "hyset_mlp_train": (C.c_int, [C.c_void_p] * 5 + [C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_void_p]),
     "hyset_selector_set": (C.c_int, [C.c_void_p] * 5),
+    "hyset_width_selector_set": (C.c_int, [C.c_void_p] * 4),
     "hyset_result_selector": (C.c_int, [C.c_void_p]),
     "hyset_verify_candidates_noalloc": (C.c_int, [C.c_void_p] * 6 + [C.c_uint32] + [C.c_void_p] * 3 +
                                         [C.c_uint32, C.c_int, C.c_double, C.c_uint32, C.c_void_p, C.c_uint64,

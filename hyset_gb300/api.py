@@ -126,18 +126,24 @@ def _fptr(a):
 
 
 class Context:
-    def __init__(self, device: int = 0, selector: bool = True):
+    def __init__(self, device: int = 0, selector: bool = True, width: bool = True):
         """selector: install the shipped technique selector (learned network
-        and analytic cost model) for technique AUTO, if it is present."""
+        and analytic cost model) for technique AUTO, if it is present.
+        width: install the shipped signature-width network, if present."""
         self._lib = load()
         h = C.c_void_p()
         check(self._lib.hyset_create(device, C.byref(h)))
         self.handle = h
         self.selector_info = None
-        if selector:
+        self.width_info = None
+        if selector or width:
             from . import selector as _sel
+            from . import width_selector as _wsel
             try:
-                self.selector_info = _sel.install_shipped(self)
+                if selector:
+                    self.selector_info = _sel.install_shipped(self)
+                if width:
+                    self.width_info = _wsel.install_shipped(self)
             except Exception:
                 self.close()
                 raise
@@ -297,6 +303,14 @@ class Context:
                 keep.append(arr)
                 args.append(_fptr(arr))
         check(self._lib.hyset_selector_set(self.handle, *args), self.handle)
+
+    def width_selector_set(self, params=None, mean=None, scale=None):
+        """Installs (or with params None removes) the signature-width network."""
+        if params is None:
+            check(self._lib.hyset_width_selector_set(self.handle, None, None, None), self.handle)
+            return
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (params, mean, scale)]
+        check(self._lib.hyset_width_selector_set(self.handle, *[_fptr(a) for a in arrs]), self.handle)
 
     def batch_join(self, joins: Sequence[tuple]) -> list:
         """joins: (indexed, probe_or_None, opts_kwargs) triples."""

@@ -112,7 +112,7 @@ void hyset_destroy(hyset_ctx* ctx) {
         for (auto& kv : ctx->bounds) kv.second->dev.release(s);
         ctx->own.release(s);
         DevBuf* bufs[] = {&ctx->s_pairs, &ctx->s_count, &ctx->s_work, &ctx->s_stats, &ctx->s_flags,
-                          &ctx->d_mlp, &ctx->d_feat, &ctx->d_moments, &ctx->d_hist};
+                          &ctx->d_mlp, &ctx->d_feat, &ctx->d_moments, &ctx->d_hist, &ctx->d_width_mlp};
         for (DevBuf* b : bufs) b->release(s);
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);

@@ -157,6 +157,10 @@ struct hyset_ctx {
     float feat_mean[hs::MLP_IN] = {}, feat_scale[hs::MLP_IN] = {};
     double cost[3][9] = {};                   // per technique (bitmap, fgss, direct)
     hs::DevBuf d_mlp, d_feat, d_moments, d_hist;
+    // learned signature width (a second network of the same shape: log-time at 128, 256, 512 bits)
+    bool has_width_mlp = false;
+    float width_mean[hs::MLP_IN] = {}, width_scale[hs::MLP_IN] = {};
+    hs::DevBuf d_width_mlp;
     std::map<std::string, std::pair<hyset_technique, int>> select_cache;  // decision, selector
     struct TuneChoice {
         uint32_t bits = 0;   // signature width

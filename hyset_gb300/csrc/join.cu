@@ -57,6 +57,11 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     }
 }
 
+#ifndef HS_VCLAIM
+#define HS_VCLAIM 1
+#endif
+constexpr uint32_t VCLAIM = HS_VCLAIM;  // probes a warp of the batch verifier takes per atomic
+
 // Explicit candidate lists: probes[i] owns candidates [offsets[i-1], offsets[i]).
 template <int VMODE, int W>
 __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, CollView S, BoundsView B,
@@ -69,10 +74,13 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t* sbuf = smem + warp * verify_smem_words(VMODE, VMAXP);
-    for (;;) {
-        uint32_t i = 0;
-        if (lane == 0) i = atomicAdd(work, 1u);
-        i = __shfl_sync(FULL, i, 0);
+    uint32_t i = 0, i_end = 0;
+    for (;; ++i) {
+        if (i >= i_end) {  // VCLAIM probes per atomic on the shared counter
+            if (lane == 0) i = atomicAdd(work, (unsigned)VCLAIM);
+            i = __shfl_sync(FULL, i, 0);
+            i_end = min(n_probes, i + VCLAIM);
+        }
         if (i >= n_probes) break;
         const uint32_t cb = i ? offsets[i - 1] : 0, ce = offsets[i];
         const uint32_t* list = cands + cb;

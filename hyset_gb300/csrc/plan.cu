@@ -335,6 +335,7 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     float est[4] = {0, 0, 0, 0}, kern_est[4] = {0, 0, 0, 0};
     float best_ms = 0;
     uint32_t best = 256;
+    const bool learned = ctx->has_width_mlp;  // the width network replaces the width samples
     // estimated kernel time of the whole probe range with signature words w and
     // verification mode vm, from three samples (start, middle, end)
     auto sample = [&](int vm, float* out) -> hyset_status {
@@ -372,7 +373,22 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
         }
         return HYSET_OK;
     };
-    for (int k = 0; k < 4; ++k) {
+    if (learned) {
+        float f[MLP_IN], x[MLP_IN], y[MLP_OUT] = {0, 0, 0};
+        ST(compute_features(ctx, R, S, o, f, nullptr));
+        for (int k = 0; k < MLP_IN; ++k) x[k] = (f[k] - ctx->width_mean[k]) / ctx->width_scale[k];
+        CK(ctx->d_feat.ensure(256, s));
+        float* dx = ctx->d_feat.as<float>();
+        CK(cudaMemcpyAsync(dx, x, sizeof x, cudaMemcpyHostToDevice, s));
+        CK(mlp_forward(ctx->d_width_mlp.as<float>(), dx, 1, dx + 32, ctx->sm_count, s));
+        CK(cudaMemcpyAsync(y, dx + 32, sizeof y, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        int w = 0;
+        for (int k = 1; k < MLP_OUT; ++k)
+            if (y[k] < y[w]) w = k;
+        best = 128u << w;  // outputs: 128, 256, 512 bits
+    }
+    for (int k = learned ? 4 : 0; k < 4; ++k) {
         const int words = (int)(cand[k] / 64);
         P.words = words;
         P.bits_R = P.bits_S = nullptr;
@@ -399,21 +415,26 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
             best = cand[k];
         }
     }
-    // the rule's width (mean size <= 48: 128 bits, else 256) unless another is clearly faster
-    const uint32_t rule = (double)R->n_tokens / (double)std::max<uint32_t>(R->n, 1) <= 48.0 ? 128u : 256u;
-    const float rule_ms = est[rule == 128u ? 1 : 2];
-    if (best != rule && best_ms > TUNE_MARGIN * rule_ms) best = rule;
     const int kb = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
-    float cur_ms = kern_est[kb];  // the chosen configuration's estimated kernel time
+    if (!learned) {
+        // the rule's width (mean size <= 48: 128 bits, else 256) unless another is clearly faster
+        const uint32_t rule = (double)R->n_tokens / (double)std::max<uint32_t>(R->n, 1) <= 48.0 ? 128u : 256u;
+        const float rule_ms = est[rule == 128u ? 1 : 2];
+        if (best != rule && best_ms > TUNE_MARGIN * rule_ms) best = rule;
+    }
+    const int kc = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
+    (void)kb;
+    float cur_ms = kern_est[kc];  // the chosen configuration's estimated kernel time
     // verification: a lane per surviving item, or the warp per item when the
     // samples show it faster at the chosen width (long merges: low thresholds,
     // cosine); an explicit mode is kept
     int vm = o->verify_mode == 2 ? 2 : 1;
     ST(use_width(best));
+    if (learned) ST(sample(1, &cur_ms));  // the predicted width's own estimate (the base of the comparisons below)
     if (vmode) {
         float warp_ms = 0;
         ST(sample(2, &warp_ms));
-        if (warp_ms < TUNE_VMODE_MARGIN * kern_est[kb]) {
+        if (warp_ms < TUNE_VMODE_MARGIN * cur_ms) {
             vm = 2;
             cur_ms = warp_ms;
         }
@@ -587,6 +608,25 @@ hyset_status hyset_mlp_train(hyset_ctx* ctx, float* params, const float* x, cons
     }
     mlp_release(ctx, B);
     return st;
+}
+
+hyset_status hyset_width_selector_set(hyset_ctx* ctx, const float* params, const float* feature_mean,
+                                      const float* feature_scale) {
+    if (!ctx) return HYSET_E_INVALID;
+    CK(cudaSetDevice(ctx->device));
+    ctx->tune_cache.clear();
+    ctx->has_width_mlp = false;
+    if (!params) return HYSET_OK;
+    if (!feature_mean || !feature_scale) return fail(ctx, HYSET_E_INVALID, "normalisation missing");
+    for (int k = 0; k < MLP_IN; ++k)
+        if (!(feature_scale[k] > 0.f)) return fail(ctx, HYSET_E_INVALID, "feature scale must be > 0");
+    std::memcpy(ctx->width_mean, feature_mean, sizeof ctx->width_mean);
+    std::memcpy(ctx->width_scale, feature_scale, sizeof ctx->width_scale);
+    CK(ctx->d_width_mlp.ensure(MLP_PARAMS * 4, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->d_width_mlp.p, params, MLP_PARAMS * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->has_width_mlp = true;
+    return HYSET_OK;
 }
 
 hyset_status hyset_selector_set(hyset_ctx* ctx, const float* params, const float* feature_mean,

@@ -319,6 +319,14 @@ hyset_status hyset_mlp_train(hyset_ctx* ctx, float* params, const float* x, cons
  * c7 index + c8 bitmap| (NULL: none). */
 hyset_status hyset_selector_set(hyset_ctx* ctx, const float* params, const float* feature_mean,
                                 const float* feature_scale, const double* cost_coefficients);
+/* No counterpart in the reference.  Installs a second network of the same
+ * shape whose three outputs predict the prefix-filter join's log-time with
+ * 128-, 256- and 512-bit signatures (same features and normalisation form);
+ * with it, AUTO joins that tune their signature width take the predicted
+ * width instead of timing samples of every width (the verification mode and
+ * probe batch are still tuned).  params NULL removes it. */
+hyset_status hyset_width_selector_set(hyset_ctx* ctx, const float* params, const float* feature_mean,
+                                      const float* feature_scale);
 /* Which selector chose the result's technique: -1 explicit, 0 rules,
  * 1 analytic cost model, 2 learned network. */
 int hyset_result_selector(const hyset_result* r);

@@ -187,3 +187,56 @@ def test_learned_partition_split_keeps_the_pairs():
     np.testing.assert_array_equal(rs.pairs, exp[np.lexsort((exp[:, 1], exp[:, 0]))])
     assert sctx.self_join(coll, threshold=0.6, count_only=True).count == len(exp)
     sctx.close()
+
+
+@pytest.mark.gpu
+def test_width_network_sets_the_signature_width():
+    """A width network whose output biases favour one width makes AUTO join
+    with that width (no width samples); the pairs stay the oracle's."""
+    import hyset_gb300 as hs
+    import oracle
+    from hyset_gb300 import synth
+    from hyset_gb300.selector import init_params
+    c = synth.generate(synth.C2, n_sets=80000, seed=141)
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.7))
+    mean, scale = np.zeros(12, np.float32), np.ones(12, np.float32)
+    for k, bits in enumerate((128, 256, 512)):
+        p = init_params(0)
+        p[:-3] *= 0.0
+        p[-3:] = [5.0, 5.0, 5.0]
+        p[-3 + k] = -5.0
+        with hs.Context(0, width=False) as wctx:
+            wctx.width_selector_set(p, mean, scale)
+            coll = wctx.upload(c.tokens, c.sizes, c.starts)
+            r = wctx.self_join(coll, threshold=0.7)
+            assert r.technique == "fgss" and r.bitmap_bits == bits, (bits, r.bitmap_bits)
+            assert oracle.as_set(r.pairs) == exp
+
+
+def test_shipped_width_report_recomputes_from_samples():
+    """The width network's held-out regrets follow from its shipped timing
+    samples (recomputed here in float64), and name every chooser."""
+    wpath = os.path.join(ROOT, "hyset_gb300", "width_weights.json")
+    spath = os.path.join(ROOT, "hyset_gb300", "width_samples.json")
+    if not (os.path.exists(wpath) and os.path.exists(spath)):
+        pytest.skip("no trained width network shipped yet")
+    from oracle import mlp
+    from hyset_gb300.width_selector import TIMED, WIDTHS, rule_bits
+    with open(wpath) as f:
+        w = json.load(f)
+    with open(spath) as f:
+        rows = json.load(f)
+    held = rows[w["trained_on"]:]
+    assert len(held) == w["held_out"]
+    x = (np.array([r["features"] for r in held]) - np.array(w["mean"])) / np.array(w["scale"])
+    y, _ = mlp.forward(np.array(w["params"]), x)
+    reg_net, reg_rule = [], []
+    for r, yy in zip(held, y):
+        ms = dict(zip(TIMED, r["ms"]))
+        best = min(ms.values())
+        reg_net.append(ms[WIDTHS[int(np.argmin(yy))]] / best - 1)
+        reg_rule.append(ms[rule_bits(r)] / best - 1)
+    rep = w["report"]["held_out"]
+    assert abs(np.mean(reg_rule) - rep["rule"]["mean_regret"]) < 1e-6
+    assert abs(np.mean(reg_net) - rep["network"]["mean_regret"]) < 0.02  # float32 GPU vs float64 argmin ties
+    assert set(rep) == {"network", "rule", "bits_256", "no_signatures", "autotuner"}
