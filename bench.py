@@ -13,8 +13,13 @@ resident in HBM (`value`), or through the public API from pinned host memory wit
 the pairs copied back (`e2e`).  Between timed steps a 512 MB buffer is written to
 flush the 129 MB L2.  The reference-shaped block-pair path (one launch per block
 pair, synchronous copies, as the reference's handlers do) is timed beside it as
-the plain baseline.  --impl reference times the reference algorithm on the host
-cores (the CPU oracle, cpu_multi semantics, all threads).  --sim cosine (or dice)
+the plain baseline.  Beside the headline, untimed by the step clock: the pair
+set against the oracle (`parity`), the plain single-launch prefix filter and
+the autotuner's configuration forced explicitly (`plain_single_launch_ms`,
+`autotuned_ms`, `auto_ms`), and the first 64 joins of the batched workload in
+one launch against one call at a time (`batch_leg`).  --impl reference times
+the reference algorithm on the host cores (the CPU oracle, cpu_multi
+semantics, all threads).  --sim cosine (or dice)
 runs the same workload under that similarity (no block-pair leg: the reference's
 handlers are Jaccard only).
 """
@@ -315,6 +320,8 @@ def run_ours(args, ws, rank, local):
     tuned_kw = dict(kw, technique="fgss", probe_major=True, bitmap=r.bitmap_bits, verify_mode=r.verify_mode,
                     fgss_batch=r.probe_batch or 0)
     legs = {"plain_single_launch_ms": leg_ms(plain_kw), "autotuned_ms": leg_ms(tuned_kw), "auto_ms": leg_ms(kw)}
+    # batching: the first 64 joins of the batched workload in one launch vs one call at a time
+    batch = None if args.no_batch or rank != 0 else batch_leg(ctx, 64, 3, 1, flush)
 
     out = None
     if rank == 0:
@@ -358,6 +365,7 @@ def run_ours(args, ws, rank, local):
                           **legs,
                           "speedup_vs_plain_single_launch": legs["plain_single_launch_ms"] / legs["auto_ms"],
                           "kernel_ms": kms},
+               "batch_leg": batch,
                "parity": parity["parity"], "parity_detail": parity,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                             "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
@@ -376,47 +384,63 @@ def run_ours(args, ws, rank, local):
     return out
 
 
-def run_batch(args):
+def batch_leg(ctx, n_joins, steps, warmup, flush):
+    """The batched workload's first `n_joins` joins (R-S joins of uneven sizes,
+    mixed similarities and thresholds): all in one persistent launch captured
+    in a CUDA graph (hyset_batch_join), against the same joins one call at a
+    time with the same AUTO configurations.  Device times, L2 flushed."""
     import torch
-    import hyset_gb300 as hs
-    t0 = time.time()
     from hyset_gb300 import synth
-    work = synth.batch_workload(args.joins)
+    t0 = time.time()
+    work = synth.batch_workload(n_joins)
     gen_s = time.time() - t0
-    ctx = hs.Context(0)
     joins, colls = [], []
     for (rt, rs, rz), (st, ss, sz), kw in work:
         R = ctx.upload(rt, rz, rs)
         S = ctx.upload(st, sz, ss)
         colls += [R, S]
         joins.append((R, S, dict(kw, device_pairs=True)))
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    for _ in range(args.warmup):
+    res = ctx.batch_join(joins)  # plans, tunes and captures the batch
+    for _ in range(warmup):
         res = ctx.batch_join(joins)
-    batch_ms, seq_ms = [], []
-    for _ in range(args.steps):
+    batch_ms, seq_ms, launches = [], [], 0
+    for _ in range(steps):
         flush.fill_(1)
         torch.cuda.synchronize()
         res = ctx.batch_join(joins)
         batch_ms.append(res[0].device_ms)
     total = sum(r.count for r in res)
-    # the same joins one launch sequence at a time (each through its own self/rs call)
-    for _ in range(max(1, args.steps // 2)):
+    for _ in range(max(1, steps // 2)):
         flush.fill_(1)
         torch.cuda.synchronize()
         t = 0.0
         for R, S, kw in joins:
-            t += ctx.rs_join(R, S, **kw).device_ms
+            one = ctx.rs_join(R, S, **kw)
+            t += one.device_ms
+            launches += one.launches
         seq_ms.append(t)
+    sets = int(sum(c.n for c in colls))
+    for c in colls:
+        c.free()
     bm, sm = statistics.mean(batch_ms), statistics.mean(seq_ms)
+    return {"joins": n_joins, "sets": sets, "result_pairs": total, "batch_ms": bm, "one_at_a_time_ms": sm,
+            "speedup_vs_one_at_a_time": sm / bm, "one_at_a_time_launches": launches // max(1, steps // 2),
+            "generation_s": gen_s}
+
+
+def run_batch(args):
+    import torch
+    import hyset_gb300 as hs
+    ctx = hs.Context(0)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    leg = batch_leg(ctx, args.joins, args.steps, args.warmup, flush)
     print(json.dumps({"metric": "batched R-S joins: result pairs/s (one persistent launch in a CUDA graph)",
-                      "value": total / (bm / 1000.0), "unit": "pairs/s", "n_gpus": 1, "steps": args.steps,
-                      "warmup": args.warmup, "ms_per_step": bm, "higher_is_better": True,
+                      "value": leg["result_pairs"] / (leg["batch_ms"] / 1000.0), "unit": "pairs/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": leg["batch_ms"],
+                      "higher_is_better": True,
                       "config": {"workload": f"{args.joins} R-S joins, |R|,|S| log-uniform [1e3, 2e5], mean size "
                                              "log-uniform [8, 300], mixed similarity, threshold U[0.5, 0.95]",
-                                 "result_pairs": total, "sets": int(sum(c.n for c in colls)),
-                                 "one_at_a_time_ms": sm, "speedup_vs_one_at_a_time": sm / bm,
-                                 "generation_s": gen_s}}), flush=True)
+                                 **leg}}), flush=True)
 
 
 def run_parse(args):
@@ -696,6 +720,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-plain", action="store_true", help="skip the block-pair baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-join batch leg")
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
     ap.add_argument("--vmode", type=int, default=0,
