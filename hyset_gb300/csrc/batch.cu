@@ -19,7 +19,7 @@ namespace {
 template <int W>
 __device__ __forceinline__ void run_unit_words(const BatchDesc& d, uint32_t i0, uint32_t k, uint32_t* sbuf, int lane) {
     if (d.tech == TECH_FGSS) {
-        fgss_batch<1, W, false>(d.P, i0, k, lane);
+        fgss_batch<1, W, false, false>(d.P, i0, k, lane);  // batches index by lists
     } else {
         for (uint32_t i = i0; i < i0 + k; ++i) enum_probe<1, W, false>(d.P, d.P.p_hi - 1 - i, sbuf, lane);
     }

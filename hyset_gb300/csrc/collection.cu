@@ -177,9 +177,11 @@ void hyset_collection_free(hyset_ctx* ctx, hyset_coll* c) {
     c->sizes.release(s);
     c->meta.release(s);
     c->index.list_off.release(s);
+    c->index.rec.release(s);
     c->index.set.release(s);
     c->index.pos.release(s);
     c->index_mid.list_off.release(s);
+    c->index_mid.rec.release(s);
     c->index_mid.set.release(s);
     c->index_mid.pos.release(s);
     c->first_ge.release(s);

@@ -67,7 +67,7 @@ uint32_t bits_for(uint64_t v);
 int key_bits_for(uint32_t universe);
 hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, int kind, Index& ix,
                                 const std::vector<uint32_t>* pre = nullptr, const uint32_t* d_pre = nullptr,
-                                int force_pb = -1);
+                                int force_pb = -1, bool records_ok = false);
 bool use_bands(const Bounds* b, bool self);
 hyset_status build_fgss_indexes(hyset_ctx* ctx, hyset_coll* R, const Bounds* b, bool self, Index& ix, Index& ix_mid,
                                 JoinParams& P);

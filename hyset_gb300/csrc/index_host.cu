@@ -91,9 +91,14 @@ int key_bits_for(uint32_t universe) {
 // pre / d_pre: the prefix length table (default: the bounds' index prefix);
 // force_pb >= 0 fixes the layout (0 = unpacked, > 0 = packed with that many
 // position bits) so that two indexes of one join share it.
+// records_ok: the caller's kernel reads token records (REC_CAP); they are
+// built once the longest list of this prefix table is known to fit (it is
+// read back on the collection's first build with the table; that build's
+// lists are converted), afterwards directly from the prefix entries: one emit
+// pass and one ordering pass, no offsets, no scan.
 hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, int kind, Index& ix,
                                 const std::vector<uint32_t>* pre, const uint32_t* d_pre,
-                                int force_pb) {
+                                int force_pb, bool records_ok) {
     // Rebuilt on every join (buffers are reused): a join's timed device work
     // always includes its own index build.  Only asynchronous stream work once
     // the buffers are large enough, so a batch can capture it into a graph.
@@ -125,15 +130,40 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
     uint32_t* len = ctx->sc->len.as<uint32_t>();
     uint32_t* off = ctx->sc->off.as<uint32_t>();
     uint32_t* scr = ctx->sc->scan.as<uint32_t>();
-    CK(set_prefix_lengths(v, d_pre, 0, n, len, s));
-    CK(scan_exclusive(len, off, n, scr, s));
     // Packed entries (set << pb | position) when set ids up to n and positions
     // below the longest prefix fit 32 bits: the sorted values are the index.
     uint32_t max_pre = 1;
     for (size_t l = 0; l < c->size_hist.size(); ++l)
         if (c->size_hist[l]) max_pre = std::max(max_pre, (*pre)[l]);
     const uint32_t pb = force_pb > 0 ? (uint32_t)force_pb : bits_for(max_pre), sb = bits_for(n);
-    if (force_pb != 0 && pb + sb <= 32) {
+    const bool packed = force_pb != 0 && pb + sb <= 32;
+    // Records are sized from the longest list seen on an earlier build, so only
+    // collections whose tokens the library owns (immutable once uploaded) use
+    // them; a collection over caller memory can change between joins.
+    const bool owned = c->tokens.p != nullptr && c->d_tokens == c->tokens.as<uint32_t>();
+    const bool rec_fits = records_ok && packed && owned && (uint64_t)U <= REC_MAX_TOKENS;
+    ix.sim = b->sim;
+    ix.tau = b->tau;
+    ix.kind = kind;
+    ix.universe = U;
+    ix.entries = E;
+    ix.records = false;
+    if (rec_fits) {
+        const auto lk = c->list_longest.find(d_pre);
+        if (lk != c->list_longest.end() && lk->second <= REC_ENTRIES) {
+            uint32_t* counts = ctx->sc->counts.as<uint32_t>();
+            CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
+            CK(cudaMemsetAsync(counts, 0, (size_t)U * 4, s));
+            CK(emit_records(v, d_pre, pb, counts, ix.rec.as<uint32_t>(), U, s));
+            CK(order_records(counts, U, ix.rec.as<uint32_t>(), s));
+            ix.records = true;
+            ix.pos_bits = pb;
+            return HYSET_OK;
+        }
+    }
+    CK(set_prefix_lengths(v, d_pre, 0, n, len, s));
+    CK(scan_exclusive(len, off, n, scr, s));
+    if (packed) {
         uint32_t* counts = ctx->sc->counts.as<uint32_t>();
         CK(ctx->sc->gate.ensure(4, s));
         CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
@@ -143,16 +173,18 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
         CK(cudaStreamIsCapturing(s, &capturing));
         int& path = c->list_path[d_pre];
+        const bool read_back = path == 0 && capturing == cudaStreamCaptureStatusNone;
         CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts, ix.list_off.as<uint32_t>(),
                        ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(), ctx->sc->gate.as<uint32_t>(),
-                       key_bits_for(U), scr, s, &path,
-                       capturing == cudaStreamCaptureStatusNone ? ctx->h_flags + 15 : nullptr));
-        ix.sim = b->sim;
-        ix.tau = b->tau;
-        ix.kind = kind;
-        ix.universe = U;
-        ix.entries = E;
+                       key_bits_for(U), scr, s, &path, read_back ? ctx->h_flags + 15 : nullptr));
+        if (read_back && E) c->list_longest[d_pre] = ctx->h_flags[15];
         ix.pos_bits = pb;
+        if (rec_fits && E && read_back && ctx->h_flags[15] <= REC_ENTRIES) {
+            // this build's lists become records; later builds emit records directly
+            CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
+            CK(records_from_lists(ix.list_off.as<uint32_t>(), ix.set.as<uint32_t>(), U, ix.rec.as<uint32_t>(), s));
+            ix.records = true;
+        }
         return HYSET_OK;
     }
     CK(emit_prefix_entries(v, 0, n, off, len, ctx->sc->tok.as<uint32_t>(), ctx->sc->set.as<uint32_t>(),
@@ -187,11 +219,11 @@ bool use_bands(const Bounds* b, bool self) { return !self && b->mo_monotone; }
 // their views in P.
 hyset_status build_fgss_indexes(hyset_ctx* ctx, hyset_coll* R, const Bounds* b, bool self, Index& ix,
                                  Index& ix_mid, JoinParams& P) {
-    ST(build_sorted_index(ctx, R, b, self ? 0 : 1, ix));
+    ST(build_sorted_index(ctx, R, b, self ? 0 : 1, ix, nullptr, nullptr, -1, true));
     P.X = ix.view();
     P.X2 = IndexView{};
     if (use_bands(b, self)) {
-        ST(build_sorted_index(ctx, R, b, 2, ix_mid, &b->mid_prefix, b->view.mid_prefix, (int)ix.pos_bits));
+        ST(build_sorted_index(ctx, R, b, 2, ix_mid, &b->mid_prefix, b->view.mid_prefix, (int)ix.pos_bits, true));
         P.X2 = ix_mid.view();
     }
     return HYSET_OK;
@@ -230,7 +262,10 @@ hyset_status get_bitmaps(hyset_ctx* ctx, hyset_coll* c, int words, const uint64_
         CK(cudaEventRecord(ctx->ev_fork, ctx->stream));
         CK(cudaStreamWaitEvent(gen, ctx->ev_fork, 0));
     }
-    CK(generate_bitmaps(c->view(), words, d.as<uint64_t>(), gen ? gen : ctx->stream));
+    // beside the index build the generation takes a few blocks per SM (it is
+    // bandwidth-bound; the index build is latency-bound and needs the SMs)
+    const unsigned cap = gen && gen != ctx->stream ? (unsigned)(ctx->sm_count * HS_SIG_BLOCKS_PER_SM) : 0u;
+    CK(generate_bitmaps(c->view(), words, d.as<uint64_t>(), gen ? gen : ctx->stream, cap));
     *out = d.as<uint64_t>();
     return HYSET_OK;
 }

@@ -69,22 +69,32 @@ struct Bounds {
     BoundsView view{};
 };
 
+#ifndef HS_SIG_BLOCKS_PER_SM
+#define HS_SIG_BLOCKS_PER_SM 4  // blocks per SM of signature generation beside an index build (0: no cap)
+#endif
+#ifndef HS_STREAM_PRIO
+#define HS_STREAM_PRIO 1  // the context's stream at the highest priority, the auxiliary stream at the lowest
+#endif
+
 struct Index {
     int sim = -1;
     double tau = -1;
     int kind = -1;
     DevBuf list_off, set, pos;
+    DevBuf rec;             // token records (REC_CAP words per token) when records is set
+    bool records = false;
     uint32_t universe = 0;
     uint64_t entries = 0;
     uint32_t pos_bits = 0;  // > 0: packed (set << pos_bits) | position entries
     IndexView view() const {
         IndexView v;
         v.list_off = list_off.as<uint32_t>();
-        v.set = set.as<uint32_t>();
+        v.set = records ? rec.as<uint32_t>() : set.as<uint32_t>();
         v.pos = pos_bits ? nullptr : pos.as<uint32_t>();
         v.universe = universe;
         v.pos_bits = pos_bits;
         v.sorted = 1;
+        v.rec = records ? 1 : 0;
         return v;
     }
 };
@@ -194,6 +204,7 @@ struct hyset_coll {
     hs::DevBuf g_off, g_set, g_ps, g_cursor;  // token groups of the prefix entries (token-major join)
     std::map<int, hs::DevBuf> bitmaps;  // by words
     std::map<const uint32_t*, int> list_path;  // per prefix table: index lists built short (1) or by radix (2)
+    std::map<const uint32_t*, uint32_t> list_longest;  // per prefix table: the longest index list, once read back
     hs::CollView view() const { return hs::CollView{d_tokens, d_starts, d_sizes, meta.as<uint2>(), n}; }
 };
 

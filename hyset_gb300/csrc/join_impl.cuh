@@ -152,6 +152,42 @@ __device__ __forceinline__ uint32_t sig_distance(const uint64_t* __restrict__ a,
     return pop;
 }
 
+// One 32-byte load (sm_100 and later), non-coherent path: p must be 32-byte aligned.
+__device__ __forceinline__ void ldg256(const uint32_t* p, uint32_t (&w)[8]) {
+    asm("ld.global.nc.v8.u32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+        : "l"(p));
+}
+
+// Window [klo, khi) of a token record (length word, then ascending entries
+// padded with 0xFFFFFFFF; 128-byte aligned): the entries below each bound,
+// counted over 32-byte pieces of the one line, the first piece giving the
+// length and the others read only as far as it reaches (no search).
+__device__ __forceinline__ void record_window(const uint32_t* __restrict__ r, uint32_t klo, uint32_t khi,
+                                              uint32_t& nlo, uint32_t& nhi) {
+    uint32_t w[8];
+    ldg256(r, w);
+    const uint32_t len = w[0];
+    nlo = 0;
+    nhi = 0;
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+        nlo += w[q] < klo;
+        nhi += w[q] < khi;
+    }
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+        if (len > 8u * k - 1u) {
+            ldg256(r + 8 * k, w);
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                nlo += w[q] < klo;
+                nhi += w[q] < khi;
+            }
+        }
+    }
+}
+
 // Lane k of the warp holds the k-th value of a non-decreasing inclusive scan;
 // returns the first lane whose value exceeds q (q < the warp total).
 __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
@@ -173,7 +209,9 @@ __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
 // candidates of probe t at least as long as the probe (its midprefix tokens
 // against the maxprefix index X), lane k + t the shorter ones (its maxprefix
 // tokens against the midprefix index X2).
-template <int VMODE, int W, bool ST>
+// RC: the index may be token records (IndexView::rec, checked per launch);
+// without it the record path is not compiled.
+template <int VMODE, int W, bool ST, bool RC = true>
 __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
     // lane t < k: probe t of the batch (largest sets first)
     uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
@@ -215,7 +253,14 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
         uint32_t first = 0, cnt = 0;
         if (sv) {
             const uint32_t tok = __ldg(P.S.tokens + t_pst + j);
-            if (tok < P.X.universe) {
+            if (RC && tok < P.X.universe && (t_band ? P.X2.rec : P.X.rec)) {
+                static_assert(REC_CAP == 32, "record_window reads four 32-byte pieces");
+                const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
+                uint32_t nlo, nhi;
+                record_window(x_set + ((uint64_t)tok << 5), klo, khi, nlo, nhi);
+                first = (tok << 5) + 1 + nlo;
+                cnt = nhi - nlo;
+            } else if (tok < P.X.universe) {
                 uint32_t b0 = x_off[tok], b1 = x_off[tok + 1];
                 if (P.X.sorted) {
                     const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
@@ -293,6 +338,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 if (keep) pop = sig_distance<W>(P.bits_S + (uint64_t)ip * W, P.bits_R + (uint64_t)c * W);
             }
             if constexpr (W > 0) keep = keep && ilp + lc - pop >= 2u * mo;
+
             count_stat<ST>(P, 1, keep ? 1u : 0u, lane);
             count_stat<ST>(P, 2, keep ? lc : 0u, lane);
             // ---- verification: the probe is read from HBM/L2 (it was just touched)

@@ -107,6 +107,28 @@ cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uin
                                 uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s,
                                 uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu, uint32_t limit = 0xFFFFFFFFu);
 
+// Token records: when no list holds more than REC_ENTRIES entries, list t is
+// the fixed REC_CAP-word record rec[REC_CAP t, REC_CAP t + REC_CAP): word 0
+// the list's length, then its entries ascending and the rest 0xFFFFFFFF
+// (never a valid packed entry).  A probe finds its window in one 128-byte
+// line (32-byte loads, only as many as the length needs) and the build needs
+// no offsets: no scan, no scatter pass.
+constexpr uint32_t REC_CAP = 32;
+constexpr uint32_t REC_ENTRIES = REC_CAP - 1;
+constexpr uint64_t REC_MAX_TOKENS = 1ull << 25;  // records of larger universes would pass 4 GB
+// Record build, pass 1: the first prefix_tab[size] tokens of every set of c
+// become entries (set << pos_bits) | position, each taking slot
+// atomicAdd(&counts[token], 1) of its token's record (tokens below `limit`;
+// counts zeroed by the caller).  The slots follow no order.
+cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
+                         uint32_t limit, cudaStream_t s);
+// Pass 2: each record's min(counts[t], REC_ENTRIES) entries in ascending
+// order after its length word, padded with 0xFFFFFFFF.
+cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s);
+// Records from index lists already built (every list at most REC_ENTRIES long).
+cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
+                               cudaStream_t s);
+
 // Token histogram of n entries into counts[limit] (warp-aggregated atomics;
 // tokens >= limit are skipped; the counts are NOT zeroed here).
 cudaError_t token_histogram(const uint32_t* e_token, uint64_t n, uint32_t* counts, uint32_t limit, cudaStream_t s);
@@ -139,7 +161,9 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
 
 // XOR bitmap signatures, bit (token mod bits) per token
 // (include/hyset/device_algorithms.hpp:58-74), words = bits / 64 in {1,2,4,8}.
-cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s);
+// max_blocks > 0 caps the grid (signatures generated beside other work leave
+// it SMs).
+cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s, unsigned max_blocks = 0);
 
 // ---- join.cu --------------------------------------------------------------
 struct IndexView {
@@ -149,6 +173,7 @@ struct IndexView {
     uint32_t universe;
     uint32_t pos_bits;                      // packed layout: bits of the position field
     int sorted;                             // lists ordered by set id
+    int rec = 0;                            // token records: list t = set[REC_CAP t, REC_CAP (t + 1)) (see REC_CAP)
 };
 
 struct JoinParams {

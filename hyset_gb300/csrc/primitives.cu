@@ -288,7 +288,12 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 // stores coalesce, and the token loads of EMIT_ROUNDS (8) rounds are issued before
 // any of their stores.  Sets [lo, c.n): c, off and len are indexed by absolute
 // set id.  counts may be nullptr (no histogram).
+// REC: instead of the entry arrays, each entry goes straight into its token's
+// record (the histogram atomic returns its slot; tokens at or above `limit`
+// and slots past REC_ENTRIES are dropped); len is then the prefix-length table
+// indexed by set size and off is not read.
 constexpr int EMIT_ROUNDS = 8;
+template <bool REC>
 __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
                               uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit) {
@@ -297,9 +302,16 @@ __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restric
     for (uint32_t s0 = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; s0 < c.n; s0 += warps * 32u) {
         const uint32_t s = s0 + lane;
         const bool has = s < c.n;
-        const uint32_t l = has ? len[s] : 0u;
-        const uint32_t start = has ? c.meta[s].x : 0u;
-        const uint32_t o0 = __shfl_sync(FULL, has ? off[s] : 0u, 0);
+        uint32_t l, start, o0 = 0;
+        if constexpr (REC) {  // len is the prefix table by size; no offsets
+            const uint2 m = has ? c.meta[s] : make_uint2(0, 0);
+            l = has ? len[m.y] : 0u;
+            start = m.x;
+        } else {
+            l = has ? len[s] : 0u;
+            start = has ? c.meta[s].x : 0u;
+            o0 = __shfl_sync(FULL, has ? off[s] : 0u, 0);
+        }
         const uint32_t incl = warp_incl_scan(l, lane);
         const uint32_t total = __shfl_sync(FULL, incl, 31);
         for (uint32_t j0 = 0; j0 < total; j0 += 32 * EMIT_ROUNDS) {
@@ -319,6 +331,19 @@ __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restric
                 const uint32_t i = j - excl_k;
                 tok[u] = j < total ? __ldg(c.tokens + start_k + i) : 0u;
                 val[u] = ((s0 + (uint32_t)k) << pos_bits) | i;
+            }
+            if constexpr (REC) {
+                // every round's slot atomic is in flight before the first store
+                uint32_t slot[EMIT_ROUNDS];
+#pragma unroll
+                for (int u = 0; u < EMIT_ROUNDS; ++u) {
+                    const uint32_t j = j0 + 32u * u + lane;
+                    slot[u] = j < total && tok[u] < limit ? atomicAdd(&counts[tok[u]], 1u) : 0xFFFFFFFFu;
+                }
+#pragma unroll
+                for (int u = 0; u < EMIT_ROUNDS; ++u)
+                    if (slot[u] < REC_ENTRIES) e_val[(uint64_t)tok[u] * REC_CAP + 1 + slot[u]] = val[u];
+                continue;
             }
 #pragma unroll
             for (int u = 0; u < EMIT_ROUNDS; ++u) {
@@ -465,6 +490,81 @@ __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __re
             order_lists(in, out, stage, ls, le, 0, 16, lane);
             order_lists(in, out, stage, ls, le, 16, 32, lane);
         }
+    }
+}
+
+// Orders the token records: a warp takes 32 consecutive records, stages in
+// shared memory (a record per 33 words, so the lanes' sorts hit distinct
+// banks) the 16-byte quarters that hold its length word and entries, lane k
+// sorts record k by insertion (the atomic slots mostly follow emission order,
+// which is set order), pads it and writes its length word, and the warp
+// stores back every 32-byte piece a probe reads for that length (the piece
+// holding word 0 and as many more as the entries reach; see record_window).
+// Pieces past them are neither read nor written.
+constexpr int REC_THREADS = 256;
+__host__ __device__ constexpr uint32_t record_pieces(uint32_t n) { return n > 7u ? 1u + (n - 7u + 7u) / 8u : 1u; }
+__global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* __restrict__ counts, uint32_t U,
+                                                               uint32_t* __restrict__ rec) {
+    __shared__ uint32_t stage_all[REC_THREADS / 32][32 * 33];
+    const int lane = threadIdx.x & 31;
+    uint32_t* stage = stage_all[threadIdx.x >> 5];
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5 << 5; t0 < U;
+         t0 += (uint64_t)warps * 32) {
+        const uint32_t nrec = U - t0 < 32 ? (uint32_t)(U - t0) : 32u;
+        const uint32_t mine = (uint32_t)lane < nrec ? min(counts[t0 + lane], REC_ENTRIES) : 0u;
+        uint4* g = reinterpret_cast<uint4*>(rec + t0 * REC_CAP);
+        // quarter k: record k / 8, words 4 (k % 8) .. +3; read if it holds the length or an entry
+#pragma unroll
+        for (uint32_t it = 0; it < 8; ++it) {  // every lane takes every round: the shuffles stay converged
+            const uint32_t k = (uint32_t)lane + 32u * it;
+            const uint32_t n = __shfl_sync(FULL, mine, k >> 3);
+            if (k < nrec * 8 && 4 * (k & 7) < n + 1) {
+                const uint4 x = g[k];
+                uint32_t* d = stage + (k >> 3) * 33 + (k & 7) * 4;
+                d[0] = x.x, d[1] = x.y, d[2] = x.z, d[3] = x.w;
+            }
+        }
+        __syncwarp();
+        if ((uint32_t)lane < nrec) {
+            uint32_t* r = stage + lane * 33 + 1;  // the entries follow the length word
+            const uint32_t n = mine;
+            for (uint32_t i = 1; i < n; ++i) {
+                const uint32_t x = r[i];
+                uint32_t j = i;
+                for (; j > 0; --j) {
+                    const uint32_t y = r[j - 1];
+                    if (y < x) break;
+                    r[j] = y;
+                }
+                r[j] = x;
+            }
+            for (uint32_t i = n; i < 8 * record_pieces(n) - 1; ++i) r[i] = 0xFFFFFFFFu;
+            r[-1] = n;
+        }
+        __syncwarp();
+#pragma unroll
+        for (uint32_t it = 0; it < 8; ++it) {
+            const uint32_t k = (uint32_t)lane + 32u * it;
+            const uint32_t n = __shfl_sync(FULL, mine, k >> 3);
+            if (k < nrec * 8 && 4 * (k & 7) < 8 * record_pieces(n)) {
+                const uint32_t* d = stage + (k >> 3) * 33 + (k & 7) * 4;
+                g[k] = make_uint4(d[0], d[1], d[2], d[3]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+// Records from built lists: a warp per token, lane 0 writes the length, lane
+// i > 0 entry i - 1 or the pad.
+__global__ void k_records_from_lists(const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ vals,
+                                     uint32_t U, uint32_t* __restrict__ rec) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < U; t += warps) {
+        const uint32_t a = list_off[t], b = list_off[t + 1];
+        rec[t * REC_CAP + lane] = lane == 0 ? b - a : (a + lane - 1 < b ? vals[a + lane - 1] : 0xFFFFFFFFu);
     }
 }
 
@@ -728,8 +828,32 @@ cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uin
     note_launches();
     CollView v = c;
     v.n = hi;  // the kernel walks ids [lo, hi)
-    k_emit_packed<<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
-                                                                     e_val, counts, limit);  // a warp per 32 sets
+    k_emit_packed<false><<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
+                                                                            e_val, counts, limit);  // a warp per 32 sets
+    return cudaGetLastError();
+}
+
+cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
+                         uint32_t limit, cudaStream_t s) {
+    if (c.n == 0) return cudaSuccess;
+    note_launches();
+    k_emit_packed<true><<<grid_for((uint64_t)c.n, 256), 256, 0, s>>>(c, 0, nullptr, prefix_tab, pos_bits, nullptr, rec,
+                                                                     counts, limit);
+    return cudaGetLastError();
+}
+
+cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s) {
+    if (U == 0) return cudaSuccess;
+    note_launches();
+    k_order_records<<<grid_for(((uint64_t)U + 31) / 32 * 32, REC_THREADS), REC_THREADS, 0, s>>>(counts, U, rec);
+    return cudaGetLastError();
+}
+
+cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
+                               cudaStream_t s) {
+    if (U == 0) return cudaSuccess;
+    note_launches();
+    k_records_from_lists<<<grid_for((uint64_t)U * 32, 256), 256, 0, s>>>(list_off, vals, U, rec);
     return cudaGetLastError();
 }
 
@@ -849,9 +973,10 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
     return cudaGetLastError();
 }
 
-cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s) {
+cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s, unsigned max_blocks) {
     if (c.n == 0) return cudaSuccess;
     unsigned g = grid_for((uint64_t)c.n * 8, BITMAP_THREADS);
+    if (max_blocks && g > max_blocks) g = max_blocks;
     note_launches();
     switch (words) {
     case 1: k_bitmaps<1><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;

@@ -7,7 +7,8 @@ sort in shared memory, or in global memory when the 32 lists exceed the stage);
 a longer list sends the whole build through the stable radix passes.  The
 choice is made on the device from the longest list, so both sides of the bound
 are checked here against the oracle, with a token planted in the prefix of
-exactly 64 and 65 sets."""
+exactly 64 and 65 sets.  Lists of at most 32 entries in a collection the
+library owns become token records for the single-join kernel (31 and 32)."""
 import numpy as np
 import pytest
 
@@ -67,6 +68,23 @@ def test_lists_on_both_sides_of_the_bound(ctx, k):
     r = ctx.self_join_host(c.tokens, c.sizes, c.starts, threshold=0.8, technique="fgss", probe_major=True,
                            bitmap=256)
     assert oracle.as_set(r.pairs) == exp
+
+
+@pytest.mark.parametrize("k", [31, 32])
+def test_token_records_on_both_sides_of_their_bound(ctx, k):
+    """Lists of at most 31 entries become fixed 32-word token records (a
+    length word and the entries): the collection's first build converts its
+    sorted lists, later builds emit the records directly (an atomic slot per
+    entry, then each record ordered).  A planted token in exactly 31 and 32
+    prefixes puts the collection on either side; every join of the sequence
+    must give the oracle's pairs."""
+    c = _plant(synth.generate(synth.C2, n_sets=20000, seed=64), k, seed=k)
+    assert _longest_list(c, 0.8) == k
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.8))
+    coll = ctx.upload(c.tokens, c.sizes, c.starts)
+    for kw in (dict(bitmap=0), dict(bitmap=256), dict(bitmap=512, verify_mode=2), dict(bitmap=0, fgss_batch=1)):
+        r = ctx.self_join(coll, threshold=0.8, technique="fgss", probe_major=True, **kw)
+        assert r.count == len(exp) and oracle.as_set(r.pairs) == exp, kw
 
 
 @pytest.mark.parametrize("n,tau", [(10000, 0.5), (200000, 0.6), (200000, 0.8)])
