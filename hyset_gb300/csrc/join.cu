@@ -26,6 +26,10 @@
 #include "join_impl.cuh"
 #include "verify_impl.cuh"
 
+#ifndef HS_ITEM_CARRY
+#define HS_ITEM_CARRY 1  // probe-major FGSS: items carried until a round of 32 is full (fgss_carry)
+#endif
+
 namespace hs {
 
 namespace {
@@ -38,6 +42,7 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     const uint32_t nprobe = P.p_hi - P.p_lo;
     const uint32_t grab = P.grab ? P.grab : 1;
     uint32_t i = 0, i_end = 0;
+    ItemCarry ic;  // FGSS with HS_ITEM_CARRY: items pending across slot rounds and batches
     for (;;) {
         if (i >= i_end) {
             const uint32_t steal = grab * HS_JOIN_STEAL;  // probes per atomic on the shared counter
@@ -49,12 +54,14 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
         const uint32_t end = min(i_end, i + grab);
         // largest sets first: the heaviest probes start early, the tail is light
         if constexpr (TECH == TECH_FGSS) {
-            fgss_batch<VMODE, W, ST>(P, i, end - i, lane);
+            if constexpr (HS_ITEM_CARRY) fgss_carry<VMODE, W, ST>(P, i, end - i, lane, ic);
+            else fgss_batch<VMODE, W, ST>(P, i, end - i, lane);
         } else {
             for (uint32_t q = i; q < end; ++q) enum_probe<VMODE, W, ST>(P, P.p_hi - 1 - q, sbuf, lane);
         }
         i = end;
     }
+    if constexpr (TECH == TECH_FGSS && HS_ITEM_CARRY) flush_items<VMODE, W, ST>(P, ic, lane);
 }
 
 #ifndef HS_VCLAIM

@@ -1,5 +1,6 @@
-// join_impl.cuh — per-probe filter + verify routines shared by the single-join
-// kernel (join.cu) and the batched multi-join kernel (batch.cu).
+// join_impl.cuh — per-probe filter + verify routines of the single-join kernel
+// (join.cu: fgss_carry, enum_probe) and the batched multi-join kernel
+// (batch.cu: fgss_batch, enum_probe).
 #pragma once
 #include "kernels.h"
 
@@ -364,6 +365,208 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 }
             }
             count_stat<ST>(P, 6, used, lane);
+        }
+    }
+}
+
+// ---- probe-major FGSS with full item rounds ---------------------------------
+//
+// fgss_batch runs the items of each slot round as soon as the round is
+// windowed, so most item rounds are partial (about 1.1 items per slot: one
+// full round and one of a few items per slot round, half the lanes idle).
+// fgss_carry keeps the last partial round's items in the lanes instead, each
+// lane holding everything its item needs (candidate, positions, probe id,
+// length and token offset), and fills the rest of the round from the next
+// slot round, or the next probe batch of the same launch: only full rounds
+// run until the warp's work ends (flush_items).
+
+constexpr uint32_t NO_ITEM = 0xFFFFFFFFu;
+
+struct ItemLane {  // one lane's pending item (c == NO_ITEM: none)
+    uint32_t c = NO_ITEM, pc = 0, jp = 0, ip = 0, ilp = 0, ipst = 0;
+};
+
+// Filters and verifies one round of items (the lanes whose c != NO_ITEM) and
+// appends the accepted pairs; every lane's item is consumed.
+template <int VMODE, int W, bool ST>
+__device__ __forceinline__ void run_items(const JoinParams& P, ItemLane& it, int lane) {
+    bool keep = it.c != NO_ITEM;
+    const uint32_t c = keep ? it.c : 0u, pc = it.pc, jp = it.jp, ip = it.ip, ilp = it.ilp;
+    uint32_t lc = 0, mo = 0, cstart = 0, pop = 0;
+    count_stat<ST>(P, 0, keep ? 1u : 0u, lane);
+    constexpr bool early_sig = W > 0 && W <= 4;  // as in fgss_batch
+    if (keep) {
+        const uint2 cm = P.R.meta[c];
+        if constexpr (early_sig) pop = sig_distance<W>(P.bits_S + (uint64_t)ip * W, P.bits_R + (uint64_t)c * W);
+        cstart = cm.x;
+        lc = cm.y;
+        const uint32_t big = max(ilp, lc), small = min(ilp, lc);
+        mo = minoverlap(P.B, big, small);
+        keep = 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
+    }
+    count_stat<ST>(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
+    if constexpr (W > 4) {
+        if (keep) pop = sig_distance<W>(P.bits_S + (uint64_t)ip * W, P.bits_R + (uint64_t)c * W);
+    }
+    if constexpr (W > 0) keep = keep && ilp + lc - pop >= 2u * mo;
+    count_stat<ST>(P, 1, keep ? 1u : 0u, lane);
+    count_stat<ST>(P, 2, keep ? lc : 0u, lane);
+    uint32_t used = 0;
+    if constexpr (VMODE == 1) {
+        bool ok = false;
+        if (keep) ok = verify_serial(P.S.tokens + it.ipst, ilp, P.R.tokens + cstart, lc, mo, jp, &used);
+        emit(P.out, ok, ip, c, lane);
+    } else {
+        unsigned m = __ballot_sync(FULL, keep);
+        while (m) {
+            const int src = __ffs(m) - 1;
+            m &= m - 1;
+            const uint32_t cc = __shfl_sync(FULL, c, src), cs = __shfl_sync(FULL, cstart, src);
+            const uint32_t ll = __shfl_sync(FULL, lc, src), mm = __shfl_sync(FULL, mo, src);
+            const uint32_t ob = __shfl_sync(FULL, pc, src), pp = __shfl_sync(FULL, ip, src);
+            const uint32_t pl = __shfl_sync(FULL, ilp, src), ps = __shfl_sync(FULL, it.ipst, src);
+            uint32_t u = 0;
+            const bool ok = verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
+            if (lane == 0) used += u;
+            emit(P.out, ok && lane == 0, pp, cc, lane);
+        }
+    }
+    count_stat<ST>(P, 6, used, lane);
+    it.c = NO_ITEM;
+}
+
+// The pending items of a warp (fewer than 32) and how many there are.
+struct ItemCarry {
+    ItemLane lane_item;
+    uint32_t pending = 0;  // warp-uniform: lanes [0, pending) hold an item
+};
+
+template <int VMODE, int W, bool ST>
+__device__ __forceinline__ void flush_items(const JoinParams& P, ItemCarry& ic, int lane) {
+    if (ic.pending) run_items<VMODE, W, ST>(P, ic.lane_item, lane);
+    ic.pending = 0;
+}
+
+template <int VMODE, int W, bool ST>
+__device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lane, ItemCarry& ic) {
+    // probes as in fgss_batch: lane t < k (banded R-S: lanes k + t too)
+    uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
+    const bool banded = P.X2.set != nullptr;
+    const uint32_t t_probe = banded && (uint32_t)lane >= k ? (uint32_t)lane - k : (uint32_t)lane;
+    if (t_probe < k && (banded || (uint32_t)lane < k)) {
+        band = (uint32_t)lane >= k ? 1u : 0u;
+        p = P.p_hi - 1 - (i0 + t_probe);
+        const uint2 pm = P.S.meta[p];
+        lp = pm.y;
+        pst = pm.x;
+        if (lp) {
+            const Window w = candidate_window(P, p, lp);
+            lo = w.lo;
+            hi = w.hi;
+            if (banded) {
+                const uint32_t mid = P.first_ge[min(lp, P.R_L + 1)];
+                if (band == 0) lo = max(lo, mid);
+                else hi = min(hi, mid);
+            }
+            if (lo < hi) mp = banded && band == 0 ? P.B.mid_prefix[lp] : P.B.probe_prefix[lp];
+        }
+    }
+    count_stat<ST>(P, 4, mp, lane);
+    const uint32_t mp_incl = warp_incl_scan(mp, lane);
+    const uint32_t slots = __shfl_sync(FULL, mp_incl, 31);
+    for (uint32_t s0 = 0; s0 < slots; s0 += 32) {
+        // ---- slot = (probe t, prefix position j): window of the token's list
+        const uint32_t sl = s0 + lane;
+        const bool sv = sl < slots;
+        const int t = scan_owner(mp_incl, sv ? sl : 0);
+        const uint32_t t_incl = __shfl_sync(FULL, mp_incl, t), t_mp = __shfl_sync(FULL, mp, t);
+        const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp);
+        const uint32_t t_pst = __shfl_sync(FULL, pst, t);
+        const uint32_t t_lo = __shfl_sync(FULL, lo, t), t_hi = __shfl_sync(FULL, hi, t);
+        const uint32_t t_band = __shfl_sync(FULL, band, t);
+        const uint32_t* __restrict__ x_off = t_band ? P.X2.list_off : P.X.list_off;
+        const uint32_t* __restrict__ x_set = t_band ? P.X2.set : P.X.set;
+        uint32_t first = 0, cnt = 0;
+        if (sv) {
+            const uint32_t tok = __ldg(P.S.tokens + t_pst + j);
+            if (tok < P.X.universe && (t_band ? P.X2.rec : P.X.rec)) {
+                const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
+                uint32_t nlo, nhi;
+                record_window(x_set + ((uint64_t)tok << 5), klo, khi, nlo, nhi);
+                first = (tok << 5) + 1 + nlo;
+                cnt = nhi - nlo;
+            } else if (tok < P.X.universe) {
+                uint32_t b0 = x_off[tok], b1 = x_off[tok + 1];
+                if (P.X.sorted) {
+                    const uint32_t klo = t_lo << P.X.pos_bits, khi = t_hi << P.X.pos_bits;
+                    const uint32_t len = b1 - b0;
+                    if (len <= SHORT_LIST) {
+                        uint32_t v[SHORT_LIST];
+#pragma unroll
+                        for (int q = 0; q < (int)SHORT_LIST; ++q)
+                            v[q] = (uint32_t)q < len ? __ldg(x_set + b0 + q) : 0xFFFFFFFFu;
+                        uint32_t nlo = 0, nhi = 0;
+#pragma unroll
+                        for (int q = 0; q < (int)SHORT_LIST; ++q) {
+                            nlo += v[q] < klo;
+                            nhi += v[q] < khi;
+                        }
+                        b1 = b0 + nhi;
+                        b0 = b0 + nlo;
+                    } else {
+                        lower_bound2_u32(x_set, b0, b1, klo, khi, b0, b1);
+                    }
+                }
+                first = b0;
+                cnt = b1 - b0;
+            }
+        }
+        const uint32_t incl = warp_incl_scan(cnt, lane);
+        const uint32_t total = __shfl_sync(FULL, incl, 31);
+        // ---- the round's items join the pending ones; every full round runs
+        uint32_t taken = 0;
+        while (taken < total) {
+            const uint32_t room = 32u - ic.pending;
+            const uint32_t take = min(room, total - taken);
+            // lanes [pending, pending + take) take items taken .. taken + take - 1
+            const bool mine = (uint32_t)lane >= ic.pending && (uint32_t)lane < ic.pending + take;
+            const uint32_t q = mine ? taken + (uint32_t)lane - ic.pending : 0u;
+            const int jj = scan_owner(incl, q);
+            const uint32_t f_jj = __shfl_sync(FULL, first, jj);
+            const uint32_t i_jj = __shfl_sync(FULL, incl, jj);
+            const uint32_t c_jj = __shfl_sync(FULL, cnt, jj);
+            const uint32_t jp = __shfl_sync(FULL, j, jj);
+            const int it = __shfl_sync(FULL, t, jj);
+            const uint32_t ip = __shfl_sync(FULL, p, it);
+            const uint32_t ilp = __shfl_sync(FULL, lp, it);
+            const uint32_t ipst = __shfl_sync(FULL, pst, it);
+            const uint32_t ilo = __shfl_sync(FULL, lo, it), ihi = __shfl_sync(FULL, hi, it);
+            const uint32_t iband = __shfl_sync(FULL, band, it);
+            if (mine) {
+                const uint32_t e = f_jj + (q - (i_jj - c_jj));
+                const uint32_t v = (iband ? P.X2.set : P.X.set)[e];
+                uint32_t c, pc;
+                if (P.X.pos) {
+                    c = v;
+                    pc = (iband ? P.X2.pos : P.X.pos)[e];
+                } else {
+                    c = v >> P.X.pos_bits;
+                    pc = v & ((1u << P.X.pos_bits) - 1u);
+                }
+                ItemLane& x = ic.lane_item;
+                x.c = (!P.X.sorted && (c < ilo || c >= ihi)) ? NO_ITEM : c;
+                x.pc = pc;
+                x.jp = jp;
+                x.ip = ip;
+                x.ilp = ilp;
+                x.ipst = ipst;
+            }
+            taken += take;
+            ic.pending += take;
+            if (ic.pending == 32u) {
+                run_items<VMODE, W, ST>(P, ic.lane_item, lane);
+                ic.pending = 0;
+            }
         }
     }
 }
