@@ -179,6 +179,7 @@ struct hyset_ctx {
     };
     std::map<std::string, TuneChoice> tune_cache;  // the autotuner's choices per join
     std::map<std::string, uint32_t> universe_cache;  // universe by collection size profile (host-input joins)
+    std::map<std::string, uint32_t> longest_cache;   // longest index list by join key (host-input joins)
     struct SplitPlan {
         uint32_t at;  // first probe id of the high range; 0 = no split
         hyset_technique low, high;

@@ -121,10 +121,14 @@ constexpr uint64_t REC_MAX_TOKENS = 1ull << 25;  // records of larger universes 
 // atomicAdd(&counts[token], 1) of its token's record (tokens below `limit`;
 // counts zeroed by the caller).  The slots follow no order.
 cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
-                         uint32_t limit, cudaStream_t s);
+                         uint32_t limit, cudaStream_t s, uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu);
 // Pass 2: each record's min(counts[t], REC_ENTRIES) entries in ascending
-// order after its length word, padded with 0xFFFFFFFF.
-cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s);
+// order after its length word, padded with 0xFFFFFFFF.  overflow (optional):
+// OR-ed with REC_OVERFLOW when a token had more entries than a record holds
+// (its record is then incomplete and the index must be built as lists).
+constexpr uint32_t REC_OVERFLOW = 16;
+cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s,
+                          uint32_t* overflow = nullptr);
 // Records from index lists already built (every list at most REC_ENTRIES long).
 cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
                                cudaStream_t s);

@@ -350,8 +350,6 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         uint32_t* len = ctx->sc->len.as<uint32_t>();
         uint32_t* off = ctx->sc->off.as<uint32_t>();
         CollView v = C->view();
-        CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
-        CK(scan_exclusive(len, off, n, ctx->sc->scan.as<uint32_t>(), s));
         const int words = (int)(tn.bits / 64);
         DevBuf& bits = C->bitmaps[words];
         if (words) CK(bits.ensure((size_t)n * words * 8 + 8, s));
@@ -369,6 +367,24 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             counts = ctx->sc->counts.as<uint32_t>();
             CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
         }
+        // Token records (see build_sorted_index) when a join with this key had
+        // lists short enough: the entries go straight into the records as the
+        // chunks land; the ordering pass flags a list that outgrew its record
+        // (this collection's tokens differ), and the join is then run again
+        // over lists.
+        auto lit = ctx->longest_cache.find(key);
+        bool records = assumed && lit != ctx->longest_cache.end() && lit->second <= REC_ENTRIES &&
+                       (uint64_t)U <= REC_MAX_TOKENS;
+        if (records) CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
+        bool lists_ready = false;  // prefix lengths and entry offsets computed
+        auto prepare_lists = [&]() -> hyset_status {
+            if (lists_ready) return HYSET_OK;
+            CK(set_prefix_lengths(v, b->view.index_prefix, 0, n, len, s));
+            CK(scan_exclusive(len, off, n, ctx->sc->scan.as<uint32_t>(), s));
+            lists_ready = true;
+            return HYSET_OK;
+        };
+        if (!records) ST(prepare_lists());
         uint32_t lo = 0;
         for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
             // sets whose tokens end inside the chunks copied so far
@@ -381,8 +397,11 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             part.meta += lo;
             part.n = hi - lo;
             CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
-            CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s, lo,
-                                   hi, U + 1));
+            if (records)
+                CK(emit_records(v, b->view.index_prefix, pb, counts, ix.rec.as<uint32_t>(), U, s, lo, hi));
+            else
+                CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s,
+                                       lo, hi, U + 1));
             if (words) CK(generate_bitmaps(part, words, bits.as<uint64_t>() + (size_t)lo * words, s));
             lo = hi;
         }
@@ -410,16 +429,24 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
             CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
             CK(ctx->sc->scan.ensure(std::max(scan_words, scan_scratch_words((uint64_t)U + 1)) * 4, s));
-            if (attempt > 0)  // the list build reordered the entries: emit them again
-                CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr, s));
-            counts = ctx->sc->counts.as<uint32_t>();
-            if (!(assumed && attempt == 0)) {  // not counted while the chunks landed
-                CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
-                CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
+            const bool rec_now = records && attempt == 0;
+            if (rec_now) {
+                CK(order_records(counts, U, ix.rec.as<uint32_t>(), s, ctx->s_flags.as<uint32_t>()));
+            } else {
+                ST(prepare_lists());
+                if (attempt > 0 || records)  // the list build reordered the entries (or none were emitted): emit them
+                    CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr,
+                                           s));
+                counts = ctx->sc->counts.as<uint32_t>();
+                if (!(assumed && attempt == 0)) {  // not counted while the chunks landed
+                    CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
+                    CK(token_histogram(ctx->sc->tok.as<uint32_t>(), E, counts, U + 1, s));
+                }
+                CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts,
+                               ix.list_off.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(),
+                               ctx->sc->gate.as<uint32_t>(), key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));
             }
-            CK(index_lists(ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), E, U, counts,
-                           ix.list_off.as<uint32_t>(), ctx->sc->altk.as<uint32_t>(), ctx->sc->altv.as<uint32_t>(),
-                           ctx->sc->gate.as<uint32_t>(), key_bits_for(U), ctx->sc->scan.as<uint32_t>(), s));
+            ix.records = rec_now;
             ix.sim = b->sim;
             ix.tau = b->tau;
             ix.kind = 0;
@@ -444,13 +471,18 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
                 P.words = words;
             }
             if (assumed) CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+            // the longest list (a list build with the device's choice writes it)
+            if (!rec_now) CK(cudaMemcpyAsync(f + 14, ctx->sc->gate.p, 4, cudaMemcpyDeviceToHost, s));
             const hyset_status js = run_join(ctx, P, TECH_FGSS, tn.vmode, o, res.get(), true);  // synchronises
             if (js != HYSET_OK) return bail(js);
+            if (!rec_now && E) ctx->longest_cache[key] = f[14];
             if (!assumed) break;
             const hyset_status vs = verdict();
             if (vs != HYSET_OK) return bail(vs);
-            if (f[1] + 1 <= U) break;  // every token was indexed: the join stands
-            U = f[1] + 1;              // a larger token: index and join again
+            const bool grown = rec_now && (f[0] & REC_OVERFLOW);  // a list outgrew its record
+            if (grown) ctx->longest_cache.erase(key);
+            if (f[1] + 1 <= U && !grown) break;  // every token was indexed: the join stands
+            U = std::max(U, f[1] + 1);  // a larger token or a longer list: index (as lists) and join again
             assumed = false;
         }
         C->universe = f[1] + 1;

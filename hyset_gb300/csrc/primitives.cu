@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __re
 constexpr int REC_THREADS = 256;
 __host__ __device__ constexpr uint32_t record_pieces(uint32_t n) { return n > 7u ? 1u + (n - 7u + 7u) / 8u : 1u; }
 __global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* __restrict__ counts, uint32_t U,
-                                                               uint32_t* __restrict__ rec) {
+                                                               uint32_t* __restrict__ rec, uint32_t* overflow) {
     __shared__ uint32_t stage_all[REC_THREADS / 32][32 * 33];
     const int lane = threadIdx.x & 31;
     uint32_t* stage = stage_all[threadIdx.x >> 5];
@@ -512,7 +512,9 @@ __global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* _
     for (uint64_t t0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5 << 5; t0 < U;
          t0 += (uint64_t)warps * 32) {
         const uint32_t nrec = U - t0 < 32 ? (uint32_t)(U - t0) : 32u;
-        const uint32_t mine = (uint32_t)lane < nrec ? min(counts[t0 + lane], REC_ENTRIES) : 0u;
+        const uint32_t cnt = (uint32_t)lane < nrec ? counts[t0 + lane] : 0u;
+        if (overflow && __any_sync(FULL, cnt > REC_ENTRIES) && lane == 0) atomicOr(overflow, REC_OVERFLOW);
+        const uint32_t mine = min(cnt, REC_ENTRIES);
         uint4* g = reinterpret_cast<uint4*>(rec + t0 * REC_CAP);
         // quarter k: record k / 8, words 4 (k % 8) .. +3; read if it holds the length or an entry
 #pragma unroll
@@ -834,18 +836,22 @@ cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uin
 }
 
 cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
-                         uint32_t limit, cudaStream_t s) {
-    if (c.n == 0) return cudaSuccess;
+                         uint32_t limit, cudaStream_t s, uint32_t lo, uint32_t hi) {
+    if (hi == 0xFFFFFFFFu) hi = c.n;
+    if (hi <= lo) return cudaSuccess;
     note_launches();
-    k_emit_packed<true><<<grid_for((uint64_t)c.n, 256), 256, 0, s>>>(c, 0, nullptr, prefix_tab, pos_bits, nullptr, rec,
-                                                                     counts, limit);
+    CollView v = c;
+    v.n = hi;  // the kernel walks ids [lo, hi)
+    k_emit_packed<true><<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, nullptr, prefix_tab, pos_bits, nullptr,
+                                                                           rec, counts, limit);
     return cudaGetLastError();
 }
 
-cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s) {
+cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s, uint32_t* overflow) {
     if (U == 0) return cudaSuccess;
     note_launches();
-    k_order_records<<<grid_for(((uint64_t)U + 31) / 32 * 32, REC_THREADS), REC_THREADS, 0, s>>>(counts, U, rec);
+    k_order_records<<<grid_for(((uint64_t)U + 31) / 32 * 32, REC_THREADS), REC_THREADS, 0, s>>>(counts, U, rec,
+                                                                                              overflow);
     return cudaGetLastError();
 }
 

@@ -103,3 +103,21 @@ def test_host_join_with_a_reused_size_profile(ctx):
     bad[int(c.starts[-1]) + int(c.sizes[-1]) - 1] = 0xFFFFFFFF  # reserved token, profile seen before
     with pytest.raises(hs.HysetError):
         ctx.self_join_host(bad, c.sizes, c.starts, threshold=0.6, **PIPELINED)
+
+
+def test_host_join_records_and_a_list_that_outgrows_them(ctx):
+    """Once a join with a size profile and threshold saw every index list at
+    most 31 long, later host-input joins with that profile put the prefix
+    entries straight into token records while the chunks land.  A collection
+    with the same sizes whose token 0 heads the prefixes of 40 sets overflows
+    one record: the ordering pass flags it and the join runs again over lists.
+    Every call must return the oracle's pairs."""
+    c = synth.generate(synth.C2, n_sets=20000, seed=103)
+    assert c.tokens.min() >= 1
+    grown = c.tokens.copy()
+    grown[c.starts[np.random.default_rng(5).choice(c.n, size=40, replace=False)]] = 0
+    exp = oracle.as_set(oracle.join(c.tokens, c.starts, c.sizes, 0.8))
+    exp_grown = oracle.as_set(oracle.join(grown, c.starts, c.sizes, 0.8))
+    for toks, want in ((c.tokens, exp), (c.tokens, exp), (grown, exp_grown), (c.tokens, exp), (c.tokens, exp)):
+        r = ctx.self_join_host(toks, c.sizes, c.starts, threshold=0.8, **PIPELINED)
+        assert r.count == len(want) and oracle.as_set(r.pairs) == want
