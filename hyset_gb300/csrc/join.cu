@@ -64,6 +64,10 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     if constexpr (TECH == TECH_FGSS && HS_ITEM_CARRY) flush_items<VMODE, W, ST>(P, ic, lane);
 }
 
+#ifndef HS_VREVERSE
+#define HS_VREVERSE 1
+#endif
+
 #ifndef HS_VCLAIM
 #define HS_VCLAIM 1
 #endif
@@ -89,9 +93,12 @@ __global__ void __launch_bounds__(JOIN_THREADS) k_verify_candidates(CollView R, 
             i_end = min(n_probes, i + VCLAIM);
         }
         if (i >= n_probes) break;
-        const uint32_t cb = i ? offsets[i - 1] : 0, ce = offsets[i];
+        // lists from the last: callers list probes by id, so the longest sets
+        // (the longest merges) start first and the launch's tail is light
+        const uint32_t li = HS_VREVERSE ? n_probes - 1 - i : i;
+        const uint32_t cb = li ? offsets[li - 1] : 0, ce = offsets[li];
         const uint32_t* list = cands + cb;
-        verify_probe_list<VMODE, W, VMAXP>(R, S, B, sig_R, sig_S, probes[i], [list](uint32_t k) { return list[k]; },
+        verify_probe_list<VMODE, W, VMAXP>(R, S, B, sig_R, sig_S, probes[li], [list](uint32_t k) { return list[k]; },
                                            ce - cb, out, sbuf, lane);
     }
 }

@@ -293,10 +293,17 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 // and slots past REC_ENTRIES are dropped); len is then the prefix-length table
 // indexed by set size and off is not read.
 constexpr int EMIT_ROUNDS = 8;
+#ifndef HS_REC_EMIT_ROUNDS
+#define HS_REC_EMIT_ROUNDS 8  // rounds of slot atomics in flight per lane (record emit)
+#endif
+#ifndef HS_REC_EMIT_MINB
+#define HS_REC_EMIT_MINB 1  // resident blocks per SM the record emit is compiled for
+#endif
 template <bool REC>
-__global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
+__global__ void __launch_bounds__(256, REC ? HS_REC_EMIT_MINB : 1) k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
                               uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit) {
+    constexpr int ROUNDS = REC ? HS_REC_EMIT_ROUNDS : EMIT_ROUNDS;
     const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t s0 = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; s0 < c.n; s0 += warps * 32u) {
@@ -314,10 +321,10 @@ __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restric
         }
         const uint32_t incl = warp_incl_scan(l, lane);
         const uint32_t total = __shfl_sync(FULL, incl, 31);
-        for (uint32_t j0 = 0; j0 < total; j0 += 32 * EMIT_ROUNDS) {
-            uint32_t tok[EMIT_ROUNDS], val[EMIT_ROUNDS];
+        for (uint32_t j0 = 0; j0 < total; j0 += 32 * ROUNDS) {
+            uint32_t tok[ROUNDS], val[ROUNDS];
 #pragma unroll
-            for (int u = 0; u < EMIT_ROUNDS; ++u) {
+            for (int u = 0; u < ROUNDS; ++u) {
                 const uint32_t j = j0 + 32u * u + lane;
                 // the set of the round's first entry r0 (sets ending at or before
                 // r0 come first), plus the sets that start inside the round up to j
@@ -334,19 +341,19 @@ __global__ void k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restric
             }
             if constexpr (REC) {
                 // every round's slot atomic is in flight before the first store
-                uint32_t slot[EMIT_ROUNDS];
+                uint32_t slot[ROUNDS];
 #pragma unroll
-                for (int u = 0; u < EMIT_ROUNDS; ++u) {
+                for (int u = 0; u < ROUNDS; ++u) {
                     const uint32_t j = j0 + 32u * u + lane;
                     slot[u] = j < total && tok[u] < limit ? atomicAdd(&counts[tok[u]], 1u) : 0xFFFFFFFFu;
                 }
 #pragma unroll
-                for (int u = 0; u < EMIT_ROUNDS; ++u)
+                for (int u = 0; u < ROUNDS; ++u)
                     if (slot[u] < REC_ENTRIES) e_val[(uint64_t)tok[u] * REC_CAP + 1 + slot[u]] = val[u];
                 continue;
             }
 #pragma unroll
-            for (int u = 0; u < EMIT_ROUNDS; ++u) {
+            for (int u = 0; u < ROUNDS; ++u) {
                 const uint32_t j = j0 + 32u * u + lane;
                 if (j < total) {
                     e_token[o0 + j] = tok[u];

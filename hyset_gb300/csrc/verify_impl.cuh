@@ -11,7 +11,11 @@ namespace {
 
 // Staged lane-serial merge: b's first VSTAGE tokens are in `head` (shared
 // memory), the rest in global memory; same early-exit bounds as verify_serial.
-constexpr uint32_t VSTAGE = 16;            // candidate tokens staged per candidate
+#ifndef HS_VSTAGE
+#define HS_VSTAGE 8
+#endif
+constexpr uint32_t VSTAGE = HS_VSTAGE;     // candidate tokens staged per candidate (a power of two, 2..32)
+static_assert(VSTAGE >= 2 && VSTAGE <= 32 && (VSTAGE & (VSTAGE - 1)) == 0, "VSTAGE: a power of two up to 32");
 constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fall in distinct banks
 
 #ifndef HS_VMAXP
@@ -21,6 +25,11 @@ constexpr uint32_t VSTRIDE = VSTAGE + 1;   // padded row: the 32 lanes' rows fal
 // merged from L1/L2).  Smaller than the join kernels' stage so that more warps
 // fit an SM: the verifier waits on gathers, and more resident warps hide them.
 constexpr uint32_t VMAXP = HS_VMAXP;
+
+#ifndef HS_VLONG
+#define HS_VLONG 256
+#endif
+constexpr uint32_t VLONG = HS_VLONG;  // merges of two sets at least this long run on the whole warp
 
 // Shared-memory words one warp needs: the probe (pmax tokens), plus the
 // staged candidate prefixes in mode 3.
@@ -116,19 +125,37 @@ __device__ __forceinline__ void verify_probe_list(const CollView& R, const CollV
             }
             staged = true;
         }
+        // Long merges (both sets of at least VLONG tokens) run on the whole
+        // warp in 32-token steps: a lane-serial merge of two similar sets of
+        // 2,000 tokens holds its warp for about 4,000 dependent steps, and
+        // one such pair at the end of a launch was its tail.
+        const bool lng = VMODE != 2 && keep && min(lp, lc) >= VLONG;
+        if (VMODE != 2) {
+            unsigned ml = __ballot_sync(FULL, lng);
+            while (ml) {
+                const int src = __ffs(ml) - 1;
+                ml &= ml - 1;
+                const uint32_t cc = __shfl_sync(FULL, c, src), c2 = __shfl_sync(FULL, cs, src);
+                const uint32_t ll = __shfl_sync(FULL, lc, src), mm = __shfl_sync(FULL, mo, src);
+                const bool ok = verify_warp(a, lp, R.tokens + c2, ll, mm, NOWN, lane);
+                emit(out, ok && lane == 0, p, cc, lane);
+            }
+            keep = keep && !lng;
+        }
         if constexpr (VMODE == 1) {
             bool ok = keep && verify_serial(a, lp, R.tokens + cs, lc, mo, NOWN);
             emit(out, ok, p, c, lane);
         } else if constexpr (VMODE == 3) {
             // the first VSTAGE tokens of the round's 32 candidates arrive with
-            // 16 coalesced loads (two candidates per load, one per half-warp);
-            // each lane then merges its candidate out of shared memory and
-            // reads global memory only past the staged prefix
+            // VSTAGE coalesced loads (32 / VSTAGE candidates per load, VSTAGE
+            // lanes each); each lane then merges its candidate out of shared
+            // memory and reads global memory only past the staged prefix
             uint32_t* tile = sbuf + PMAX;
             const uint32_t t = lane & (VSTAGE - 1);
+            constexpr int PER = 32 / VSTAGE;  // candidates per load
 #pragma unroll
-            for (int r = 0; r < 16; ++r) {
-                const int j = 2 * r + (lane >> 4);
+            for (int r = 0; r < (int)VSTAGE; ++r) {
+                const int j = PER * r + lane / (int)VSTAGE;
                 const uint32_t cj = __shfl_sync(FULL, cs, j), lj = __shfl_sync(FULL, keep ? lc : 0u, j);
                 if (t < lj) tile[j * VSTRIDE + t] = __ldg(R.tokens + cj + t);
             }
