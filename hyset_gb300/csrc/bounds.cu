@@ -112,9 +112,17 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
         b->mo_monotone = true;
         for (uint32_t s = 1; s <= 2 * L; ++s)
             if (b->mo_sum[s] < b->mo_sum[s - 1]) b->mo_monotone = false;
+        if (b->mo_monotone) {  // the sums whose minoverlap is <= v form the prefix [0, max_sum[v]]
+            b->max_sum.resize((size_t)L + 1);
+            uint32_t s = 0;
+            for (uint32_t v = 0; v <= L; ++v) {
+                while (s < 2 * L && b->mo_sum[s + 1] <= v) ++s;
+                b->max_sum[v] = s;
+            }
+        }
     }
     // one device allocation holding all tables
-    size_t n32 = 5 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size();
+    size_t n32 = 5 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size() + b->max_sum.size();
     size_t bytes = b->mo_row.size() * 8 + n32 * 4;
     CK(b->dev.ensure(bytes, ctx->stream));
     uint8_t* base = b->dev.as<uint8_t>();
@@ -126,7 +134,7 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
         dst = d;
         return cudaMemcpyAsync(d, v.data(), v.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
     };
-    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_mid, *d_sum, *d_tab;
+    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_mid, *d_sum, *d_tab, *d_msum = nullptr;
     CK(cudaMemcpyAsync(d_row, b->mo_row.data(), b->mo_row.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(put(b->minsize, d_minsize));
     CK(put(b->probe_prefix, d_pp));
@@ -135,8 +143,9 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
     CK(put(b->mid_prefix, d_mid));
     CK(put(b->mo_sum, d_sum));
     CK(put(b->mo_tab, d_tab));
+    if (!b->max_sum.empty()) CK(put(b->max_sum, d_msum));
     CK(cudaStreamSynchronize(ctx->stream));
-    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_mid, d_sum, d_row, d_tab, L, sim};
+    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_mid, d_sum, d_row, d_tab, L, sim, d_msum};
     *out = b.get();
     ctx->bounds.emplace(key, std::move(b));
     return HYSET_OK;

@@ -38,7 +38,38 @@ struct BoundsView {
     const uint32_t* __restrict__ mo_tab;        // cosine: raw minoverlap at (big, small)
     uint32_t L;
     int sim;
+    // [L+1] jaccard, dice: the largest l1 + l2 whose raw minoverlap is at most
+    // v (nullptr for cosine or a table that is not monotone)
+    const uint32_t* __restrict__ max_sum = nullptr;
 };
+
+// Copy chunks of a host-input join (in tokens): 64 MB while more than three
+// remain, then a third of what is left, at least 16 MB, so the work left when
+// the last chunk lands is small.  The next chunk's size when `rem` tokens are
+// left (the host schedules the copies with it, the size scan finds the sets
+// each chunk completes with it).
+constexpr uint64_t PIPE_CHUNK_TOKENS = 16ull << 20;
+constexpr uint64_t PIPE_TAIL_TOKENS = 4ull << 20;
+constexpr uint32_t PIPE_MAX_CHUNKS = 1024;  // 2^32 tokens take at most 259
+__host__ __device__ inline uint64_t pipe_chunk(uint64_t rem) {
+    uint64_t c = (rem / 3 + 0xFFFFu) & ~0xFFFFull;
+    c = c > PIPE_TAIL_TOKENS ? c : PIPE_TAIL_TOKENS;
+    c = c < PIPE_CHUNK_TOKENS ? c : PIPE_CHUNK_TOKENS;
+    return c < rem ? c : rem;
+}
+
+// The low field of a bound-layout index entry (a self-join's midprefix index,
+// jaccard or dice) for position pos of a set of size len: the longest probe lp
+// (lp >= len, as every probe of a self-join window) whose positional bound this
+// side of the pair admits, len - pos >= minoverlap(lp, len).  For pos > 0 that
+// is raw minoverlap(lp + len) <= len - pos, i.e. lp + len <= max_sum[len - pos];
+// pos 0 admits every probe (maxf, at least the longest set).
+__device__ __forceinline__ uint32_t bound_field(const uint32_t* __restrict__ max_sum, uint32_t len, uint32_t pos,
+                                                uint32_t maxf) {
+    if (pos == 0) return maxf;
+    const uint32_t s = max_sum[len - pos];
+    return s <= len ? 0u : min(maxf, s - len);
+}
 
 // generic_similarity::minoverlap (similarity.hpp:21-23): min(l2, min(l1, raw)).
 // Requires big >= small >= minsize(big) (guaranteed by every caller's length window).

@@ -60,10 +60,21 @@ hyset_status make_collection(hyset_ctx* ctx, hyset_coll* c, const uint32_t* h_si
 
 // ---- index builds and size statistics (index_host.cu) ------------------------
 hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c, const uint32_t* sizes);
+// The host side of the size metadata (max_size, size_hist, h_first_ge) from a
+// first_ge table computed on the device (c->first_ge holds it already).
+void size_meta_from_first_ge(hyset_coll* c, const uint32_t* first_ge, uint32_t L);
 uint32_t size_at(const hyset_coll* c, uint32_t i);
 std::vector<uint64_t> range_hist(const hyset_coll* c, uint32_t lo, uint32_t hi);
 uint64_t prefix_entries(const hyset_coll* c, const std::vector<uint32_t>& pre);
 uint32_t bits_for(uint64_t v);
+// The entry layout of an index's token records: the low rec_bits hold the
+// longest probe the entry's positional bound admits (*bound: a self-join's
+// midprefix index, kind 0, under jaccard or dice, when set ids and that field
+// fit 32 bits) or the entry's position (rec_bits = pb, the lists' layout).
+void record_layout(const hyset_coll* c, const Bounds* b, int kind, uint32_t pb, uint32_t* rec_bits, bool* bound);
+// The first set id whose prefix (pre[size] tokens) is long enough to be
+// emitted a warp per set (0xFFFFFFFF: none).
+uint32_t first_long_prefix(const hyset_coll* c, const std::vector<uint32_t>& pre);
 int key_bits_for(uint32_t universe);
 hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, int kind, Index& ix,
                                 const std::vector<uint32_t>* pre = nullptr, const uint32_t* d_pre = nullptr,
@@ -107,11 +118,19 @@ hyset_status sort_device_pairs(hyset_ctx* ctx, uint2* pairs, uint64_t n, uint32_
 bool swap_sides(const hyset_coll* R, const hyset_coll* S, const hyset_join_opts* o);
 hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const hyset_join_opts* o, hyset_result* res,
                       bool timed_from_ev0, TokenJoinParams* T = nullptr);
+// The probe-major prefix filter's split of the longest probes of S into slot
+// segments (JoinParams::heavy_from, segs, seg_slots); none for banded joins.
+// The launch's work buffer then needs two zeroed counters.
+void split_heavy(const hyset_coll* S, const Bounds* b, JoinParams& P);
+// The pairs of a finished join (res->count of them in the context's pair
+// buffer): sorted when asked, left on the device or copied to the host.
+hyset_status deliver_pairs(hyset_ctx* ctx, const JoinParams& P, const hyset_join_opts* o, hyset_result* res);
 hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, hyset_result* res);
 
 // ---- host-input pipelines (pipeline.cu) --------------------------------------
 // One event per copy chunk, created on demand (nullptr on failure).
 cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k);
+
 
 // ---- batches (batch_host.cu) --------------------------------------------------
 void batch_release(hyset_ctx* ctx);

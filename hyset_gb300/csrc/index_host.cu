@@ -19,10 +19,10 @@ namespace hs {
 // needed here).  The collection keeps no per-set host array: sizes of single
 // sets and of id ranges come from first_ge.
 hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c, const uint32_t* sizes) {
-    // run lengths: sorted sizes repeat, so the count stays in a register
     std::vector<uint64_t>& hist = c->size_hist;
     hist.assign(c->n ? (size_t)sizes[c->n - 1] + 1 : 1, 0);
     uint32_t i = 0;
+    // run lengths: sorted sizes repeat, so the count stays in a register
     while (i < c->n) {
         const uint32_t v = sizes[i];
         uint32_t j = i + 1;
@@ -43,6 +43,13 @@ hyset_status build_size_meta(hyset_ctx* ctx, hyset_coll* c, const uint32_t* size
     CK(c->first_ge.ensure(f.size() * 4, ctx->stream));
     CK(cudaMemcpyAsync(c->first_ge.p, f.data(), f.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
     return HYSET_OK;
+}
+
+void size_meta_from_first_ge(hyset_coll* c, const uint32_t* first_ge, uint32_t L) {
+    c->max_size = L;
+    c->h_first_ge.assign(first_ge, first_ge + (size_t)L + 2);
+    c->size_hist.assign((size_t)L + 1, 0);
+    for (uint32_t l = 0; l <= L; ++l) c->size_hist[l] = first_ge[l + 1] - first_ge[l];
 }
 
 // Size of set i (sizes are non-decreasing: the last l with first_ge[l] <= i).
@@ -70,6 +77,22 @@ uint64_t prefix_entries(const hyset_coll* c, const std::vector<uint32_t>& pre) {
 }
 
 // Bits needed to represent v (at least 1).
+uint32_t first_long_prefix(const hyset_coll* c, const std::vector<uint32_t>& pre) {
+    constexpr uint32_t LONG_PREFIX = 32;  // longer prefixes are emitted a warp per set
+    uint64_t id = 0;
+    for (size_t l = 0; l < c->size_hist.size(); ++l) {
+        if (l < pre.size() && pre[l] > LONG_PREFIX) return (uint32_t)id;
+        id += c->size_hist[l];
+    }
+    return 0xFFFFFFFFu;
+}
+
+void record_layout(const hyset_coll* c, const Bounds* b, int kind, uint32_t pb, uint32_t* rec_bits, bool* bound) {
+    const uint32_t fb = bits_for(b->L);  // a field that holds every probe length
+    *bound = kind == 0 && b->view.max_sum != nullptr && fb + bits_for(c->n) <= 32;
+    *rec_bits = *bound ? fb : pb;
+}
+
 uint32_t bits_for(uint64_t v) {
     uint32_t b = 1;
     while (b < 64 && (v >> b)) ++b;
@@ -152,9 +175,11 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         const auto lk = c->list_longest.find(d_pre);
         if (lk != c->list_longest.end() && lk->second <= REC_ENTRIES) {
             uint32_t* counts = ctx->sc->counts.as<uint32_t>();
+            record_layout(c, b, kind, pb, &ix.rec_bits, &ix.rec_bound);
             CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
             CK(cudaMemsetAsync(counts, 0, (size_t)U * 4, s));
-            CK(emit_records(v, d_pre, pb, counts, ix.rec.as<uint32_t>(), U, s));
+            CK(emit_records(v, d_pre, ix.rec_bits, counts, ix.rec.as<uint32_t>(), U, s, 0, 0xFFFFFFFFu,
+                            ix.rec_bound ? b->view.max_sum : nullptr, first_long_prefix(c, *pre)));
             CK(order_records(counts, U, ix.rec.as<uint32_t>(), s));
             ix.records = true;
             ix.pos_bits = pb;
@@ -167,7 +192,8 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         uint32_t* counts = ctx->sc->counts.as<uint32_t>();
         CK(ctx->sc->gate.ensure(4, s));
         CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
-        CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s));
+        CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s, 0,
+                               0xFFFFFFFFu, 0xFFFFFFFFu, first_long_prefix(c, *pre)));
         // the list build's path is read back once per collection and prefix
         // table (not while a batch is being captured into a graph)
         cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
@@ -181,8 +207,10 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
         ix.pos_bits = pb;
         if (rec_fits && E && read_back && ctx->h_flags[15] <= REC_ENTRIES) {
             // this build's lists become records; later builds emit records directly
+            record_layout(c, b, kind, pb, &ix.rec_bits, &ix.rec_bound);
             CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
-            CK(records_from_lists(ix.list_off.as<uint32_t>(), ix.set.as<uint32_t>(), U, ix.rec.as<uint32_t>(), s));
+            CK(records_from_lists(ix.list_off.as<uint32_t>(), ix.set.as<uint32_t>(), U, ix.rec.as<uint32_t>(), s,
+                                  ix.rec_bound ? b->view.max_sum : nullptr, c->d_sizes, pb, ix.rec_bits));
             ix.records = true;
         }
         return HYSET_OK;

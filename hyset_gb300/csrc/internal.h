@@ -62,7 +62,7 @@ struct Bounds {
     double tau = 0;
     uint32_t L = 0;
     int index_maxprefix = 0;  // 0: index midprefix (self-join), 1: maxprefix (R-S)
-    std::vector<uint32_t> minsize, probe_prefix, index_prefix, max_partner, mid_prefix, mo_sum, mo_tab;
+    std::vector<uint32_t> minsize, probe_prefix, index_prefix, max_partner, mid_prefix, mo_sum, mo_tab, max_sum;
     bool mo_monotone = false;  // minoverlap non-decreasing in each length (R-S bands are valid)
     std::vector<uint64_t> mo_row;
     DevBuf dev;
@@ -86,15 +86,20 @@ struct Index {
     uint32_t universe = 0;
     uint64_t entries = 0;
     uint32_t pos_bits = 0;  // > 0: packed (set << pos_bits) | position entries
+    // the records' layout: low rec_bits of an entry, the position or (rec_bound)
+    // the longest probe the entry's positional bound admits
+    uint32_t rec_bits = 0;
+    bool rec_bound = false;
     IndexView view() const {
         IndexView v;
         v.list_off = list_off.as<uint32_t>();
         v.set = records ? rec.as<uint32_t>() : set.as<uint32_t>();
         v.pos = pos_bits ? nullptr : pos.as<uint32_t>();
         v.universe = universe;
-        v.pos_bits = pos_bits;
+        v.pos_bits = records ? rec_bits : pos_bits;
         v.sorted = 1;
         v.rec = records ? 1 : 0;
+        v.bound = records && rec_bound ? 1 : 0;
         return v;
     }
 };
@@ -122,9 +127,9 @@ struct BatchJoin {
 // Scratch of an index build (prefix lengths and offsets, entries, radix sort
 // ping-pong buffers, token counts, scan/sort scratch).
 struct Scratch {
-    DevBuf len, off, tok, set, pos, order, altk, altv, counts, scan, gate;
+    DevBuf len, off, tok, set, pos, order, altk, altv, counts, scan, gate, sscan;
     void release(cudaStream_t s) {
-        DevBuf* all[] = {&len, &off, &tok, &set, &pos, &order, &altk, &altv, &counts, &scan, &gate};
+        DevBuf* all[] = {&len, &off, &tok, &set, &pos, &order, &altk, &altv, &counts, &scan, &gate, &sscan};
         for (DevBuf* d : all) d->release(s);
     }
 };

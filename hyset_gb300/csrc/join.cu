@@ -34,7 +34,9 @@ namespace hs {
 
 namespace {
 
-template <int TECH, int VMODE, int W, bool ST>
+// BD: the index is token records in the bound layout (IndexView::bound;
+// prefix-index joins only).
+template <int TECH, int VMODE, int W, bool ST, bool BD = false>
 __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinParams P) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -43,25 +45,41 @@ __global__ void __launch_bounds__(JOIN_THREADS, HS_JOIN_MIN_BLOCKS) k_join(JoinP
     const uint32_t grab = P.grab ? P.grab : 1;
     uint32_t i = 0, i_end = 0;
     ItemCarry ic;  // FGSS with HS_ITEM_CARRY: items pending across slot rounds and batches
+    ic.q = sbuf;   // its queue for bound-layout indexes (QSLOTS * QF_N <= MAXP words)
+    static_assert(QSLOTS * QF_N <= MAXP, "item queue exceeds the warp's shared-memory slot");
+    uint32_t nheavy = 0;  // the longest probes (the first from the top) go as slot segments, one per steal
+    if constexpr (TECH == TECH_FGSS && HS_ITEM_CARRY) {
+        const uint32_t hf = max(P.heavy_from, P.p_lo);
+        nheavy = P.p_hi > hf ? P.p_hi - hf : 0u;
+        const uint32_t units = nheavy * P.segs;
+        for (;;) {
+            uint32_t u = 0;
+            if (lane == 0) u = atomicAdd(P.work + 1, 1u);
+            u = __shfl_sync(FULL, u, 0);
+            if (u >= units) break;
+            const uint32_t h = u / P.segs, g = u - h * P.segs;
+            fgss_carry<VMODE, W, ST, BD>(P, h, 1, lane, ic, g * P.seg_slots, (g + 1) * P.seg_slots);
+        }
+    }
     for (;;) {
         if (i >= i_end) {
             const uint32_t steal = grab * HS_JOIN_STEAL;  // probes per atomic on the shared counter
             if (lane == 0) i = atomicAdd(P.work, steal);
-            i = __shfl_sync(FULL, i, 0);
+            i = __shfl_sync(FULL, i, 0) + nheavy;
             i_end = min(nprobe, i + steal);
         }
         if (i >= nprobe) break;
         const uint32_t end = min(i_end, i + grab);
         // largest sets first: the heaviest probes start early, the tail is light
         if constexpr (TECH == TECH_FGSS) {
-            if constexpr (HS_ITEM_CARRY) fgss_carry<VMODE, W, ST>(P, i, end - i, lane, ic);
-            else fgss_batch<VMODE, W, ST>(P, i, end - i, lane);
+            if constexpr (HS_ITEM_CARRY) fgss_carry<VMODE, W, ST, BD>(P, i, end - i, lane, ic);
+            else fgss_batch<VMODE, W, ST, true, BD>(P, i, end - i, lane);
         } else {
             for (uint32_t q = i; q < end; ++q) enum_probe<VMODE, W, ST>(P, P.p_hi - 1 - q, sbuf, lane);
         }
         i = end;
     }
-    if constexpr (TECH == TECH_FGSS && HS_ITEM_CARRY) flush_items<VMODE, W, ST>(P, ic, lane);
+    if constexpr (TECH == TECH_FGSS && HS_ITEM_CARRY) flush_items<VMODE, W, ST, BD>(P, ic, lane);
 }
 
 #ifndef HS_VREVERSE
@@ -144,16 +162,24 @@ cudaError_t launch_persistent(K kernel, int sm_count, cudaStream_t s, const Join
     return cudaGetLastError();
 }
 
-template <int TECH, int VMODE, bool ST>
-cudaError_t dispatch_words_st(const JoinParams& P, int sm_count, cudaStream_t s) {
+template <int TECH, int VMODE, bool ST, bool BD>
+cudaError_t dispatch_words_bd(const JoinParams& P, int sm_count, cudaStream_t s) {
     switch (P.bits_R ? P.words : 0) {
-    case 0: return launch_persistent(k_join<TECH, VMODE, 0, ST>, sm_count, s, P);
-    case 1: return launch_persistent(k_join<TECH, VMODE, 1, ST>, sm_count, s, P);
-    case 2: return launch_persistent(k_join<TECH, VMODE, 2, ST>, sm_count, s, P);
-    case 4: return launch_persistent(k_join<TECH, VMODE, 4, ST>, sm_count, s, P);
-    case 8: return launch_persistent(k_join<TECH, VMODE, 8, ST>, sm_count, s, P);
+    case 0: return launch_persistent(k_join<TECH, VMODE, 0, ST, BD>, sm_count, s, P);
+    case 1: return launch_persistent(k_join<TECH, VMODE, 1, ST, BD>, sm_count, s, P);
+    case 2: return launch_persistent(k_join<TECH, VMODE, 2, ST, BD>, sm_count, s, P);
+    case 4: return launch_persistent(k_join<TECH, VMODE, 4, ST, BD>, sm_count, s, P);
+    case 8: return launch_persistent(k_join<TECH, VMODE, 8, ST, BD>, sm_count, s, P);
     default: return cudaErrorInvalidValue;
     }
+}
+
+template <int TECH, int VMODE, bool ST>
+cudaError_t dispatch_words_st(const JoinParams& P, int sm_count, cudaStream_t s) {
+    if constexpr (TECH == TECH_FGSS) {
+        if (P.X.bound) return dispatch_words_bd<TECH, VMODE, ST, true>(P, sm_count, s);
+    }
+    return dispatch_words_bd<TECH, VMODE, ST, false>(P, sm_count, s);
 }
 
 template <int TECH, int VMODE>

@@ -91,6 +91,28 @@ hyset_status run_join(hyset_ctx* ctx, JoinParams P, int tech, int vmode, const h
         cap = count + count / 8 + 1024;  // overflow: retry once with room for everything
         if (attempt == 1) return fail(ctx, HYSET_E_OVERFLOW, "pair buffer overflow after resize");
     }
+    return deliver_pairs(ctx, P, o, res);
+}
+
+void split_heavy(const hyset_coll* S, const Bounds* b, JoinParams& P) {
+    constexpr uint32_t HEAVY_SLOTS = 128;  // probes with longer prefixes are split
+    constexpr uint32_t SEG_SLOTS = 64;     // prefix slots per unit of a split probe
+    P.heavy_from = 0xFFFFFFFFu;
+    P.segs = 0;
+    P.seg_slots = SEG_SLOTS;
+    if (P.X2.set) return;  // banded R-S joins keep two lanes per probe
+    const uint32_t L = std::min(S->max_size, b->L);
+    for (uint32_t l = 0; l <= L; ++l)
+        if (b->probe_prefix[l] > HEAVY_SLOTS) {
+            P.heavy_from = S->h_first_ge[l];
+            P.segs = (b->probe_prefix[L] + SEG_SLOTS - 1) / SEG_SLOTS;
+            return;
+        }
+}
+
+hyset_status deliver_pairs(hyset_ctx* ctx, const JoinParams& P, const hyset_join_opts* o, hyset_result* res) {
+    cudaStream_t s = ctx->stream;
+    const bool count_only = o->count_only != 0;
     if (!count_only && o->sort_pairs)
         ST(sort_device_pairs(ctx, ctx->s_pairs.as<uint2>(), res->count, P.out.swap ? P.R.n : P.S.n,
                              P.out.swap ? P.S.n : P.R.n));
@@ -223,6 +245,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     if (!token_major && tech == HYSET_TECH_FGSS) {
         ST(build_fgss_indexes(ctx, R, b, self, R->index, R->index_mid, P));
         if (P.X2.set) P.grab = std::min<uint32_t>(P.grab, 16);  // two bands per probe share a warp batch
+        split_heavy(S, b, P);
     }
     if (words) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
     int ktech = tech == HYSET_TECH_FGSS ? TECH_FGSS : (tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);

@@ -212,7 +212,7 @@ __device__ __forceinline__ int scan_owner(uint32_t incl, uint32_t q) {
 // tokens against the midprefix index X2).
 // RC: the index may be token records (IndexView::rec, checked per launch);
 // without it the record path is not compiled.
-template <int VMODE, int W, bool ST, bool RC = true>
+template <int VMODE, int W, bool ST, bool RC = true, bool BD = false>
 __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lane) {
     // lane t < k: probe t of the batch (largest sets first)
     uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
@@ -317,6 +317,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                     pc = v & ((1u << P.X.pos_bits) - 1u);
                 }
                 if (!P.X.sorted) keep = c >= ilo && c < ihi;
+                if constexpr (BD) keep = keep && ilp <= pc;  // pc: the longest probe the entry admits
             }
             // Signatures up to 256 bits are loaded with the candidate's meta (one
             // round trip); wider ones only for items that pass the positional
@@ -331,7 +332,7 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 lc = cm.y;
                 const uint32_t big = max(ilp, lc), small = min(ilp, lc);
                 mo = minoverlap(P.B, big, small);
-                keep = 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
+                keep = BD ? ilp - jp >= mo : 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
             }
             count_stat<ST>(P, 0, q < total ? 1u : 0u, lane);
             count_stat<ST>(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
@@ -356,10 +357,12 @@ __device__ void fgss_batch(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                     m &= m - 1;
                     const uint32_t cc = __shfl_sync(FULL, c, src), cs = __shfl_sync(FULL, cstart, src);
                     const uint32_t ll = __shfl_sync(FULL, lc, src), mm = __shfl_sync(FULL, mo, src);
-                    const uint32_t ob = __shfl_sync(FULL, pc, src), pp = __shfl_sync(FULL, ip, src);
+                    const uint32_t ob = __shfl_sync(FULL, BD ? jp : pc, src), pp = __shfl_sync(FULL, ip, src);
                     const uint32_t pl = __shfl_sync(FULL, ilp, src), ps = __shfl_sync(FULL, ipst, src);
                     uint32_t u = 0;
-                    const bool ok = verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
+                    const bool ok = BD
+                                        ? verify_warp(P.R.tokens + cs, ll, P.S.tokens + ps, pl, mm, ob, lane, &u)
+                                        : verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
                     if (lane == 0) used += u;
                     emit(P.out, ok && lane == 0, pp, cc, lane);
                 }
@@ -388,7 +391,7 @@ struct ItemLane {  // one lane's pending item (c == NO_ITEM: none)
 
 // Filters and verifies one round of items (the lanes whose c != NO_ITEM) and
 // appends the accepted pairs; every lane's item is consumed.
-template <int VMODE, int W, bool ST>
+template <int VMODE, int W, bool ST, bool BD>
 __device__ __forceinline__ void run_items(const JoinParams& P, ItemLane& it, int lane) {
     bool keep = it.c != NO_ITEM;
     const uint32_t c = keep ? it.c : 0u, pc = it.pc, jp = it.jp, ip = it.ip, ilp = it.ilp;
@@ -402,7 +405,9 @@ __device__ __forceinline__ void run_items(const JoinParams& P, ItemLane& it, int
         lc = cm.y;
         const uint32_t big = max(ilp, lc), small = min(ilp, lc);
         mo = minoverlap(P.B, big, small);
-        keep = 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;  // positional bound
+        // positional bound; with bound-layout entries the candidate's side was
+        // checked when the item was taken
+        keep = BD ? ilp - jp >= mo : 1u + min(ilp - jp - 1u, lc - pc - 1u) >= mo;
     }
     count_stat<ST>(P, 5, (W > 0 && keep) ? 1u : 0u, lane);
     if constexpr (W > 4) {
@@ -423,10 +428,13 @@ __device__ __forceinline__ void run_items(const JoinParams& P, ItemLane& it, int
             m &= m - 1;
             const uint32_t cc = __shfl_sync(FULL, c, src), cs = __shfl_sync(FULL, cstart, src);
             const uint32_t ll = __shfl_sync(FULL, lc, src), mm = __shfl_sync(FULL, mo, src);
-            const uint32_t ob = __shfl_sync(FULL, pc, src), pp = __shfl_sync(FULL, ip, src);
+            const uint32_t ob = __shfl_sync(FULL, BD ? jp : pc, src), pp = __shfl_sync(FULL, ip, src);
             const uint32_t pl = __shfl_sync(FULL, ilp, src), ps = __shfl_sync(FULL, it.ipst, src);
             uint32_t u = 0;
-            const bool ok = verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
+            // ownership by the candidate's position, or (bound layout: no
+            // candidate position) by the probe's, with the merge's sides swapped
+            const bool ok = BD ? verify_warp(P.R.tokens + cs, ll, P.S.tokens + ps, pl, mm, ob, lane, &u)
+                                      : verify_warp(P.S.tokens + ps, pl, P.R.tokens + cs, ll, mm, ob, lane, &u);
             if (lane == 0) used += u;
             emit(P.out, ok && lane == 0, pp, cc, lane);
         }
@@ -436,19 +444,47 @@ __device__ __forceinline__ void run_items(const JoinParams& P, ItemLane& it, int
 }
 
 // The pending items of a warp (fewer than 32) and how many there are.
+// Bound-layout indexes keep them in the warp's shared-memory queue instead
+// (QSLOTS slots of the fields below, one array per field), because the items
+// that pass the candidate's side of the positional bound are compacted there.
 struct ItemCarry {
     ItemLane lane_item;
-    uint32_t pending = 0;  // warp-uniform: lanes [0, pending) hold an item
+    uint32_t pending = 0;  // warp-uniform: lanes [0, pending) hold an item (or queue slots [0, pending))
+    uint32_t* q = nullptr;  // the warp's queue (bound layout)
 };
+constexpr uint32_t QSLOTS = 64;  // pending (< 32) plus one window's survivors (<= 32)
+enum : uint32_t { QF_C = 0, QF_JP, QF_IP, QF_ILP, QF_IPST, QF_N };
 
-template <int VMODE, int W, bool ST>
+__device__ __forceinline__ ItemLane queue_item(const uint32_t* q, uint32_t slot) {
+    ItemLane x;
+    x.c = q[QF_C * QSLOTS + slot];
+    x.pc = 0;
+    x.jp = q[QF_JP * QSLOTS + slot];
+    x.ip = q[QF_IP * QSLOTS + slot];
+    x.ilp = q[QF_ILP * QSLOTS + slot];
+    x.ipst = q[QF_IPST * QSLOTS + slot];
+    return x;
+}
+
+template <int VMODE, int W, bool ST, bool BD>
 __device__ __forceinline__ void flush_items(const JoinParams& P, ItemCarry& ic, int lane) {
-    if (ic.pending) run_items<VMODE, W, ST>(P, ic.lane_item, lane);
+    if constexpr (BD) {
+        if (ic.pending) {
+            ItemLane x;
+            if ((uint32_t)lane < ic.pending) x = queue_item(ic.q, lane);
+            run_items<VMODE, W, ST, BD>(P, x, lane);
+        }
+    } else {
+        if (ic.pending) run_items<VMODE, W, ST, BD>(P, ic.lane_item, lane);
+    }
     ic.pending = 0;
 }
 
-template <int VMODE, int W, bool ST>
-__device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lane, ItemCarry& ic) {
+// [jb, je): the prefix slots of each probe to run (all by default; a heavy
+// probe's segment otherwise).
+template <int VMODE, int W, bool ST, bool BD>
+__device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lane, ItemCarry& ic, uint32_t jb = 0,
+                           uint32_t je = 0xFFFFFFFFu) {
     // probes as in fgss_batch: lane t < k (banded R-S: lanes k + t too)
     uint32_t p = 0, lp = 0, pst = 0, mp = 0, lo = 0, hi = 0, band = 0;
     const bool banded = P.X2.set != nullptr;
@@ -469,6 +505,8 @@ __device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 else hi = min(hi, mid);
             }
             if (lo < hi) mp = banded && band == 0 ? P.B.mid_prefix[lp] : P.B.probe_prefix[lp];
+            mp = min(mp, je);
+            mp = mp > jb ? mp - jb : 0u;  // the slots [jb, je) of the prefix
         }
     }
     count_stat<ST>(P, 4, mp, lane);
@@ -480,7 +518,7 @@ __device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lan
         const bool sv = sl < slots;
         const int t = scan_owner(mp_incl, sv ? sl : 0);
         const uint32_t t_incl = __shfl_sync(FULL, mp_incl, t), t_mp = __shfl_sync(FULL, mp, t);
-        const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp);
+        const uint32_t j = (sv ? sl : 0) - (t_incl - t_mp) + jb;
         const uint32_t t_pst = __shfl_sync(FULL, pst, t);
         const uint32_t t_lo = __shfl_sync(FULL, lo, t), t_hi = __shfl_sync(FULL, hi, t);
         const uint32_t t_band = __shfl_sync(FULL, band, t);
@@ -523,6 +561,62 @@ __device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lan
         }
         const uint32_t incl = warp_incl_scan(cnt, lane);
         const uint32_t total = __shfl_sync(FULL, incl, 31);
+        if constexpr (BD) {
+            // ---- bound layout: 32 of the round's items at a time are checked
+            // against the candidate's side of the positional bound (the entry
+            // carries the longest probe it admits); the survivors are appended
+            // to the warp's queue and every full round of 32 runs
+            uint32_t* q = ic.q;
+            for (uint32_t taken = 0; taken < total; taken += 32) {
+                const uint32_t qi = taken + (uint32_t)lane;
+                const bool has = qi < total;
+                const int jj = scan_owner(incl, has ? qi : 0u);
+                const uint32_t f_jj = __shfl_sync(FULL, first, jj);
+                const uint32_t i_jj = __shfl_sync(FULL, incl, jj);
+                const uint32_t c_jj = __shfl_sync(FULL, cnt, jj);
+                const uint32_t jp = __shfl_sync(FULL, j, jj);
+                const int it = __shfl_sync(FULL, t, jj);
+                const uint32_t ip = __shfl_sync(FULL, p, it);
+                const uint32_t ilp = __shfl_sync(FULL, lp, it);
+                const uint32_t ipst = __shfl_sync(FULL, pst, it);
+                bool ok = false;
+                uint32_t c = 0;
+                if (has) {
+                    const uint32_t v = x_set[f_jj + (qi - (i_jj - c_jj))];
+                    c = v >> P.X.pos_bits;
+                    ok = ilp <= (v & ((1u << P.X.pos_bits) - 1u));
+                }
+                const unsigned m = __ballot_sync(FULL, ok);
+                if (ok) {
+                    const uint32_t slot = ic.pending + __popc(m & lanemask_lt(lane));
+                    q[QF_C * QSLOTS + slot] = c;
+                    q[QF_JP * QSLOTS + slot] = jp;
+                    q[QF_IP * QSLOTS + slot] = ip;
+                    q[QF_ILP * QSLOTS + slot] = ilp;
+                    q[QF_IPST * QSLOTS + slot] = ipst;
+                }
+                ic.pending += __popc(m);
+                __syncwarp();
+                if (ic.pending >= 32u) {
+                    ItemLane x = queue_item(q, lane);
+                    // slots [32, pending) move to the front for the next round
+                    const uint32_t rest = ic.pending - 32u;
+                    ItemLane y;
+                    if ((uint32_t)lane < rest) y = queue_item(q, 32u + lane);
+                    __syncwarp();
+                    if ((uint32_t)lane < rest) {
+                        q[QF_C * QSLOTS + lane] = y.c;
+                        q[QF_JP * QSLOTS + lane] = y.jp;
+                        q[QF_IP * QSLOTS + lane] = y.ip;
+                        q[QF_ILP * QSLOTS + lane] = y.ilp;
+                        q[QF_IPST * QSLOTS + lane] = y.ipst;
+                    }
+                    ic.pending = rest;
+                    __syncwarp();
+                    run_items<VMODE, W, ST, BD>(P, x, lane);
+                }
+            }
+        } else {
         // ---- the round's items join the pending ones; every full round runs
         uint32_t taken = 0;
         while (taken < total) {
@@ -564,10 +658,11 @@ __device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lan
             taken += take;
             ic.pending += take;
             if (ic.pending == 32u) {
-                run_items<VMODE, W, ST>(P, ic.lane_item, lane);
+                run_items<VMODE, W, ST, BD>(P, ic.lane_item, lane);
                 ic.pending = 0;
             }
         }
+        }  // BD
     }
 }
 

@@ -103,9 +103,12 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
 // token histogram counts[token]++ of tokens below `limit` in the same pass
 // (counts may be nullptr).  Sets [lo, hi) only (hi = 0xFFFFFFFF: to the end);
 // ids stay absolute.
+// big_lo: sets from this id on have long prefixes and are emitted a warp
+// per set (below it, a warp per 32 sets).
 cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
                                 uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s,
-                                uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu, uint32_t limit = 0xFFFFFFFFu);
+                                uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu, uint32_t limit = 0xFFFFFFFFu,
+                                uint32_t big_lo = 0xFFFFFFFFu);
 
 // Token records: when no list holds more than REC_ENTRIES entries, list t is
 // the fixed REC_CAP-word record rec[REC_CAP t, REC_CAP t + REC_CAP): word 0
@@ -120,18 +123,31 @@ constexpr uint64_t REC_MAX_TOKENS = 1ull << 25;  // records of larger universes 
 // become entries (set << pos_bits) | position, each taking slot
 // atomicAdd(&counts[token], 1) of its token's record (tokens below `limit`;
 // counts zeroed by the caller).  The slots follow no order.
+// max_sum (optional, a self-join's midprefix index under jaccard or dice):
+// the low pos_bits of each entry hold bound_field instead of the position.
 cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
-                         uint32_t limit, cudaStream_t s, uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu);
+                         uint32_t limit, cudaStream_t s, uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu,
+                         const uint32_t* max_sum = nullptr, uint32_t big_lo = 0xFFFFFFFFu);
 // Pass 2: each record's min(counts[t], REC_ENTRIES) entries in ascending
 // order after its length word, padded with 0xFFFFFFFF.  overflow (optional):
 // OR-ed with REC_OVERFLOW when a token had more entries than a record holds
 // (its record is then incomplete and the index must be built as lists).
+// prev (optional): each record's count at the previous pass (0xFFFFFFFF
+// before the first); a group of 32 records none of whose counts changed is
+// skipped, and prev is brought up to date.  Entries emitted after a pass
+// belong to later sets than every entry before it, so a later pass leaves
+// the ordered front of each record where it was and only fills padding
+// words and the length: a join reading sets below the earlier pass's bound
+// may run beside it.
 constexpr uint32_t REC_OVERFLOW = 16;
 cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s,
-                          uint32_t* overflow = nullptr);
+                          uint32_t* overflow = nullptr, uint32_t* prev = nullptr);
 // Records from index lists already built (every list at most REC_ENTRIES long).
+// max_sum (optional): entries (set << list_bits) | position become
+// (set << rec_bits) | bound_field (sizes: the indexed sets' sizes).
 cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
-                               cudaStream_t s);
+                               cudaStream_t s, const uint32_t* max_sum = nullptr, const uint32_t* sizes = nullptr,
+                               uint32_t list_bits = 0, uint32_t rec_bits = 0);
 
 // Token histogram of n entries into counts[limit] (warp-aggregated atomics;
 // tokens >= limit are skipped; the counts are NOT zeroed here).
@@ -160,6 +176,19 @@ cudaError_t sort_pair_list(uint2* pairs, uint64_t n, int first_bits, int second_
 // empty set, 2 for a set whose tokens are not strictly ascending, 4 for a size
 // smaller than the previous set's, 8 for a set reaching past n_tokens;
 // flags[1] gets the largest token (atomicMax).  flags must be zeroed first.
+// One pass over the n sizes (and starts: given, or the scan of the sizes) of
+// a host-input collection as its copy begins: out[0] gets bit 1 where a size
+// is below the one before it and bit 2 where a given start is not where the
+// set before it ends (or the first start is not 0); out[2..3] the sum of the
+// sizes (u64); first_ge[l] (l in [0, L+1], L the last size) the first set
+// with size >= l (meaningful when the sizes are ordered); and
+// chunk_hi[k] (filled with 0xFFFFFFFF first) the first set that ends past
+// the end of copy chunk k of n_tokens tokens (pipe_chunk), meaningful when
+// the sets are contiguous and ordered.  out must be zeroed.
+cudaError_t size_scan(const uint32_t* sizes, const uint32_t* starts, bool starts_given, uint32_t n, uint32_t L,
+                      uint64_t n_tokens, uint32_t* out, uint32_t* first_ge, uint32_t* chunk_hi, cudaStream_t s);
+
+
 // The same pass writes meta[i] = (starts[i], sizes[i]).
 cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, cudaStream_t s);
 
@@ -178,6 +207,9 @@ struct IndexView {
     uint32_t pos_bits;                      // packed layout: bits of the position field
     int sorted;                             // lists ordered by set id
     int rec = 0;                            // token records: list t = set[REC_CAP t, REC_CAP (t + 1)) (see REC_CAP)
+    // packed entries carry, in place of the position, the longest probe the
+    // entry's side of the positional bound admits (see bound_field)
+    int bound = 0;
 };
 
 struct JoinParams {
@@ -195,9 +227,14 @@ struct JoinParams {
     const uint64_t* __restrict__ bits_S;
     int words;
     Sink out;
-    unsigned int* work;         // work-stealing counter, zero before launch
+    unsigned int* work;         // work-stealing counters, zero before launch ([2] when probes are split)
     uint32_t grab;              // probes taken per steal
     unsigned long long* stats;  // optional [8] counters (nullptr = off)
+    // probe-major prefix filter: probes from heavy_from on (the longest
+    // prefixes; 0xFFFFFFFF = none) are split into `segs` units of seg_slots
+    // prefix slots each, taken one per steal from work[1] before the batches
+    uint32_t heavy_from = 0xFFFFFFFFu;
+    uint32_t segs = 0, seg_slots = 0;
 };
 
 enum Technique : int { TECH_BITMAP = 1, TECH_FGSS = 2, TECH_DIRECT = 3 };

@@ -14,17 +14,31 @@
 namespace hs {
 
 namespace {
-constexpr uint64_t PIPE_CHUNK_TOKENS = 16ull << 20;  // 64 MB of tokens per copy chunk
+constexpr uint64_t JOIN_POINT_TOKENS = 24ull << 20;  // a host-input join runs a piece every 96 MB landed
 }  // namespace
 
-cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k) {
-    while (ctx->pipe_ev.size() <= k) {
+namespace {
+cudaEvent_t nth_event(std::vector<cudaEvent_t>& v, size_t k) {
+    while (v.size() <= k) {
         cudaEvent_t e = nullptr;
         if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
-        ctx->pipe_ev.push_back(e);
+        v.push_back(e);
     }
-    return ctx->pipe_ev[k];
+    return v[k];
 }
+
+// Token offsets where the copy chunks of a host-input join end (pipe_chunk).
+std::vector<uint64_t> chunk_ends(uint64_t n_tokens) {
+    std::vector<uint64_t> ends;
+    for (uint64_t t = 0; t < n_tokens;) {
+        t += pipe_chunk(n_tokens - t);
+        ends.push_back(t);
+    }
+    return ends;
+}
+}  // namespace
+
+cudaEvent_t pipe_event(hyset_ctx* ctx, size_t k) { return nth_event(ctx->pipe_ev, k); }
 
 }  // namespace hs
 
@@ -256,38 +270,50 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         CK(ctx->sc->scan.ensure(scan_scratch_words(n_sets) * 4, s));
         CK(scan_exclusive(C->d_sizes, C->starts.as<uint32_t>(), n_sets, ctx->sc->scan.as<uint32_t>(), s));
     }
-    const uint64_t n_chunks = n_tokens ? (n_tokens + PIPE_CHUNK_TOKENS - 1) / PIPE_CHUNK_TOKENS : 0;
+    const std::vector<uint64_t> ends = chunk_ends(n_tokens);
+    const uint64_t n_chunks = ends.size();
     for (uint64_t k = 0; k < n_chunks; ++k) {
-        const uint64_t t0 = k * PIPE_CHUNK_TOKENS, t1 = std::min(n_tokens, t0 + PIPE_CHUNK_TOKENS);
+        const uint64_t t0 = k ? ends[k - 1] : 0, t1 = ends[k];
         CK(cudaMemcpyAsync(C->tokens.as<uint32_t>() + t0, tokens + t0, (t1 - t0) * 4, cudaMemcpyHostToDevice, cp));
         cudaEvent_t e = pipe_event(ctx, k);
         if (!e) return bail(fail(ctx, HYSET_E_CUDA, "event creation"));
         CK(cudaEventRecord(e, cp));
     }
-    // 2. on the host meanwhile, one pass over the sizes: contiguity of the given
-    //    starts, size order, and for every chunk the first set that ends past it
-    //    (sets before it are complete once the chunk has landed)
+    // 2. one device pass over the sizes (and starts) while the tokens are copied:
+    //    size order, contiguity of given starts, the total size, first_ge, and
+    //    for every chunk the first set that ends past it (sets before it are
+    //    complete once the chunk has landed), read back with one wait (a host
+    //    pass over a million sets outlasted the copy of the first chunks)
     bool contiguous = true, ordered = true;
     std::vector<uint32_t> chunk_hi(n_chunks, n_sets);
     {
-        uint64_t run = 0, bound = PIPE_CHUNK_TOKENS, k = 0;
-        uint32_t prev = 0;
-        for (uint32_t i = 0; i < n_sets; ++i) {
-            const uint32_t z = sizes[i];
-            if (starts_given) contiguous &= starts[i] == run;
-            ordered &= z >= prev;
-            prev = z;
-            const uint64_t end = run + z;
-            while (k < n_chunks && end > bound) {
-                chunk_hi[k++] = i;
-                bound += PIPE_CHUNK_TOKENS;
-            }
-            run = end;
-        }
-        if (!starts_given && run > n_tokens) return bail(fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens"));
+        const uint32_t L = n_sets ? sizes[n_sets - 1] : 0;  // the largest size once the order is confirmed
+        if (n_chunks > PIPE_MAX_CHUNKS) return bail(fail(ctx, HYSET_E_UNSUPPORTED, "too many copy chunks"));
+        const size_t words = 4 + n_chunks;  // flags, spare, total size (u64), chunk_hi[n_chunks]
+        CK(C->first_ge.ensure(((size_t)L + 2) * 4, s));
+        CK(ctx->sc->sscan.ensure(words * 4, s));
+        uint32_t* d = ctx->sc->sscan.as<uint32_t>();
+        CK(cudaMemsetAsync(d, 0, 16, s));
+        CK(cudaMemsetAsync(d + 4, 0xFF, n_chunks * 4, s));
+        CK(size_scan(C->d_sizes, C->d_starts, starts_given, n_sets, L, n_tokens, d, C->first_ge.as<uint32_t>(), d + 4,
+                     s));
+        void* stage = nullptr;
+        ST(host_stage(ctx, (words + L + 2) * 4, &stage));
+        uint32_t* h = static_cast<uint32_t*>(stage);
+        CK(cudaMemcpyAsync(h, d, words * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(h + words, C->first_ge.p, ((size_t)L + 2) * 4, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        ordered = (h[0] & 1u) == 0;
+        contiguous = !starts_given || (h[0] & 2u) == 0;
+        uint64_t run = 0;
+        std::memcpy(&run, h + 2, 8);
+        // contiguous sets past the token array: rejected here, before any
+        // kernel reads them (the device checks are read only after the join)
+        if (contiguous && run > n_tokens) return bail(fail(ctx, HYSET_E_INVALID, "sizes sum past n_tokens"));
+        if (!ordered) return bail(fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size"));
+        for (uint64_t k = 0; k < n_chunks; ++k) chunk_hi[k] = h[4 + k] == 0xFFFFFFFFu ? n_sets : h[4 + k];
+        size_meta_from_first_ge(C, h + words, L);
     }
-    if (!ordered) return bail(fail(ctx, HYSET_E_INVALID, "sets must be ordered by non-decreasing size"));
-    ST(build_size_meta(ctx, C, sizes));
     // 3. the configuration, from the options or the context's earlier choices
     const hyset_join_opts* o = opts;
     bool pipelined = contiguous && n_sets > 0;
@@ -375,7 +401,11 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
         auto lit = ctx->longest_cache.find(key);
         bool records = assumed && lit != ctx->longest_cache.end() && lit->second <= REC_ENTRIES &&
                        (uint64_t)U <= REC_MAX_TOKENS;
-        if (records) CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
+        if (records) {
+            CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
+            record_layout(C, b, 0, pb, &ix.rec_bits, &ix.rec_bound);
+        }
+        const uint32_t big_lo = first_long_prefix(C, b->index_prefix);  // emitted a warp per set from here on
         bool lists_ready = false;  // prefix lengths and entry offsets computed
         auto prepare_lists = [&]() -> hyset_status {
             if (lists_ready) return HYSET_OK;
@@ -385,6 +415,62 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             return HYSET_OK;
         };
         if (!records) ST(prepare_lists());
+        // With records, the join runs in pieces while the copy goes on: once the
+        // entries of every landed set are in the records and the records are
+        // ordered, the landed probes have every candidate they can pair with (a
+        // candidate comes before its probe in size order), so they are joined
+        // then, on the context's stream (the copy engine keeps copying); the
+        // pairs of all pieces go to one buffer.
+        const bool streamed = records && n_chunks > 1;
+        JoinParams SP{};
+        uint64_t cap = 0;
+        uint32_t* prev = nullptr;  // each record's count at the last ordering pass
+        uint32_t join_launches = 0, join_lo = 0;  // probes [0, join_lo) are joined
+        uint64_t joined_to = 0;                    // the tokens that had landed at the last join point
+        if (streamed) {
+            ix.records = true;
+            ix.sim = b->sim;
+            ix.tau = b->tau;
+            ix.kind = 0;
+            ix.universe = U;
+            ix.entries = E;
+            ix.pos_bits = pb;
+            const bool count_only = o->count_only != 0;
+            cap = count_only ? 0 : (o->pair_capacity ? o->pair_capacity : std::max<uint64_t>(1u << 20, 4ull * n));
+            CK(ctx->s_count.ensure(16, s));
+            CK(ctx->s_work.ensure((2 * n_chunks + 4) * 4, s));
+            CK(ctx->s_stats.ensure(64, s));
+            if (!count_only) CK(ctx->s_pairs.ensure(std::max<uint64_t>(cap, 1) * sizeof(uint2), s));
+            CK(ctx->sc->order.ensure((size_t)U * 4 + 4, s));
+            prev = ctx->sc->order.as<uint32_t>();
+            CK(cudaMemsetAsync(prev, 0xFF, (size_t)U * 4, s));  // the first pass orders every record
+            // every record word padding until written: a join reading a record
+            // while a later pass orders it sees only entries of its own and
+            // earlier chunks in place, padding, or entries of later sets (above
+            // every window it counts), never a word left from an earlier call
+            CK(cudaMemsetAsync(ix.rec.p, 0xFF, (size_t)U * REC_CAP * 4, s));
+            CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+            CK(cudaMemsetAsync(ctx->s_work.p, 0, (2 * n_chunks + 4) * 4, s));
+            if (o->collect_stats) CK(cudaMemsetAsync(ctx->s_stats.p, 0, 64, s));
+            SP.R = C->view();
+            SP.S = SP.R;
+            SP.B = b->view;
+            SP.first_ge = C->first_ge.as<uint32_t>();
+            SP.R_L = C->max_size;
+            SP.self = 1;
+            SP.grab = std::min<uint32_t>(tn.batch, 32);
+            SP.r_lo = 0;
+            SP.r_hi = n;
+            SP.X = ix.view();
+            split_heavy(C, b, SP);
+            if (words) {
+                SP.bits_R = SP.bits_S = bits.as<uint64_t>();
+                SP.words = words;
+            }
+            SP.out = Sink{count_only ? nullptr : ctx->s_pairs.as<uint2>(), ctx->s_count.as<unsigned long long>(), cap,
+                          count_only ? 1 : 0, 0};
+            SP.stats = o->collect_stats ? ctx->s_stats.as<unsigned long long>() : nullptr;
+        }
         uint32_t lo = 0;
         for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
             // sets whose tokens end inside the chunks copied so far
@@ -398,11 +484,27 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             part.n = hi - lo;
             CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
             if (records)
-                CK(emit_records(v, b->view.index_prefix, pb, counts, ix.rec.as<uint32_t>(), U, s, lo, hi));
+                CK(emit_records(v, b->view.index_prefix, ix.rec_bits, counts, ix.rec.as<uint32_t>(), U, s, lo, hi,
+                                ix.rec_bound ? b->view.max_sum : nullptr, big_lo));
             else
                 CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s,
-                                       lo, hi, U + 1));
+                                       lo, hi, U + 1, big_lo));
             if (words) CK(generate_bitmaps(part, words, bits.as<uint64_t>() + (size_t)lo * words, s));
+            // at a join point (the last chunk, or JOIN_POINT_TOKENS since the last
+            // one): order the records, then join the probes not joined yet, all
+            // in stream order while the next chunks are copied
+            if (streamed && (k + 1 == n_chunks || ends[k] - joined_to >= JOIN_POINT_TOKENS)) {
+                CK(order_records(counts, U, ix.rec.as<uint32_t>(), s, ctx->s_flags.as<uint32_t>(), prev));
+                if (join_launches == 0) CK(cudaEventRecord(ctx->ek0, s));
+                JoinParams Q = SP;
+                Q.p_lo = join_lo;
+                Q.p_hi = hi;
+                Q.work = ctx->s_work.as<unsigned int>() + 2 * join_launches;  // probe batches, split probes
+                CK(launch_join(Q, TECH_FGSS, tn.vmode, ctx->sm_count, s));
+                ++join_launches;
+                join_lo = hi;
+                joined_to = ends[k];
+            }
             lo = hi;
         }
         if (n_chunks) CK(cudaStreamWaitEvent(s, pipe_event(ctx, n_chunks - 1), 0));  // every copy has landed
@@ -424,7 +526,33 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             U = f[1] + 1;
         }
         JoinParams P{};
-        for (int attempt = 0; attempt < 2; ++attempt) {
+        bool joined = false;  // the chunk-by-chunk join stands
+        if (streamed) {
+            CK(cudaEventRecord(ctx->ek1, s));
+            CK(cudaEventRecord(ctx->ev1, s));
+            CK(cudaMemcpyAsync(f, ctx->s_flags.p, 8, cudaMemcpyDeviceToHost, s));
+            CK(cudaMemcpyAsync(f + 10, ctx->s_count.p, 8, cudaMemcpyDeviceToHost, s));
+            if (SP.stats) CK(cudaMemcpyAsync(res->stats, SP.stats, 64, cudaMemcpyDeviceToHost, s));
+            CK(cudaStreamSynchronize(s));
+            const hyset_status vs = verdict();
+            if (vs != HYSET_OK) return bail(vs);
+            unsigned long long count = 0;
+            std::memcpy(&count, f + 10, 8);
+            // a list that outgrew its record, a token past the assumed universe
+            // or a full pair buffer: the join is run again below (records, then lists)
+            if (!(f[0] & REC_OVERFLOW) && f[1] + 1 <= U && (o->count_only || count <= cap)) {
+                float ms = 0, kms = 0;
+                CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+                CK(cudaEventElapsedTime(&kms, ctx->ek0, ctx->ek1));
+                res->device_ms = ms;
+                res->kernel_ms = kms;
+                res->count = count;
+                P = SP;
+                ST(deliver_pairs(ctx, P, o, res.get()));
+                joined = true;
+            }
+        }
+        for (int attempt = 0; attempt < 2 && !joined; ++attempt) {
             C->universe = U;
             CK(ctx->sc->counts.ensure(((size_t)U + 1) * 4, s));
             CK(ix.list_off.ensure(((size_t)U + 1) * 4, s));
@@ -436,7 +564,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
                 ST(prepare_lists());
                 if (attempt > 0 || records)  // the list build reordered the entries (or none were emitted): emit them
                     CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), nullptr,
-                                           s));
+                                           s, 0, 0xFFFFFFFFu, 0xFFFFFFFFu, big_lo));
                 counts = ctx->sc->counts.as<uint32_t>();
                 if (!(assumed && attempt == 0)) {  // not counted while the chunks landed
                     CK(cudaMemsetAsync(counts, 0, ((size_t)U + 1) * 4, s));
@@ -466,6 +594,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             P.r_lo = 0;
             P.r_hi = n;
             P.X = ix.view();
+            split_heavy(C, b, P);
             if (words) {
                 P.bits_R = P.bits_S = bits.as<uint64_t>();
                 P.words = words;

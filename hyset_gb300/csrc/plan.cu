@@ -324,6 +324,7 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     P.self = self ? 1 : 0;
     P.r_lo = 0;
     P.r_hi = R->n;
+    split_heavy(S, b, P);
     const uint32_t grab_cap = P.X2.set ? 16u : 32u;  // banded R-S joins: two lanes per probe
     const uint32_t base_batch = std::min(o->fgss_batch ? o->fgss_batch : DEFAULT_PROBE_BATCH, grab_cap);
     P.grab = base_batch;
@@ -430,7 +431,10 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     // cosine); an explicit mode is kept
     int vm = o->verify_mode == 2 ? 2 : 1;
     ST(use_width(best));
-    if (learned) ST(sample(1, &cur_ms));  // the predicted width's own estimate (the base of the comparisons below)
+    if (learned) {  // the predicted width's own estimate (the base of the comparisons below)
+        ST(sample(1, &cur_ms));  // the first run after the generation warms the caches: not kept
+        ST(sample(1, &cur_ms));
+    }
     if (vmode) {
         float warp_ms = 0;
         ST(sample(2, &warp_ms));

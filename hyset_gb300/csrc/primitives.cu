@@ -302,18 +302,21 @@ constexpr int EMIT_ROUNDS = 8;
 template <bool REC>
 __global__ void __launch_bounds__(256, REC ? HS_REC_EMIT_MINB : 1) k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
-                              uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit) {
+                              uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit,
+                              const uint32_t* __restrict__ max_sum, uint32_t spw) {
     constexpr int ROUNDS = REC ? HS_REC_EMIT_ROUNDS : EMIT_ROUNDS;
+    const uint32_t maxf = (1u << pos_bits) - 1u;
     const int lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t s0 = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u; s0 < c.n; s0 += warps * 32u) {
+    for (uint32_t s0 = lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * spw; s0 < c.n; s0 += warps * spw) {
         const uint32_t s = s0 + lane;
-        const bool has = s < c.n;
-        uint32_t l, start, o0 = 0;
+        const bool has = (uint32_t)lane < spw && s < c.n;
+        uint32_t l, start, o0 = 0, size = 0;
         if constexpr (REC) {  // len is the prefix table by size; no offsets
             const uint2 m = has ? c.meta[s] : make_uint2(0, 0);
             l = has ? len[m.y] : 0u;
             start = m.x;
+            size = m.y;
         } else {
             l = has ? len[s] : 0u;
             start = has ? c.meta[s].x : 0u;
@@ -337,7 +340,12 @@ __global__ void __launch_bounds__(256, REC ? HS_REC_EMIT_MINB : 1) k_emit_packed
                 const uint32_t start_k = __shfl_sync(FULL, start, k);
                 const uint32_t i = j - excl_k;
                 tok[u] = j < total ? __ldg(c.tokens + start_k + i) : 0u;
-                val[u] = ((s0 + (uint32_t)k) << pos_bits) | i;
+                uint32_t low = i;
+                if constexpr (REC) {
+                    const uint32_t size_k = __shfl_sync(FULL, size, k);
+                    if (max_sum && j < total) low = bound_field(max_sum, size_k, i, maxf);
+                }
+                val[u] = ((s0 + (uint32_t)k) << pos_bits) | low;
             }
             if constexpr (REC) {
                 // every round's slot atomic is in flight before the first store
@@ -511,7 +519,8 @@ __global__ void __launch_bounds__(RANK_THREADS) k_list_rank(const uint32_t* __re
 constexpr int REC_THREADS = 256;
 __host__ __device__ constexpr uint32_t record_pieces(uint32_t n) { return n > 7u ? 1u + (n - 7u + 7u) / 8u : 1u; }
 __global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* __restrict__ counts, uint32_t U,
-                                                               uint32_t* __restrict__ rec, uint32_t* overflow) {
+                                                               uint32_t* __restrict__ rec, uint32_t* overflow,
+                                                               uint32_t* __restrict__ prev) {
     __shared__ uint32_t stage_all[REC_THREADS / 32][32 * 33];
     const int lane = threadIdx.x & 31;
     uint32_t* stage = stage_all[threadIdx.x >> 5];
@@ -520,6 +529,11 @@ __global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* _
          t0 += (uint64_t)warps * 32) {
         const uint32_t nrec = U - t0 < 32 ? (uint32_t)(U - t0) : 32u;
         const uint32_t cnt = (uint32_t)lane < nrec ? counts[t0 + lane] : 0u;
+        if (prev) {  // incremental pass: only groups with new entries
+            const bool changed = (uint32_t)lane < nrec && prev[t0 + lane] != cnt;
+            if (!__any_sync(FULL, changed)) continue;
+            if (changed) prev[t0 + lane] = cnt;
+        }
         if (overflow && __any_sync(FULL, cnt > REC_ENTRIES) && lane == 0) atomicOr(overflow, REC_OVERFLOW);
         const uint32_t mine = min(cnt, REC_ENTRIES);
         uint4* g = reinterpret_cast<uint4*>(rec + t0 * REC_CAP);
@@ -568,12 +582,18 @@ __global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* _
 // Records from built lists: a warp per token, lane 0 writes the length, lane
 // i > 0 entry i - 1 or the pad.
 __global__ void k_records_from_lists(const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ vals,
-                                     uint32_t U, uint32_t* __restrict__ rec) {
+                                     uint32_t U, uint32_t* __restrict__ rec, const uint32_t* __restrict__ max_sum,
+                                     const uint32_t* __restrict__ sizes, uint32_t list_bits, uint32_t rec_bits) {
     const int lane = threadIdx.x & 31;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < U; t += warps) {
         const uint32_t a = list_off[t], b = list_off[t + 1];
-        rec[t * REC_CAP + lane] = lane == 0 ? b - a : (a + lane - 1 < b ? vals[a + lane - 1] : 0xFFFFFFFFu);
+        uint32_t w = lane == 0 ? b - a : (a + lane - 1 < b ? vals[a + lane - 1] : 0xFFFFFFFFu);
+        if (max_sum && lane > 0 && a + lane - 1 < b) {  // (set, position) -> (set, bound field)
+            const uint32_t set = w >> list_bits, pos = w & ((1u << list_bits) - 1u);
+            w = (set << rec_bits) | bound_field(max_sum, sizes[set], pos, (1u << rec_bits) - 1u);
+        }
+        rec[t * REC_CAP + lane] = w;
     }
 }
 
@@ -829,44 +849,123 @@ cudaError_t emit_prefix_entries(CollView c, uint32_t lo, uint32_t hi, const uint
     return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(256) k_size_scan(const uint32_t* __restrict__ sizes,
+                                                   const uint32_t* __restrict__ starts, int starts_given, uint32_t n,
+                                                   uint32_t L, uint64_t n_tokens, uint32_t* out,
+                                                   uint32_t* __restrict__ first_ge, uint32_t* __restrict__ chunk_hi) {
+    __shared__ uint64_t ends[PIPE_MAX_CHUNKS];
+    __shared__ uint32_t n_ends;
+    __shared__ uint32_t bflags;
+    __shared__ unsigned long long bsum;
+    if (threadIdx.x == 0) {  // the copy schedule, as the host makes it
+        uint32_t k = 0;
+        for (uint64_t t = 0; t < n_tokens && k < PIPE_MAX_CHUNKS;) {
+            t += pipe_chunk(n_tokens - t);
+            ends[k++] = t;
+        }
+        n_ends = k;
+        bflags = 0;
+        bsum = 0;
+    }
+    __syncthreads();
+    uint32_t flags = 0;
+    unsigned long long sum = 0;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += stride) {
+        // first_ge[l] = i for l in (sizes[i-1], sizes[i]] (from 0 for i = 0; up to L + 1 for i = n)
+        const uint32_t lo = i == 0 ? 0u : min(sizes[i - 1], L + 1u) + 1u;
+        const uint32_t hi = i == n ? L + 1u : min(sizes[i], L + 1u);
+        for (uint32_t l = lo; l <= hi; ++l) first_ge[l] = i;
+        if (i == n) continue;
+        const uint32_t z = sizes[i];
+        sum += z;
+        if (i > 0 && z < sizes[i - 1]) flags |= 1u;
+        if (starts_given && starts[i] != (i ? starts[i - 1] + sizes[i - 1] : 0u)) flags |= 2u;
+        // the chunks whose end lies in [end of set i - 1, end of set i): set i is the first to end past them
+        const uint64_t e1 = (uint64_t)starts[i] + z, e0 = i ? (uint64_t)starts[i - 1] + sizes[i - 1] : 0ull;
+        uint32_t a = 0, b = n_ends;  // first chunk with end >= e0
+        while (a < b) {
+            const uint32_t m = (a + b) >> 1;
+            if (ends[m] < e0) a = m + 1;
+            else b = m;
+        }
+        for (uint32_t k = a; k < n_ends && ends[k] < e1; ++k) chunk_hi[k] = i;
+    }
+    if (flags) atomicOr(&bflags, flags);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+    if ((threadIdx.x & 31) == 0 && sum) atomicAdd(&bsum, sum);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (bflags) atomicOr(out, bflags);
+        if (bsum) atomicAdd(reinterpret_cast<unsigned long long*>(out + 2), bsum);
+    }
+}
+
+cudaError_t size_scan(const uint32_t* sizes, const uint32_t* starts, bool starts_given, uint32_t n, uint32_t L,
+                      uint64_t n_tokens, uint32_t* out, uint32_t* first_ge, uint32_t* chunk_hi, cudaStream_t s) {
+    note_launches();
+    k_size_scan<<<grid_for((uint64_t)n + 1, 256, 152u * 8u), 256, 0, s>>>(sizes, starts, starts_given ? 1 : 0, n, L,
+                                                                        n_tokens, out, first_ge, chunk_hi);
+    return cudaGetLastError();
+}
+
+namespace {
+// Sets [lo, hi) in two launches: below big_lo a warp per 32 sets, from big_lo
+// on (the sets with long prefixes) a warp per set, so that no warp walks 32
+// long prefixes alone while the others have finished.
+template <bool REC>
+cudaError_t launch_emit(CollView c, uint32_t lo, uint32_t hi, uint32_t big_lo, const uint32_t* off,
+                        const uint32_t* len, uint32_t pos_bits, uint32_t* e_token, uint32_t* e_val, uint32_t* counts,
+                        uint32_t limit, const uint32_t* max_sum, cudaStream_t s) {
+    if (hi == 0xFFFFFFFFu) hi = c.n;
+    const uint32_t mid = std::min(std::max(lo, big_lo), hi);
+    CollView v = c;
+    if (mid > lo) {
+        note_launches();
+        v.n = mid;  // the kernel walks ids [lo, mid)
+        k_emit_packed<REC><<<grid_for((uint64_t)(mid - lo), 256), 256, 0, s>>>(v, lo, off, len, pos_bits, e_token,
+                                                                             e_val, counts, limit, max_sum, 32u);
+    }
+    if (hi > mid) {
+        note_launches();
+        v.n = hi;
+        k_emit_packed<REC><<<grid_for((uint64_t)(hi - mid) * 32u, 256), 256, 0, s>>>(v, mid, off, len, pos_bits,
+                                                                                   e_token, e_val, counts, limit,
+                                                                                   max_sum, 1u);
+    }
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
                                 uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s, uint32_t lo,
-                                uint32_t hi, uint32_t limit) {
-    if (hi == 0xFFFFFFFFu) hi = c.n;
-    if (hi <= lo) return cudaSuccess;
-    note_launches();
-    CollView v = c;
-    v.n = hi;  // the kernel walks ids [lo, hi)
-    k_emit_packed<false><<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, entry_off, len, pos_bits, e_token,
-                                                                            e_val, counts, limit);  // a warp per 32 sets
-    return cudaGetLastError();
+                                uint32_t hi, uint32_t limit, uint32_t big_lo) {
+    return launch_emit<false>(c, lo, hi, big_lo, entry_off, len, pos_bits, e_token, e_val, counts, limit, nullptr, s);
 }
 
 cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
-                         uint32_t limit, cudaStream_t s, uint32_t lo, uint32_t hi) {
-    if (hi == 0xFFFFFFFFu) hi = c.n;
-    if (hi <= lo) return cudaSuccess;
-    note_launches();
-    CollView v = c;
-    v.n = hi;  // the kernel walks ids [lo, hi)
-    k_emit_packed<true><<<grid_for((uint64_t)(hi - lo), 256), 256, 0, s>>>(v, lo, nullptr, prefix_tab, pos_bits, nullptr,
-                                                                           rec, counts, limit);
-    return cudaGetLastError();
+                         uint32_t limit, cudaStream_t s, uint32_t lo, uint32_t hi, const uint32_t* max_sum,
+                         uint32_t big_lo) {
+    return launch_emit<true>(c, lo, hi, big_lo, nullptr, prefix_tab, pos_bits, nullptr, rec, counts, limit, max_sum, s);
 }
 
-cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s, uint32_t* overflow) {
+cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s, uint32_t* overflow,
+                          uint32_t* prev) {
     if (U == 0) return cudaSuccess;
     note_launches();
     k_order_records<<<grid_for(((uint64_t)U + 31) / 32 * 32, REC_THREADS), REC_THREADS, 0, s>>>(counts, U, rec,
-                                                                                              overflow);
+                                                                                              overflow, prev);
     return cudaGetLastError();
 }
 
 cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
-                               cudaStream_t s) {
+                               cudaStream_t s, const uint32_t* max_sum, const uint32_t* sizes, uint32_t list_bits,
+                               uint32_t rec_bits) {
     if (U == 0) return cudaSuccess;
     note_launches();
-    k_records_from_lists<<<grid_for((uint64_t)U * 32, 256), 256, 0, s>>>(list_off, vals, U, rec);
+    k_records_from_lists<<<grid_for((uint64_t)U * 32, 256), 256, 0, s>>>(list_off, vals, U, rec, max_sum, sizes,
+                                                                         list_bits, rec_bits);
     return cudaGetLastError();
 }
 

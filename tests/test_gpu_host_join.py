@@ -121,3 +121,32 @@ def test_host_join_records_and_a_list_that_outgrows_them(ctx):
     for toks, want in ((c.tokens, exp), (c.tokens, exp), (grown, exp_grown), (c.tokens, exp), (c.tokens, exp)):
         r = ctx.self_join_host(toks, c.sizes, c.starts, threshold=0.8, **PIPELINED)
         assert r.count == len(want) and oracle.as_set(r.pairs) == want
+
+
+def test_host_join_chunk_by_chunk(ctx):
+    """A repeat of a size profile whose index lists fit token records, in more
+    than one copy chunk: each chunk's probes are joined as soon as its entries
+    are in the records and ordered, beside the copies of the later chunks.
+    Every call must return the oracle's pairs: plain repeats, a pair buffer
+    too small (the join runs again with room), a list that outgrows its record
+    and a token past the assumed universe (both run again over lists), count
+    only and work counters."""
+    c = synth.generate(synth.C3, n_sets=200000, seed=131)
+    assert c.tokens.size > (16 << 20)
+    base = (c.tokens.astype(np.int64) + 1).astype(np.uint32)  # token 0 unused: same pairs
+    exp = oracle.as_set(oracle.join(base, c.starts, c.sizes, 0.8))
+    grown = base.copy()
+    grown[c.starts[np.random.default_rng(7).choice(c.n, size=40, replace=False)]] = 0  # 40 prefixes share token 0
+    exp_grown = oracle.as_set(oracle.join(grown, c.starts, c.sizes, 0.8))
+    shifted = (base.astype(np.int64) + 2_000_000).astype(np.uint32)
+    calls = [(base, exp, {}), (base, exp, {}), (base, exp, {}), (base, exp, dict(pair_capacity=64)),
+             (grown, exp_grown, {}), (base, exp, {}), (base, exp, {}), (shifted, exp, {}), (base, exp, {}),
+             (base, exp, {}), (base, exp, {})]
+    for i, (toks, want, kw) in enumerate(calls):
+        r = ctx.self_join_host(toks, c.sizes, c.starts, threshold=0.8, **PIPELINED, **kw)
+        assert r.count == len(want) and oracle.as_set(r.pairs) == want, (i, kw)
+    r = ctx.self_join_host(base, c.sizes, c.starts, threshold=0.8, count_only=True, **PIPELINED)
+    assert r.count == len(exp)
+    r = ctx.self_join_host(base, c.sizes, None, threshold=0.8, collect_stats=True, **PIPELINED)
+    assert r.count == len(exp) and oracle.as_set(r.pairs) == exp
+    assert r.stats[0] > 0 and r.stats[3] > 0  # filter items, index entries
