@@ -133,12 +133,15 @@ def ncu_traffic():
 def algorithmic_bytes(st, count, words, n_probes):
     """Bytes the probe-major filter+verify launch must touch, from its own work
     counters: per probe its (start, size) record (8); per prefix token the token
-    and its list bounds (12); per index entry in a window the packed entry and
-    the candidate's (start, size) (12); per signature check both signatures
-    (16 W); per token read by verification 4; per result pair 8."""
+    and its list bounds (12); per index entry in a window the packed entry (4);
+    per entry that passes the entry's side of the positional bound (all of
+    them unless the records carry that bound) the candidate's (start, size)
+    (8); per signature check both signatures (16 W); per token read by
+    verification 4; per result pair 8."""
     prefix_tokens, items, bitmap_checks, verify_tokens = st[4], st[0], st[5], st[6]
-    return (8 * n_probes + 12 * prefix_tokens + 12 * items + 16 * words * bitmap_checks + 4 * verify_tokens
-            + 8 * count)
+    entries = st[7] or items
+    return (8 * n_probes + 12 * prefix_tokens + 4 * entries + 8 * items + 16 * words * bitmap_checks
+            + 4 * verify_tokens + 8 * count)
 
 
 def cpu_baseline(c, threads, sample_note, sim="jaccard"):

@@ -581,6 +581,7 @@ __device__ void fgss_carry(const JoinParams& P, uint32_t i0, uint32_t k, int lan
                 const uint32_t ipst = __shfl_sync(FULL, pst, it);
                 bool ok = false;
                 uint32_t c = 0;
+                count_stat<ST>(P, 7, has ? 1u : 0u, lane);  // index entries in windows, before the bound
                 if (has) {
                     const uint32_t v = x_set[f_jj + (qi - (i_jj - c_jj))];
                     c = v >> P.X.pos_bits;

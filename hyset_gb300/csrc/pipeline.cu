@@ -482,14 +482,18 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             part.starts += lo;
             part.meta += lo;
             part.n = hi - lo;
-            CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
+            // the checks (and the signatures, in the same pass over the tokens)
+            if (words)
+                CK(validate_with_bitmaps(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, words,
+                                         bits.as<uint64_t>() + (size_t)lo * words, s));
+            else
+                CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
             if (records)
                 CK(emit_records(v, b->view.index_prefix, ix.rec_bits, counts, ix.rec.as<uint32_t>(), U, s, lo, hi,
                                 ix.rec_bound ? b->view.max_sum : nullptr, big_lo));
             else
                 CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s,
                                        lo, hi, U + 1, big_lo));
-            if (words) CK(generate_bitmaps(part, words, bits.as<uint64_t>() + (size_t)lo * words, s));
             // at a join point (the last chunk, or JOIN_POINT_TOKENS since the last
             // one): order the records, then join the probes not joined yet, all
             // in stream order while the next chunks are copied

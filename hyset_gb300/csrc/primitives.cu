@@ -700,6 +700,76 @@ __global__ void __launch_bounds__(BITMAP_THREADS) k_bitmaps(CollView c, uint64_t
     }
 }
 
+// The checks of k_validate and the signatures of k_bitmaps in one pass over
+// the tokens of the sets of c (eight lanes per set, as k_bitmaps): the set's
+// meta pair is written from its start and size, and its tokens are read once
+// for both (the order check reads each token's successor, an L1 hit).
+template <int W>
+__global__ void __launch_bounds__(BITMAP_THREADS) k_validate_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags,
+                                                                    uint2* meta, uint64_t* out) {
+    constexpr int NW = 2 * W;
+    __shared__ uint32_t sw[BITMAP_THREADS / 8][NW];
+    const int lane = threadIdx.x & 31, g = lane & 7;
+    uint32_t* mine = sw[threadIdx.x >> 3];
+    const uint32_t mask = 64u * W - 1u;
+    const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
+    uint32_t* out32 = reinterpret_cast<uint32_t*>(out);
+    uint32_t f = 0, mx = 0;
+    const uint32_t rounds = (c.n + groups - 1) / groups;  // the same for every lane: the warp barriers match
+    uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    for (uint32_t r = 0; r < rounds; ++r, s += groups) {
+#pragma unroll
+        for (int q = g; q < NW; q += 8) mine[q] = 0u;
+        __syncwarp();
+        const bool live = s < c.n;
+        uint32_t st = 0, l = 0;
+        if (live) {
+            st = c.starts[s];
+            l = c.sizes[s];
+            if (g == 0) meta[s] = make_uint2(st, l);
+            if (l == 0) f |= 1;
+            if (s > 0 && c.sizes[s - 1] > l) f |= 4;
+            if ((uint64_t)st + l > n_tokens) {
+                f |= 8;
+                l = 0;
+            } else if (l > 0 && g == 0) {
+                mx = max(mx, c.tokens[st + l - 1]);
+            }
+        }
+        const uint32_t* t = c.tokens + st;
+        for (uint32_t i0 = g; i0 < l; i0 += 8 * BITMAP_UNROLL) {
+            uint32_t tok[BITMAP_UNROLL], nxt[BITMAP_UNROLL];
+#pragma unroll
+            for (int u = 0; u < BITMAP_UNROLL; ++u) {
+                const uint32_t i = i0 + 8u * u;
+                tok[u] = i < l ? __ldg(t + i) : 0xFFFFFFFFu;
+                nxt[u] = i + 1 < l ? __ldg(t + i + 1) : 0xFFFFFFFFu;
+            }
+#pragma unroll
+            for (int u = 0; u < BITMAP_UNROLL; ++u) {
+                const uint32_t i = i0 + 8u * u;
+                if (i < l) {
+                    if (i + 1 < l && tok[u] >= nxt[u]) f |= 2;
+                    const uint32_t b = tok[u] & mask;
+                    atomicXor(&mine[b >> 5], 1u << (b & 31));
+                }
+            }
+        }
+        __syncwarp();
+        if (live) {
+#pragma unroll
+            for (int q = g; q < NW; q += 8) out32[(uint64_t)s * NW + q] = mine[q];
+        }
+        __syncwarp();
+    }
+    f = __reduce_or_sync(FULL, f);
+    mx = __reduce_max_sync(FULL, mx);
+    if (lane == 0) {
+        if (f) atomicOr(&flags[0], f);
+        atomicMax(&flags[1], mx);
+    }
+}
+
 // One warp per set: checks the input contract and writes the set's (start,
 // size) pair.  The largest token is kept per lane and reduced once per warp, so
 // the kernel makes one atomic per warp, not one per set.
@@ -1082,6 +1152,21 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
     if (c.n == 0) return cudaSuccess;
     note_launches();
     k_validate<<<grid_for((uint64_t)c.n * 32, 256), 256, 0, s>>>(c, n_tokens, flags, meta);
+    return cudaGetLastError();
+}
+
+cudaError_t validate_with_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, int words, uint64_t* out,
+                                  cudaStream_t s) {
+    if (c.n == 0) return cudaSuccess;
+    const unsigned g = grid_for((uint64_t)c.n * 8, BITMAP_THREADS);
+    note_launches();
+    switch (words) {
+    case 1: k_validate_bitmaps<1><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 2: k_validate_bitmaps<2><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 4: k_validate_bitmaps<4><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 8: k_validate_bitmaps<8><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
