@@ -234,7 +234,7 @@ def run_ours(args, ws, rank, local):
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     kw = dict(threshold=THRESHOLD, sim=args.sim, technique=args.technique, bitmap=args.bitmap, device_pairs=True,
-              probe_range=(p_lo, p_hi), probe_major=args.probe_major, verify_mode=args.vmode)
+              probe_range=(p_lo, p_hi), probe_major=args.probe_major, verify_mode=args.vmode, fgss_batch=args.batch)
 
     def barrier():
         torch.cuda.synchronize()
@@ -726,6 +726,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-join batch leg")
     ap.add_argument("--sets", type=int, default=0, help="smaller case of the same workload (profiling)")
     ap.add_argument("--probe-major", action="store_true", help="FGSS: probe-major kernel instead of token-major")
+    ap.add_argument("--batch", type=int, default=0, help="probe batch of the probe-major kernel; 0 = the autotuner")
     ap.add_argument("--vmode", type=int, default=0,
                     help="verification: 0 auto (the autotuner's samples choose), 1 lane, 2 warp per candidate")
     ap.add_argument("--workload", default="selfjoin", choices=["selfjoin", "batch", "parse", "verify", "c1", "c2"],

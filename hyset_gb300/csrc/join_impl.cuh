@@ -397,7 +397,9 @@ __device__ __forceinline__ void run_items(const JoinParams& P, ItemLane& it, int
     const uint32_t c = keep ? it.c : 0u, pc = it.pc, jp = it.jp, ip = it.ip, ilp = it.ilp;
     uint32_t lc = 0, mo = 0, cstart = 0, pop = 0;
     count_stat<ST>(P, 0, keep ? 1u : 0u, lane);
-    constexpr bool early_sig = W > 0 && W <= 4;  // as in fgss_batch
+    // as in fgss_batch; with bound-layout entries almost every item here has
+    // passed the positional bound already, so every width loads early
+    constexpr bool early_sig = W > 0 && (W <= 4 || BD);
     if (keep) {
         const uint2 cm = P.R.meta[c];
         if constexpr (early_sig) pop = sig_distance<W>(P.bits_S + (uint64_t)ip * W, P.bits_R + (uint64_t)c * W);
