@@ -14,6 +14,8 @@
 namespace hs {
 
 namespace {
+constexpr float SOLO_MS = 20.0f;  // a join whose kernel is estimated this long runs as a launch of its own
+
 std::string opts_key(const hyset_join_desc& d) {
     std::string k((const char*)&d.indexed, sizeof(d.indexed));
     k.append((const char*)&d.probe, sizeof(d.probe));
@@ -53,19 +55,33 @@ hyset_status batch_record(hyset_ctx* ctx, BatchPlan& bp) {
     cudaStream_t s = ctx->stream;
     const uint32_t n = (uint32_t)bp.joins.size();
     CK(cudaMemsetAsync(bp.counts.p, 0, n * sizeof(unsigned long long), s));
-    CK(cudaMemsetAsync(bp.work.p, 0, 16, s));
+    CK(cudaMemsetAsync(bp.work.p, 0, 16 + 8 * (size_t)n, s));
     for (auto& bjp : bp.joins) {
         BatchJoin& bj = *bjp;
         if (bj.ktech == TECH_FGSS) {
-            ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix));
+            ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix, nullptr, nullptr, -1, bj.solo));
             if (use_bands(bj.b, bj.self))
                 ST(build_sorted_index(ctx, bj.R, bj.b, 2, bj.ix_mid, &bj.b->mid_prefix, bj.b->view.mid_prefix,
-                                      (int)bj.ix.pos_bits));
+                                      (int)bj.ix.pos_bits, bj.solo));
         }
         if (bj.words) {
             CK(generate_bitmaps(bj.R->view(), bj.words, bj.bits_r.as<uint64_t>(), s));
             if (!bj.self) CK(generate_bitmaps(bj.S->view(), bj.words, bj.bits_s.as<uint64_t>(), s));
         }
+    }
+    // the solo joins, heaviest first, each with the single-join kernel over its
+    // own index (token records when its lists fit them), then the shared launch
+    uint32_t q = 0;
+    for (uint32_t k = 0; k < n; ++k) {
+        BatchJoin& bj = *bp.joins[bp.order[k]];
+        if (!bj.solo) continue;
+        JoinParams P = bp.host_desc[k].P;
+        P.X = bj.ix.view();
+        if (use_bands(bj.b, bj.self)) P.X2 = bj.ix_mid.view();
+        P.grab = std::min<uint32_t>(bj.batch, P.X2.set ? 16u : 32u);
+        split_heavy(bj.S, bj.b, P);
+        P.work = bp.work.as<unsigned int>() + 4 + 2 * q++;
+        CK(launch_join(P, TECH_FGSS, bj.vmode, ctx->sm_count, s));
     }
     CK(launch_batch_join(bp.desc.as<BatchDesc>(), bp.unit_off.as<uint32_t>(), n, bp.work.as<unsigned int>(),
                          ctx->sm_count, s));
@@ -118,13 +134,19 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         ST(select_technique(ctx, R, S, o, &selected, &selector));
         Tuned tn = tune(R, S, o, selected);
         tn.probe_major = 1;  // the batched kernel runs the probe-major form
+        float est_ms = 0;  // the autotuner's estimate of the join kernel's time (0: not tuned)
         {
             const uint32_t a_lo = o->probe_end ? o->probe_begin : 0, a_hi = o->probe_end ? o->probe_end : S->n;
             if (o->technique == HYSET_TECH_AUTO && o->bitmap_bits == 0 && tn.tech == HYSET_TECH_FGSS &&
                 a_hi - a_lo >= TUNE_MIN_PROBES)
-                ST(autotune_bits(ctx, R, S, o, bj->b, bj->self, a_lo, a_hi, &tn.bits, nullptr,
-                                 o->fgss_batch ? nullptr : &tn.batch));
+                ST(autotune_bits(ctx, R, S, o, bj->b, bj->self, a_lo, a_hi, &tn.bits,
+                                 o->verify_mode ? nullptr : &tn.vmode, o->fgss_batch ? nullptr : &tn.batch, &est_ms));
         }
+        // a join whose kernel alone takes tens of milliseconds gains nothing from
+        // sharing a launch and loses the single-join kernel's token records and
+        // carried items: it runs as a launch of its own in the batch's graph
+        bj->solo = tn.tech == HYSET_TECH_FGSS && est_ms >= SOLO_MS;
+        bj->vmode = tn.vmode;
         bj->tech = tn.tech;
         bj->ktech = tn.tech == HYSET_TECH_FGSS ? TECH_FGSS : (tn.tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
         bj->words = (int)(tn.bits / 64);
@@ -181,8 +203,9 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         desc[j].words = (uint32_t)bj->words;
         desc[j].unit_probes = bj->ktech == TECH_FGSS ? std::min<uint32_t>(tn.batch, P.X2.set ? 16 : 32) : 1;
         bj->unit_probes = bj->ktech == TECH_FGSS ? desc[j].unit_probes : 0;
+        bj->batch = desc[j].unit_probes;
         const uint32_t np = P.p_hi - P.p_lo;
-        bj->units = (np + desc[j].unit_probes - 1) / desc[j].unit_probes;
+        bj->units = bj->solo ? 0u : (np + desc[j].unit_probes - 1) / desc[j].unit_probes;
         cost[j] = (double)np * (double)(R->n_tokens / std::max<uint32_t>(R->n, 1) + 1) *
                   (bj->ktech == TECH_FGSS ? 1.0 : (double)R->n);
     }
@@ -206,7 +229,7 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
     for (uint32_t j = 0; j < n; ++j) plan->order[j] = j;
     std::stable_sort(plan->order.begin(), plan->order.end(), [&](uint32_t a, uint32_t b) { return cost[a] > cost[b]; });
     CK(plan->counts.ensure(n * sizeof(unsigned long long), s));
-    CK(plan->work.ensure(16, s));
+    CK(plan->work.ensure(16 + 8 * (size_t)n, s));  // the shared launch's counter, then two per solo join
     std::vector<BatchDesc> ordered(n);
     std::vector<uint32_t> unit_off(n + 1, 0);
     for (uint32_t k = 0; k < n; ++k) {
@@ -218,6 +241,7 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
                                 bj.swapped ? 1 : 0};
         unit_off[k + 1] = unit_off[k] + bj.units;
     }
+    plan->host_desc = ordered;
     CK(plan->desc.ensure(n * sizeof(BatchDesc), s));
     CK(plan->unit_off.ensure((n + 1) * 4, s));
     CK(cudaMemcpyAsync(plan->desc.p, ordered.data(), n * sizeof(BatchDesc), cudaMemcpyHostToDevice, s));
@@ -233,10 +257,13 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         if (bj.ktech != TECH_FGSS) continue;
         const uint32_t* index_tab = bj.b->view.index_prefix;
         const uint32_t* mid_tab = bj.b->view.mid_prefix;
-        if (!bj.R->list_path.count(index_tab)) ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix));
-        if (use_bands(bj.b, bj.self) && !bj.R->list_path.count(mid_tab))
+        // a solo join builds here once more, with token records, so that the
+        // records exist before the capture (the capture allocates nothing)
+        if (bj.solo || !bj.R->list_path.count(index_tab))
+            ST(build_sorted_index(ctx, bj.R, bj.b, bj.self ? 0 : 1, bj.ix, nullptr, nullptr, -1, bj.solo));
+        if (use_bands(bj.b, bj.self) && (bj.solo || !bj.R->list_path.count(mid_tab)))
             ST(build_sorted_index(ctx, bj.R, bj.b, 2, bj.ix_mid, &bj.b->mid_prefix, bj.b->view.mid_prefix,
-                                  (int)bj.ix.pos_bits));
+                                  (int)bj.ix.pos_bits, bj.solo));
     }
     // capture the device work once; later calls with the same batch replay it
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));

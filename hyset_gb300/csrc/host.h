@@ -109,9 +109,10 @@ hyset_status plan_split(hyset_ctx* ctx, hyset_coll* R, const hyset_join_opts* o,
                         hyset_technique* low, hyset_technique* high);
 // The autotuner: signature width (always), verification mode (vmode != NULL)
 // and probe batch (batch != NULL) of a prefix-index join from timed samples.
+// est_ms (optional): the join kernel's estimated time in the chosen configuration.
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
                            bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode = nullptr,
-                           uint32_t* batch = nullptr);
+                           uint32_t* batch = nullptr, float* est_ms = nullptr);
 
 // ---- joins (join_host.cu) -----------------------------------------------------
 hyset_status sort_device_pairs(hyset_ctx* ctx, uint2* pairs, uint64_t n, uint32_t n_probe, uint32_t n_indexed);

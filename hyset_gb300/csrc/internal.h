@@ -122,6 +122,12 @@ struct BatchJoin {
     hyset_technique tech = HYSET_TECH_AUTO;
     uint32_t units = 0;
     uint32_t unit_probes = 0;  // probes per work unit of the prefix-index kernel (0: window technique)
+    // a heavy prefix-index join runs as a launch of its own inside the batch's
+    // graph (the single-join kernel: token records, carried items), not in the
+    // shared launch
+    bool solo = false;
+    int vmode = 1;
+    uint32_t batch = 3;
 };
 
 // Scratch of an index build (prefix lengths and offsets, entries, radix sort
@@ -142,6 +148,7 @@ struct BatchPlan {
     std::vector<std::unique_ptr<BatchJoin>> joins;
     std::vector<uint32_t> order;  // joins[order[k]] is descriptor k (heaviest first)
     DevBuf desc, unit_off, counts, work;
+    std::vector<BatchDesc> host_desc;  // the joins' descriptors in launch order (solo joins launch from them)
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -181,6 +188,7 @@ struct hyset_ctx {
         uint32_t bits = 0;   // signature width
         int vmode = 0;       // verification mode (0: not tuned)
         uint32_t batch = 0;  // probes per warp batch of the probe-major kernel (0: not tuned)
+        float est_ms = 0;    // the join kernel's estimated time in this configuration
     };
     std::map<std::string, TuneChoice> tune_cache;  // the autotuner's choices per join
     std::map<std::string, uint32_t> universe_cache;  // universe by collection size profile (host-input joins)

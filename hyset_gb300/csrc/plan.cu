@@ -304,13 +304,15 @@ constexpr float TUNE_BATCH_FULL_MS = 40.0f;  // batches are timed over the whole
 // the batch, so a larger batch keeps more loads in flight per warp but
 // balances worse across warps).
 hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_join_opts* o, Bounds* b,
-                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode, uint32_t* batch) {
+                           bool self, uint32_t p_lo, uint32_t p_hi, uint32_t* bits, int* vmode, uint32_t* batch,
+                           float* est_ms) {
     const std::string key = join_key(R, S, o);
     auto it = ctx->tune_cache.find(key);
     if (it != ctx->tune_cache.end() && (!vmode || it->second.vmode) && (!batch || it->second.batch)) {
         *bits = it->second.bits;
         if (vmode) *vmode = it->second.vmode;
         if (batch) *batch = it->second.batch;
+        if (est_ms) *est_ms = it->second.est_ms;
         return HYSET_OK;
     }
     cudaStream_t s = ctx->stream;
@@ -481,6 +483,7 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
                     tb_ms = ms;
                 }
             }
+            cur_ms = tb_ms;  // a whole-range run: the estimate becomes a measurement
         }
         P.grab = base_batch;
         *batch = tb;
@@ -489,7 +492,9 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     ch.bits = best;
     if (vmode) ch.vmode = vm;
     if (batch) ch.batch = tb;
+    ch.est_ms = cur_ms;
     *bits = best;
+    if (est_ms) *est_ms = cur_ms;
     return HYSET_OK;
 }
 
