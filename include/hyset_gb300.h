@@ -171,8 +171,12 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
                                   hyset_coll** coll_out, hyset_result** out);
 
 /* Many independent joins in one persistent, work-stealing launch (the
- * device-resident form of src/queue.cu:142-281's block-pair queue).
- * probe == NULL (or probe == indexed) means a self-join. */
+ * device-resident form of src/queue.cu:142-281's block-pair queue), the whole
+ * sequence (index builds, signatures, launches) captured in a CUDA graph and
+ * replayed when the same batch comes again.  An AUTO prefix-filter join the
+ * autotuner estimates at 20 ms of kernel time or more runs as a launch of its
+ * own inside the same graph (the single-join kernel: sharing a launch saves it
+ * nothing).  probe == NULL (or probe == indexed) means a self-join. */
 typedef struct {
     const hyset_coll* indexed;
     const hyset_coll* probe;
