@@ -144,13 +144,16 @@ hyset_status batch_prepare(hyset_ctx* ctx, const hyset_join_desc* joins, uint32_
         }
         // a join whose kernel alone takes tens of milliseconds gains nothing from
         // sharing a launch and loses the single-join kernel's token records and
-        // carried items: it runs as a launch of its own in the batch's graph
-        bj->solo = tn.tech == HYSET_TECH_FGSS && est_ms >= SOLO_MS;
+        // carried items: it runs as a launch of its own in the batch's graph; so
+        // does one tuned to 1024-bit signatures, which the shared launch lacks
+        // (their code would cost it registers)
+        bj->solo = tn.tech == HYSET_TECH_FGSS && (est_ms >= SOLO_MS || tn.bits > 512);
         bj->vmode = tn.vmode;
         bj->tech = tn.tech;
         bj->ktech = tn.tech == HYSET_TECH_FGSS ? TECH_FGSS : (tn.tech == HYSET_TECH_DIRECT ? TECH_DIRECT : TECH_BITMAP);
         bj->words = (int)(tn.bits / 64);
         if (bj->ktech == TECH_DIRECT) bj->words = 0;
+        if (bj->words > 8 && !bj->solo) bj->words = 8;  // explicit 1024 bits on a window technique
         JoinParams& P = desc[j].P;
         P = JoinParams{};
         P.R = R->view();

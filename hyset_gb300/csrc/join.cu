@@ -170,6 +170,9 @@ cudaError_t dispatch_words_bd(const JoinParams& P, int sm_count, cudaStream_t s)
     case 2: return launch_persistent(k_join<TECH, VMODE, 2, ST, BD>, sm_count, s, P);
     case 4: return launch_persistent(k_join<TECH, VMODE, 4, ST, BD>, sm_count, s, P);
     case 8: return launch_persistent(k_join<TECH, VMODE, 8, ST, BD>, sm_count, s, P);
+    case 16:  // 1024-bit signatures: the prefix filter only
+        if constexpr (TECH == TECH_FGSS) return launch_persistent(k_join<TECH, VMODE, 16, ST, BD>, sm_count, s, P);
+        return cudaErrorInvalidValue;
     default: return cudaErrorInvalidValue;
     }
 }

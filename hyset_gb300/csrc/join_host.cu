@@ -184,7 +184,7 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     }
     const int vmode = tn.vmode;
     res->verify_mode = (uint32_t)vmode;
-    res->bitmap_bits = tech == HYSET_TECH_DIRECT ? 0 : tn.bits;
+    res->bitmap_bits = tech == HYSET_TECH_DIRECT ? 0 : (tn.bits > 512 && !(tech == HYSET_TECH_FGSS && tn.probe_major) ? 512 : tn.bits);
     if (o->probe_end > S->n || o->probe_begin > o->probe_end)
         return fail(ctx, HYSET_E_INVALID, "probe range outside the probe collection");
     const unsigned long long launches0 = launches();
@@ -231,7 +231,9 @@ hyset_status do_join(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const hyset_j
     }
     // signatures do not depend on the index: they are generated on the
     // auxiliary stream while the index builds on the context's stream
-    const int words = (int)(tn.bits / 64);
+    // 1024-bit signatures serve the probe-major prefix filter; the window
+    // techniques and the token-major kernel take 512 at most
+    const int words = (int)(tn.bits / 64) > 8 && !(tech == HYSET_TECH_FGSS && tn.probe_major) ? 8 : (int)(tn.bits / 64);
     if (words) {
         const uint64_t *br = nullptr, *bs = nullptr;
         ST(get_bitmaps(ctx, R, words, &br, ctx->aux));

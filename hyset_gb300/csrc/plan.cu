@@ -21,8 +21,8 @@ hyset_status check_opts(hyset_ctx* ctx, const hyset_join_opts* o) {
     if (o->technique < HYSET_TECH_AUTO || o->technique > HYSET_TECH_DIRECT)
         return fail(ctx, HYSET_E_INVALID, "unknown technique");
     if (o->bitmap_bits != 0 && o->bitmap_bits != 64 && o->bitmap_bits != 128 && o->bitmap_bits != 256 &&
-        o->bitmap_bits != 512)
-        return fail(ctx, HYSET_E_INVALID, "bitmap_bits must be 0, 64, 128, 256 or 512");
+        o->bitmap_bits != 512 && o->bitmap_bits != 1024)
+        return fail(ctx, HYSET_E_INVALID, "bitmap_bits must be 0, 64, 128, 256, 512 or 1024");
     if (o->verify_mode > 3) return fail(ctx, HYSET_E_INVALID, "verify_mode must be 0, 1, 2 or 3");
     if (o->orientation > 2) return fail(ctx, HYSET_E_INVALID, "orientation must be 0, 1 or 2");
     return HYSET_OK;
@@ -334,8 +334,8 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
     CK(ctx->s_work.ensure(16, s));
     P.out = Sink{nullptr, ctx->s_count.as<unsigned long long>(), 0, 1};
     P.work = ctx->s_work.as<unsigned int>();
-    const uint32_t cand[4] = {0, 128, 256, 512};
-    float est[4] = {0, 0, 0, 0}, kern_est[4] = {0, 0, 0, 0};
+    const uint32_t cand[5] = {0, 128, 256, 512, 1024};
+    float est[5] = {0, 0, 0, 0, 0}, kern_est[5] = {0, 0, 0, 0, 0};
     float best_ms = 0;
     uint32_t best = 256;
     const bool learned = ctx->has_width_mlp;  // the width network replaces the width samples
@@ -391,11 +391,13 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
             if (y[k] < y[w]) w = k;
         best = 128u << w;  // outputs: 128, 256, 512 bits
     }
-    for (int k = learned ? 4 : 0; k < 4; ++k) {
+    // the estimated time of width cand[k]: its signature generation (paid once
+    // per join) plus the whole probe range's kernel time from the samples
+    auto time_width = [&](int k) -> hyset_status {
         const int words = (int)(cand[k] / 64);
         P.words = words;
         P.bits_R = P.bits_S = nullptr;
-        float gen_ms = 0;  // the width's signature generation, paid once per join
+        float gen_ms = 0;
         if (words) {
             const uint64_t *br = nullptr, *bs = nullptr;
             CK(cudaEventRecord(ctx->ek0, s));
@@ -408,25 +410,30 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
             P.bits_R = br;
             P.bits_S = bs;
         }
-        float total = 0;
-        ST(sample(1, &total));
-        kern_est[k] = total;
-        total += gen_ms;  // the whole probe range's estimated kernel time plus the generation
-        est[k] = total;
-        if (k == 0 || total < best_ms) {
-            best_ms = total;
-            best = cand[k];
-        }
-    }
-    const int kb = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
+        ST(sample(1, &kern_est[k]));
+        est[k] = kern_est[k] + gen_ms;
+        return HYSET_OK;
+    };
     if (!learned) {
+        for (int k = 0; k < 5; ++k) {
+            ST(time_width(k));
+            if (k == 0 || est[k] < best_ms) {
+                best_ms = est[k];
+                best = cand[k];
+            }
+        }
         // the rule's width (mean size <= 48: 128 bits, else 256) unless another is clearly faster
         const uint32_t rule = (double)R->n_tokens / (double)std::max<uint32_t>(R->n, 1) <= 48.0 ? 128u : 256u;
         const float rule_ms = est[rule == 128u ? 1 : 2];
         if (best != rule && best_ms > TUNE_MARGIN * rule_ms) best = rule;
+    } else if (best == 512) {
+        // the network's widest output: 1024 bits (long sets at low thresholds,
+        // where 512-bit signatures pass most candidates) when clearly faster
+        ST(time_width(3));
+        ST(time_width(4));
+        if (est[4] < TUNE_MARGIN * est[3]) best = 1024;
     }
-    const int kc = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : 3;
-    (void)kb;
+    const int kc = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : best == 512 ? 3 : 4;
     float cur_ms = kern_est[kc];  // the chosen configuration's estimated kernel time
     // verification: a lane per surviving item, or the warp per item when the
     // samples show it faster at the chosen width (long merges: low thresholds,

@@ -1165,6 +1165,7 @@ cudaError_t validate_with_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags
     case 2: k_validate_bitmaps<2><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
     case 4: k_validate_bitmaps<4><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
     case 8: k_validate_bitmaps<8><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 16: k_validate_bitmaps<16><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
@@ -1180,6 +1181,7 @@ cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t 
     case 2: k_bitmaps<2><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
     case 4: k_bitmaps<4><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
     case 8: k_bitmaps<8><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
+    case 16: k_bitmaps<16><<<g, BITMAP_THREADS, 0, s>>>(c, out); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

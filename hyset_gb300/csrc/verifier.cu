@@ -288,7 +288,7 @@ hyset_status hyset_verify_device(hyset_ctx* ctx, const hyset_coll* indexed, cons
     int words = 0;
     if (opts->technique != HYSET_TECH_DIRECT && opts->technique != HYSET_TECH_FGSS) {
         const double avg = R->n ? (double)R->n_tokens / (double)R->n : 0.0;
-        words = opts->bitmap_bits ? (int)(opts->bitmap_bits / 64) : (avg <= 48.0 ? 2 : 4);
+        words = opts->bitmap_bits ? std::min(8, (int)(opts->bitmap_bits / 64)) : (avg <= 48.0 ? 2 : 4);  // 512 bits at most
     }
     CK(cudaEventRecord(ctx->ev0, s));
     const uint64_t *sig_r = nullptr, *sig_s = nullptr;

@@ -66,7 +66,9 @@ typedef struct {
     hyset_sim sim;
     double threshold;          /* in (0, 1] */
     hyset_technique technique;
-    uint32_t bitmap_bits;      /* 64, 128, 256 or 512; 0 = chosen by the library with technique
+    uint32_t bitmap_bits;      /* 64, 128, 256, 512 or 1024 (the probe-major prefix filter only; the
+                                  window techniques, the token-major kernel and the candidate
+                                  verifier use 512 for it); 0 = chosen by the library with technique
                                   AUTO (timed samples for joins of 60,000 probes or more, else
                                   128 bits for mean set sizes <= 48 and 256 above), no signature
                                   filter with an explicit technique */

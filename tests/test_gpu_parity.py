@@ -21,6 +21,7 @@ TECHS = [
     dict(technique="bitmap", bitmap=64, verify_mode=1),
     dict(technique="bitmap", bitmap=256, verify_mode=2),
     dict(technique="bitmap", bitmap=512, verify_mode=1),
+    dict(technique="fgss", probe_major=True, bitmap=1024, verify_mode=1),  # 1024-bit signatures
     dict(technique="direct", verify_mode=1),
 ]
 TECH_IDS = ["-".join(f"{k}{v}" for k, v in t.items()) for t in TECHS]
@@ -62,6 +63,7 @@ def test_self_join_matches_oracle_on_workloads(ctx, label, spec, kw, taus, sim):
         for kw in (dict(technique="fgss"), dict(technique="fgss", bitmap=128),
                    dict(technique="fgss", probe_major=True, verify_mode=2),
                    dict(technique="fgss", probe_major=True, bitmap=128, verify_mode=1),
+                   dict(technique="fgss", probe_major=True, bitmap=1024, verify_mode=1),
                    dict(technique="bitmap", bitmap=256, verify_mode=2)):
             r = ctx.self_join(coll, threshold=tau, sim=sim, **kw)
             assert as_set_checked(r.pairs) == exp, (label, sim, tau, kw)
@@ -85,7 +87,7 @@ def test_rs_join_matches_brute_force(ctx, sim):
         assert len(exp) > 0
         for kw in (dict(technique="fgss"), dict(technique="fgss", bitmap=64),
                    dict(technique="fgss", probe_major=True), dict(technique="bitmap", bitmap=128),
-                   dict(technique="direct")):
+                   dict(technique="fgss", probe_major=True, bitmap=1024), dict(technique="direct")):
             r = ctx.rs_join(cr, cs, threshold=tau, sim=sim, **kw)
             assert as_set_checked(r.pairs) == exp, (sim, tau, kw)
 
@@ -251,7 +253,7 @@ def test_autotuned_join_keeps_the_pairs(ctx, tau):
     coll = ctx.upload(c.tokens, c.sizes, c.starts)
     r1 = ctx.self_join(coll, threshold=tau)
     r2 = ctx.self_join(coll, threshold=tau)
-    assert r1.bitmap_bits in (0, 128, 256, 512) and r1.verify_mode in (1, 2), (r1.bitmap_bits, r1.verify_mode)
+    assert r1.bitmap_bits in (0, 128, 256, 512, 1024) and r1.verify_mode in (1, 2), (r1.bitmap_bits, r1.verify_mode)
     assert (r2.bitmap_bits, r2.verify_mode) == (r1.bitmap_bits, r1.verify_mode)
     assert as_set_checked(r1.pairs) == exp and as_set_checked(r2.pairs) == exp
     r3 = ctx.self_join_host(c.tokens, c.sizes, c.starts, threshold=tau)

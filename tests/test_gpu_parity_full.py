@@ -73,6 +73,7 @@ def test_c3_full_size_matches_oracle(ctx, c3, sim):
     coll = ctx.upload(c3.tokens, c3.sizes, c3.starts)
     for kw in (dict(technique="auto"), dict(technique="fgss", probe_major=True, verify_mode=2),
                dict(technique="fgss", probe_major=True, bitmap=512, verify_mode=1),
+               dict(technique="fgss", probe_major=True, bitmap=1024, verify_mode=1),
                dict(technique="fgss", probe_major=True, verify_mode=1, sort_pairs=True)):
         r = ctx.self_join(coll, threshold=0.8, sim=sim, **kw)
         assert r.count == exp.size, (sim, kw)
