@@ -433,6 +433,35 @@ hyset_status autotune_bits(hyset_ctx* ctx, hyset_coll* R, hyset_coll* S, const h
         ST(time_width(4));
         if (est[4] < TUNE_MARGIN * est[3]) best = 1024;
     }
+    if (best >= 512 && std::max(kern_est[3], kern_est[4]) > 0 &&
+        std::max(kern_est[3], kern_est[4]) <= TUNE_BATCH_FULL_MS) {
+        // 512 against 1024 bits again over the whole probe range when that is
+        // cheap: the samples weigh the heaviest probes (the largest sets, where
+        // the wider signature pays) like the light ones and can misjudge it
+        auto whole_at = [&](uint32_t width, float* out) -> hyset_status {
+            ST(use_width(width));
+            P.p_lo = p_lo;
+            P.p_hi = p_hi;
+            float ms = 0;
+            for (int rep = 0; rep < 2; ++rep) {  // the first run warms the caches
+                CK(cudaMemsetAsync(ctx->s_count.p, 0, 16, s));
+                CK(cudaMemsetAsync(ctx->s_work.p, 0, 16, s));
+                CK(cudaEventRecord(ctx->ek0, s));
+                CK(launch_join(P, TECH_FGSS, 1, ctx->sm_count, s));
+                CK(cudaEventRecord(ctx->ek1, s));
+                CK(cudaEventSynchronize(ctx->ek1));
+                CK(cudaEventElapsedTime(&ms, ctx->ek0, ctx->ek1));
+            }
+            *out = ms;
+            return HYSET_OK;
+        };
+        float ms512 = 0, ms1024 = 0;
+        ST(whole_at(512, &ms512));
+        ST(whole_at(1024, &ms1024));
+        best = ms1024 < TUNE_MARGIN * ms512 ? 1024u : 512u;
+        kern_est[3] = ms512;
+        kern_est[4] = ms1024;
+    }
     const int kc = best == 0 ? 0 : best == 128 ? 1 : best == 256 ? 2 : best == 512 ? 3 : 4;
     float cur_ms = kern_est[kc];  // the chosen configuration's estimated kernel time
     // verification: a lane per surviving item, or the warp per item when the
