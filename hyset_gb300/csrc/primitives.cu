@@ -294,10 +294,10 @@ __global__ void k_emit_entries(CollView c, uint32_t lo, uint32_t hi, const uint3
 // indexed by set size and off is not read.
 constexpr int EMIT_ROUNDS = 8;
 #ifndef HS_REC_EMIT_ROUNDS
-#define HS_REC_EMIT_ROUNDS 8  // rounds of slot atomics in flight per lane (record emit)
+#define HS_REC_EMIT_ROUNDS 4  // rounds of slot atomics in flight per lane (record emit)
 #endif
 #ifndef HS_REC_EMIT_MINB
-#define HS_REC_EMIT_MINB 1  // resident blocks per SM the record emit is compiled for
+#define HS_REC_EMIT_MINB 6  // resident blocks per SM the record emit is compiled for
 #endif
 template <bool REC>
 __global__ void __launch_bounds__(256, REC ? HS_REC_EMIT_MINB : 1) k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
