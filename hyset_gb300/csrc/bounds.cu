@@ -104,6 +104,40 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
                     b->mo_tab[b->mo_row[big - 1] + (small - b->minsize[big - 1])] > v)
                     b->mo_monotone = false;
             }
+        if (b->mo_monotone) {
+            // bound fields: for each size l and position p of its maxprefix, the
+            // largest probe length lp whose minoverlap with l leaves l - p enough
+            // (monotone in lp; lengths incompatible with l count as admitted
+            // below l and refused above it: no window pairs them)
+            auto admits = [&](uint32_t lp, uint32_t l, uint32_t v) -> bool {
+                const uint32_t big = std::max(lp, l), small = std::min(lp, l);
+                if (small < b->minsize[big]) return lp < l;
+                const uint32_t raw = b->mo_tab[b->mo_row[big] + (small - b->minsize[big])];
+                return v >= std::min(small, std::min(big, raw));
+            };
+            uint64_t total = 0;
+            b->lp_row.assign((size_t)L + 2, 0);
+            for (uint32_t l = 0; l <= L; ++l) {
+                b->lp_row[l] = (uint32_t)total;
+                total += b->probe_prefix[l];
+            }
+            b->lp_row[L + 1] = (uint32_t)total;
+            if (total <= MAX_COSINE_TABLE) {
+                b->lp_tab.resize(total ? total : 1);
+                for (uint32_t l = 1; l <= L; ++l)
+                    for (uint32_t p = 0; p < b->probe_prefix[l]; ++p) {
+                        uint32_t lo = 0, hi = L + 1;  // admits(lo), not admits(hi)
+                        while (hi - lo > 1) {
+                            const uint32_t mid = lo + (hi - lo) / 2;
+                            if (admits(mid, l, l - p)) lo = mid;
+                            else hi = mid;
+                        }
+                        b->lp_tab[b->lp_row[l] + p] = lo;
+                    }
+            } else {
+                b->lp_row.clear();
+            }
+        }
     } else {
         b->mo_sum.resize(2 * (size_t)L + 1);
         for (uint32_t s = 0; s <= 2 * L; ++s) b->mo_sum[s] = sim_minoverlap(sim, s, 0, tau);
@@ -122,7 +156,8 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
         }
     }
     // one device allocation holding all tables
-    size_t n32 = 5 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size() + b->max_sum.size();
+    size_t n32 = 5 * ((size_t)L + 1) + b->mo_sum.size() + b->mo_tab.size() + b->max_sum.size() + b->lp_row.size() +
+                 b->lp_tab.size();
     size_t bytes = b->mo_row.size() * 8 + n32 * 4;
     CK(b->dev.ensure(bytes, ctx->stream));
     uint8_t* base = b->dev.as<uint8_t>();
@@ -134,7 +169,8 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
         dst = d;
         return cudaMemcpyAsync(d, v.data(), v.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
     };
-    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_mid, *d_sum, *d_tab, *d_msum = nullptr;
+    uint32_t *d_minsize, *d_pp, *d_ip, *d_mp, *d_mid, *d_sum, *d_tab, *d_msum = nullptr, *d_lprow = nullptr,
+             *d_lptab = nullptr;
     CK(cudaMemcpyAsync(d_row, b->mo_row.data(), b->mo_row.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(put(b->minsize, d_minsize));
     CK(put(b->probe_prefix, d_pp));
@@ -144,8 +180,12 @@ hyset_status get_bounds(hyset_ctx* ctx, int sim, double tau, uint32_t L, int ind
     CK(put(b->mo_sum, d_sum));
     CK(put(b->mo_tab, d_tab));
     if (!b->max_sum.empty()) CK(put(b->max_sum, d_msum));
+    if (!b->lp_row.empty()) {
+        CK(put(b->lp_row, d_lprow));
+        CK(put(b->lp_tab, d_lptab));
+    }
     CK(cudaStreamSynchronize(ctx->stream));
-    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_mid, d_sum, d_row, d_tab, L, sim, d_msum};
+    b->view = BoundsView{d_minsize, d_pp, d_ip, d_mp, d_mid, d_sum, d_row, d_tab, L, sim, d_msum, d_lprow, d_lptab};
     *out = b.get();
     ctx->bounds.emplace(key, std::move(b));
     return HYSET_OK;

@@ -41,6 +41,9 @@ struct BoundsView {
     // [L+1] jaccard, dice: the largest l1 + l2 whose raw minoverlap is at most
     // v (nullptr for cosine or a table that is not monotone)
     const uint32_t* __restrict__ max_sum = nullptr;
+    // cosine: bound fields by (size, position), rows lp_row[l] (see Bounds)
+    const uint32_t* __restrict__ lp_row = nullptr;
+    const uint32_t* __restrict__ lp_tab = nullptr;
 };
 
 // Copy chunks of a host-input join (in tokens): 64 MB while more than three
@@ -69,6 +72,18 @@ __device__ __forceinline__ uint32_t bound_field(const uint32_t* __restrict__ max
     if (pos == 0) return maxf;
     const uint32_t s = max_sum[len - pos];
     return s <= len ? 0u : min(maxf, s - len);
+}
+// The tables a bound-layout index build reads (all null: positions).
+struct BoundFields {
+    const uint32_t* __restrict__ max_sum;  // jaccard, dice
+    const uint32_t* __restrict__ lp_row;   // cosine
+    const uint32_t* __restrict__ lp_tab;
+    __host__ __device__ bool on() const { return max_sum || lp_tab; }
+};
+// The field from either table (any similarity with monotone minoverlap).
+__device__ __forceinline__ uint32_t bound_field_of(const BoundFields& F, uint32_t len, uint32_t pos, uint32_t maxf) {
+    if (F.max_sum) return bound_field(F.max_sum, len, pos, maxf);
+    return min(maxf, F.lp_tab[F.lp_row[len] + pos]);
 }
 
 // generic_similarity::minoverlap (similarity.hpp:21-23): min(l2, min(l1, raw)).

@@ -69,9 +69,13 @@ uint64_t prefix_entries(const hyset_coll* c, const std::vector<uint32_t>& pre);
 uint32_t bits_for(uint64_t v);
 // The entry layout of an index's token records: the low rec_bits hold the
 // longest probe the entry's positional bound admits (*bound: a self-join's
-// midprefix index, kind 0, under jaccard or dice, when set ids and that field
-// fit 32 bits) or the entry's position (rec_bits = pb, the lists' layout).
+// midprefix index, kind 0, with a monotone minoverlap table, when set ids and
+// that field fit 32 bits) or the entry's position (rec_bits = pb, the lists'
+// layout).
 void record_layout(const hyset_coll* c, const Bounds* b, int kind, uint32_t pb, uint32_t* rec_bits, bool* bound);
+// The tables a bound-layout record build reads (jaccard, dice: max_sum;
+// cosine: lp_row / lp_tab).
+BoundFields bound_fields(const Bounds* b);
 // The first set id whose prefix (pre[size] tokens) is long enough to be
 // emitted a warp per set (0xFFFFFFFF: none).
 uint32_t first_long_prefix(const hyset_coll* c, const std::vector<uint32_t>& pre);

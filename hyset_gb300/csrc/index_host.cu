@@ -76,7 +76,10 @@ uint64_t prefix_entries(const hyset_coll* c, const std::vector<uint32_t>& pre) {
     return E;
 }
 
-// Bits needed to represent v (at least 1).
+BoundFields bound_fields(const Bounds* b) {
+    return BoundFields{b->view.max_sum, b->view.lp_row, b->view.lp_tab};
+}
+
 uint32_t first_long_prefix(const hyset_coll* c, const std::vector<uint32_t>& pre) {
     constexpr uint32_t LONG_PREFIX = 32;  // longer prefixes are emitted a warp per set
     uint64_t id = 0;
@@ -89,10 +92,11 @@ uint32_t first_long_prefix(const hyset_coll* c, const std::vector<uint32_t>& pre
 
 void record_layout(const hyset_coll* c, const Bounds* b, int kind, uint32_t pb, uint32_t* rec_bits, bool* bound) {
     const uint32_t fb = bits_for(b->L);  // a field that holds every probe length
-    *bound = kind == 0 && b->view.max_sum != nullptr && fb + bits_for(c->n) <= 32;
+    *bound = kind == 0 && (b->view.max_sum != nullptr || b->view.lp_tab != nullptr) && fb + bits_for(c->n) <= 32;
     *rec_bits = *bound ? fb : pb;
 }
 
+// Bits needed to represent v (at least 1).
 uint32_t bits_for(uint64_t v) {
     uint32_t b = 1;
     while (b < 64 && (v >> b)) ++b;
@@ -179,7 +183,7 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
             CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
             CK(cudaMemsetAsync(counts, 0, (size_t)U * 4, s));
             CK(emit_records(v, d_pre, ix.rec_bits, counts, ix.rec.as<uint32_t>(), U, s, 0, 0xFFFFFFFFu,
-                            ix.rec_bound ? b->view.max_sum : nullptr, first_long_prefix(c, *pre)));
+                            ix.rec_bound ? bound_fields(b) : BoundFields{}, first_long_prefix(c, *pre)));
             CK(order_records(counts, U, ix.rec.as<uint32_t>(), s));
             ix.records = true;
             ix.pos_bits = pb;
@@ -210,7 +214,7 @@ hyset_status build_sorted_index(hyset_ctx* ctx, hyset_coll* c, const Bounds* b, 
             record_layout(c, b, kind, pb, &ix.rec_bits, &ix.rec_bound);
             CK(ix.rec.ensure((size_t)U * REC_CAP * 4, s));
             CK(records_from_lists(ix.list_off.as<uint32_t>(), ix.set.as<uint32_t>(), U, ix.rec.as<uint32_t>(), s,
-                                  ix.rec_bound ? b->view.max_sum : nullptr, c->d_sizes, pb, ix.rec_bits));
+                                  ix.rec_bound ? bound_fields(b) : BoundFields{}, c->d_sizes, pb, ix.rec_bits));
             ix.records = true;
         }
         return HYSET_OK;

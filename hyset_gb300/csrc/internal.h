@@ -63,6 +63,10 @@ struct Bounds {
     uint32_t L = 0;
     int index_maxprefix = 0;  // 0: index midprefix (self-join), 1: maxprefix (R-S)
     std::vector<uint32_t> minsize, probe_prefix, index_prefix, max_partner, mid_prefix, mo_sum, mo_tab, max_sum;
+    // cosine (monotone tables): for a set of size l and position p < maxprefix(l),
+    // lp_tab[lp_row[l] + p] = the longest probe the entry's side of the
+    // positional bound admits (the bound layout of token records)
+    std::vector<uint32_t> lp_row, lp_tab;
     bool mo_monotone = false;  // minoverlap non-decreasing in each length (R-S bands are valid)
     std::vector<uint64_t> mo_row;
     DevBuf dev;

@@ -123,11 +123,11 @@ constexpr uint64_t REC_MAX_TOKENS = 1ull << 25;  // records of larger universes 
 // become entries (set << pos_bits) | position, each taking slot
 // atomicAdd(&counts[token], 1) of its token's record (tokens below `limit`;
 // counts zeroed by the caller).  The slots follow no order.
-// max_sum (optional, a self-join's midprefix index under jaccard or dice):
-// the low pos_bits of each entry hold bound_field instead of the position.
+// bf (optional, a self-join's midprefix index): the low pos_bits of each entry
+// hold its bound field (bound_field_of) instead of the position.
 cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
                          uint32_t limit, cudaStream_t s, uint32_t lo = 0, uint32_t hi = 0xFFFFFFFFu,
-                         const uint32_t* max_sum = nullptr, uint32_t big_lo = 0xFFFFFFFFu);
+                         BoundFields bf = BoundFields{}, uint32_t big_lo = 0xFFFFFFFFu);
 // Pass 2: each record's min(counts[t], REC_ENTRIES) entries in ascending
 // order after its length word, padded with 0xFFFFFFFF.  overflow (optional):
 // OR-ed with REC_OVERFLOW when a token had more entries than a record holds
@@ -143,10 +143,10 @@ constexpr uint32_t REC_OVERFLOW = 16;
 cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s,
                           uint32_t* overflow = nullptr, uint32_t* prev = nullptr);
 // Records from index lists already built (every list at most REC_ENTRIES long).
-// max_sum (optional): entries (set << list_bits) | position become
-// (set << rec_bits) | bound_field (sizes: the indexed sets' sizes).
+// bf (optional): entries (set << list_bits) | position become
+// (set << rec_bits) | bound field (sizes: the indexed sets' sizes).
 cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
-                               cudaStream_t s, const uint32_t* max_sum = nullptr, const uint32_t* sizes = nullptr,
+                               cudaStream_t s, BoundFields bf = BoundFields{}, const uint32_t* sizes = nullptr,
                                uint32_t list_bits = 0, uint32_t rec_bits = 0);
 
 // Token histogram of n entries into counts[limit] (warp-aggregated atomics;

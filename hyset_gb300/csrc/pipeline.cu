@@ -488,7 +488,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
                 CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
             if (records)
                 CK(emit_records(v, b->view.index_prefix, ix.rec_bits, counts, ix.rec.as<uint32_t>(), U, s, lo, hi,
-                                ix.rec_bound ? b->view.max_sum : nullptr, big_lo));
+                                ix.rec_bound ? bound_fields(b) : BoundFields{}, big_lo));
             else
                 CK(emit_packed_entries(v, off, len, pb, ctx->sc->tok.as<uint32_t>(), ix.set.as<uint32_t>(), counts, s,
                                        lo, hi, U + 1, big_lo));

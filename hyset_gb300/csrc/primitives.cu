@@ -303,7 +303,7 @@ template <bool REC>
 __global__ void __launch_bounds__(256, REC ? HS_REC_EMIT_MINB : 1) k_emit_packed(CollView c, uint32_t lo, const uint32_t* __restrict__ off,
                               const uint32_t* __restrict__ len, uint32_t pos_bits, uint32_t* __restrict__ e_token,
                               uint32_t* __restrict__ e_val, uint32_t* __restrict__ counts, uint32_t limit,
-                              const uint32_t* __restrict__ max_sum, uint32_t spw) {
+                              BoundFields bf, uint32_t spw) {
     constexpr int ROUNDS = REC ? HS_REC_EMIT_ROUNDS : EMIT_ROUNDS;
     const uint32_t maxf = (1u << pos_bits) - 1u;
     const int lane = threadIdx.x & 31;
@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(256, REC ? HS_REC_EMIT_MINB : 1) k_emit_packed
                 uint32_t low = i;
                 if constexpr (REC) {
                     const uint32_t size_k = __shfl_sync(FULL, size, k);
-                    if (max_sum && j < total) low = bound_field(max_sum, size_k, i, maxf);
+                    if (bf.on() && j < total) low = bound_field_of(bf, size_k, i, maxf);
                 }
                 val[u] = ((s0 + (uint32_t)k) << pos_bits) | low;
             }
@@ -582,16 +582,16 @@ __global__ void __launch_bounds__(REC_THREADS) k_order_records(const uint32_t* _
 // Records from built lists: a warp per token, lane 0 writes the length, lane
 // i > 0 entry i - 1 or the pad.
 __global__ void k_records_from_lists(const uint32_t* __restrict__ list_off, const uint32_t* __restrict__ vals,
-                                     uint32_t U, uint32_t* __restrict__ rec, const uint32_t* __restrict__ max_sum,
+                                     uint32_t U, uint32_t* __restrict__ rec, BoundFields bf,
                                      const uint32_t* __restrict__ sizes, uint32_t list_bits, uint32_t rec_bits) {
     const int lane = threadIdx.x & 31;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < U; t += warps) {
         const uint32_t a = list_off[t], b = list_off[t + 1];
         uint32_t w = lane == 0 ? b - a : (a + lane - 1 < b ? vals[a + lane - 1] : 0xFFFFFFFFu);
-        if (max_sum && lane > 0 && a + lane - 1 < b) {  // (set, position) -> (set, bound field)
+        if (bf.on() && lane > 0 && a + lane - 1 < b) {  // (set, position) -> (set, bound field)
             const uint32_t set = w >> list_bits, pos = w & ((1u << list_bits) - 1u);
-            w = (set << rec_bits) | bound_field(max_sum, sizes[set], pos, (1u << rec_bits) - 1u);
+            w = (set << rec_bits) | bound_field_of(bf, sizes[set], pos, (1u << rec_bits) - 1u);
         }
         rec[t * REC_CAP + lane] = w;
     }
@@ -987,7 +987,7 @@ namespace {
 template <bool REC>
 cudaError_t launch_emit(CollView c, uint32_t lo, uint32_t hi, uint32_t big_lo, const uint32_t* off,
                         const uint32_t* len, uint32_t pos_bits, uint32_t* e_token, uint32_t* e_val, uint32_t* counts,
-                        uint32_t limit, const uint32_t* max_sum, cudaStream_t s) {
+                        uint32_t limit, BoundFields bf, cudaStream_t s) {
     if (hi == 0xFFFFFFFFu) hi = c.n;
     const uint32_t mid = std::min(std::max(lo, big_lo), hi);
     CollView v = c;
@@ -995,14 +995,14 @@ cudaError_t launch_emit(CollView c, uint32_t lo, uint32_t hi, uint32_t big_lo, c
         note_launches();
         v.n = mid;  // the kernel walks ids [lo, mid)
         k_emit_packed<REC><<<grid_for((uint64_t)(mid - lo), 256), 256, 0, s>>>(v, lo, off, len, pos_bits, e_token,
-                                                                             e_val, counts, limit, max_sum, 32u);
+                                                                             e_val, counts, limit, bf, 32u);
     }
     if (hi > mid) {
         note_launches();
         v.n = hi;
         k_emit_packed<REC><<<grid_for((uint64_t)(hi - mid) * 32u, 256), 256, 0, s>>>(v, mid, off, len, pos_bits,
                                                                                    e_token, e_val, counts, limit,
-                                                                                   max_sum, 1u);
+                                                                                   bf, 1u);
     }
     return cudaGetLastError();
 }
@@ -1011,13 +1011,14 @@ cudaError_t launch_emit(CollView c, uint32_t lo, uint32_t hi, uint32_t big_lo, c
 cudaError_t emit_packed_entries(CollView c, const uint32_t* entry_off, const uint32_t* len, uint32_t pos_bits,
                                 uint32_t* e_token, uint32_t* e_val, uint32_t* counts, cudaStream_t s, uint32_t lo,
                                 uint32_t hi, uint32_t limit, uint32_t big_lo) {
-    return launch_emit<false>(c, lo, hi, big_lo, entry_off, len, pos_bits, e_token, e_val, counts, limit, nullptr, s);
+    return launch_emit<false>(c, lo, hi, big_lo, entry_off, len, pos_bits, e_token, e_val, counts, limit,
+                              BoundFields{}, s);
 }
 
 cudaError_t emit_records(CollView c, const uint32_t* prefix_tab, uint32_t pos_bits, uint32_t* counts, uint32_t* rec,
-                         uint32_t limit, cudaStream_t s, uint32_t lo, uint32_t hi, const uint32_t* max_sum,
+                         uint32_t limit, cudaStream_t s, uint32_t lo, uint32_t hi, BoundFields bf,
                          uint32_t big_lo) {
-    return launch_emit<true>(c, lo, hi, big_lo, nullptr, prefix_tab, pos_bits, nullptr, rec, counts, limit, max_sum, s);
+    return launch_emit<true>(c, lo, hi, big_lo, nullptr, prefix_tab, pos_bits, nullptr, rec, counts, limit, bf, s);
 }
 
 cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cudaStream_t s, uint32_t* overflow,
@@ -1030,11 +1031,11 @@ cudaError_t order_records(const uint32_t* counts, uint32_t U, uint32_t* rec, cud
 }
 
 cudaError_t records_from_lists(const uint32_t* list_off, const uint32_t* vals, uint32_t U, uint32_t* rec,
-                               cudaStream_t s, const uint32_t* max_sum, const uint32_t* sizes, uint32_t list_bits,
+                               cudaStream_t s, BoundFields bf, const uint32_t* sizes, uint32_t list_bits,
                                uint32_t rec_bits) {
     if (U == 0) return cudaSuccess;
     note_launches();
-    k_records_from_lists<<<grid_for((uint64_t)U * 32, 256), 256, 0, s>>>(list_off, vals, U, rec, max_sum, sizes,
+    k_records_from_lists<<<grid_for((uint64_t)U * 32, 256), 256, 0, s>>>(list_off, vals, U, rec, bf, sizes,
                                                                          list_bits, rec_bits);
     return cudaGetLastError();
 }
