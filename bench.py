@@ -121,8 +121,13 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per launch of the join kernel from the committed ncu summary, if present."""
+def ncu_traffic(sim, n_sets, bits, batch):
+    """DRAM bytes per launch of the join kernel from the committed ncu summary,
+    when this run's workload and kernel configuration are the ones captured
+    there (the full 1M-set Jaccard workload, 512-bit signatures, probe batch
+    6); otherwise None."""
+    if sim != "jaccard" or n_sets or bits != 512 or batch != 6:
+        return None
     try:
         with open(os.path.join(ROOT, "profiles", "join_kernel_c3_traffic.json")) as f:
             return json.load(f).get("dram_bytes_per_launch")
@@ -347,7 +352,7 @@ def run_ours(args, ws, rank, local):
         alg = algorithmic_bytes(st, st_run.count, words, p_hi - p_lo)
         kms = statistics.mean(kern_ms)
         achieved = alg / (kms / 1000.0) / 1e9
-        traffic = ncu_traffic()
+        traffic = ncu_traffic(args.sim, args.sets, st_run.bitmap_bits, st_run.probe_batch) if ws == 1 else None
         cpu = {"value": None}
         if not args.no_cpu:
             n_cpu, join_s, idx_s, wall = cpu_baseline(c, 1, "", args.sim)
