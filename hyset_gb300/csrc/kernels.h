@@ -191,10 +191,11 @@ cudaError_t size_scan(const uint32_t* sizes, const uint32_t* starts, bool starts
 
 // The same pass writes meta[i] = (starts[i], sizes[i]).
 cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, cudaStream_t s);
-// validate_collection and generate_bitmaps (words in {1, 2, 4, 8}) in one pass
-// over the tokens.
+// validate_collection and generate_bitmaps (words in {1, 2, 4, 8, 16}) in one
+// pass over the tokens; min_size (optional): no set of c is shorter (sizes are
+// ordered), parts of long sets are read a warp per set.
 cudaError_t validate_with_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, int words, uint64_t* out,
-                                  cudaStream_t s);
+                                  cudaStream_t s, uint32_t min_size = 0);
 
 // XOR bitmap signatures, bit (token mod bits) per token
 // (include/hyset/device_algorithms.hpp:58-74), words = bits / 64 in {1,2,4,8}.

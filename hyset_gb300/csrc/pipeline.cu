@@ -483,7 +483,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             // the checks (and the signatures, in the same pass over the tokens)
             if (words)
                 CK(validate_with_bitmaps(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, words,
-                                         bits.as<uint64_t>() + (size_t)lo * words, s));
+                                         bits.as<uint64_t>() + (size_t)lo * words, s, size_at(C, lo)));
             else
                 CK(validate_collection(part, n_tokens, ctx->s_flags.as<uint32_t>(), C->meta.as<uint2>() + lo, s));
             if (records)

@@ -701,25 +701,29 @@ __global__ void __launch_bounds__(BITMAP_THREADS) k_bitmaps(CollView c, uint64_t
 }
 
 // The checks of k_validate and the signatures of k_bitmaps in one pass over
-// the tokens of the sets of c (eight lanes per set, as k_bitmaps): the set's
-// meta pair is written from its start and size, and its tokens are read once
-// for both (the order check reads each token's successor, an L1 hit).
-template <int W>
+// the tokens of the sets of c (LPS lanes per set: eight as k_bitmaps, or a
+// warp for parts of long sets, which would otherwise leave most SMs idle):
+// the set's meta pair is written from its start and size, and its tokens are
+// read once for both (the order check reads each token's successor, an L1
+// hit).
+template <int W, int LPS>
 __global__ void __launch_bounds__(BITMAP_THREADS) k_validate_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags,
                                                                     uint2* meta, uint64_t* out) {
+    static_assert(LPS == 8 || LPS == 32, "lanes per set");
     constexpr int NW = 2 * W;
-    __shared__ uint32_t sw[BITMAP_THREADS / 8][NW];
-    const int lane = threadIdx.x & 31, g = lane & 7;
-    uint32_t* mine = sw[threadIdx.x >> 3];
+    constexpr int SH = LPS == 8 ? 3 : 5;
+    __shared__ uint32_t sw[BITMAP_THREADS / LPS][NW];
+    const int lane = threadIdx.x & 31, g = lane & (LPS - 1);
+    uint32_t* mine = sw[threadIdx.x >> SH];
     const uint32_t mask = 64u * W - 1u;
-    const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
+    const uint32_t groups = (gridDim.x * blockDim.x) >> SH;
     uint32_t* out32 = reinterpret_cast<uint32_t*>(out);
     uint32_t f = 0, mx = 0;
     const uint32_t rounds = (c.n + groups - 1) / groups;  // the same for every lane: the warp barriers match
-    uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> SH;
     for (uint32_t r = 0; r < rounds; ++r, s += groups) {
 #pragma unroll
-        for (int q = g; q < NW; q += 8) mine[q] = 0u;
+        for (int q = g; q < NW; q += LPS) mine[q] = 0u;
         __syncwarp();
         const bool live = s < c.n;
         uint32_t st = 0, l = 0;
@@ -737,17 +741,17 @@ __global__ void __launch_bounds__(BITMAP_THREADS) k_validate_bitmaps(CollView c,
             }
         }
         const uint32_t* t = c.tokens + st;
-        for (uint32_t i0 = g; i0 < l; i0 += 8 * BITMAP_UNROLL) {
+        for (uint32_t i0 = g; i0 < l; i0 += LPS * BITMAP_UNROLL) {
             uint32_t tok[BITMAP_UNROLL], nxt[BITMAP_UNROLL];
 #pragma unroll
             for (int u = 0; u < BITMAP_UNROLL; ++u) {
-                const uint32_t i = i0 + 8u * u;
+                const uint32_t i = i0 + (uint32_t)LPS * u;
                 tok[u] = i < l ? __ldg(t + i) : 0xFFFFFFFFu;
                 nxt[u] = i + 1 < l ? __ldg(t + i + 1) : 0xFFFFFFFFu;
             }
 #pragma unroll
             for (int u = 0; u < BITMAP_UNROLL; ++u) {
-                const uint32_t i = i0 + 8u * u;
+                const uint32_t i = i0 + (uint32_t)LPS * u;
                 if (i < l) {
                     if (i + 1 < l && tok[u] >= nxt[u]) f |= 2;
                     const uint32_t b = tok[u] & mask;
@@ -758,7 +762,7 @@ __global__ void __launch_bounds__(BITMAP_THREADS) k_validate_bitmaps(CollView c,
         __syncwarp();
         if (live) {
 #pragma unroll
-            for (int q = g; q < NW; q += 8) out32[(uint64_t)s * NW + q] = mine[q];
+            for (int q = g; q < NW; q += LPS) out32[(uint64_t)s * NW + q] = mine[q];
         }
         __syncwarp();
     }
@@ -1156,20 +1160,30 @@ cudaError_t validate_collection(CollView c, uint64_t n_tokens, uint32_t* flags, 
     return cudaGetLastError();
 }
 
-cudaError_t validate_with_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, int words, uint64_t* out,
-                                  cudaStream_t s) {
-    if (c.n == 0) return cudaSuccess;
-    const unsigned g = grid_for((uint64_t)c.n * 8, BITMAP_THREADS);
+namespace {
+template <int LPS>
+cudaError_t launch_validate_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, int words,
+                                    uint64_t* out, cudaStream_t s) {
+    const unsigned g = grid_for((uint64_t)c.n * LPS, BITMAP_THREADS);
     note_launches();
     switch (words) {
-    case 1: k_validate_bitmaps<1><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
-    case 2: k_validate_bitmaps<2><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
-    case 4: k_validate_bitmaps<4><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
-    case 8: k_validate_bitmaps<8><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
-    case 16: k_validate_bitmaps<16><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 1: k_validate_bitmaps<1, LPS><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 2: k_validate_bitmaps<2, LPS><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 4: k_validate_bitmaps<4, LPS><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 8: k_validate_bitmaps<8, LPS><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
+    case 16: k_validate_bitmaps<16, LPS><<<g, BITMAP_THREADS, 0, s>>>(c, n_tokens, flags, meta, out); break;
     default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t validate_with_bitmaps(CollView c, uint64_t n_tokens, uint32_t* flags, uint2* meta, int words, uint64_t* out,
+                                  cudaStream_t s, uint32_t min_size) {
+    if (c.n == 0) return cudaSuccess;
+    constexpr uint32_t WARP_SET_SIZE = 128;  // sets this long (all of the part) take a warp each
+    return min_size >= WARP_SET_SIZE ? launch_validate_bitmaps<32>(c, n_tokens, flags, meta, words, out, s)
+                                     : launch_validate_bitmaps<8>(c, n_tokens, flags, meta, words, out, s);
 }
 
 cudaError_t generate_bitmaps(CollView c, int words, uint64_t* out, cudaStream_t s, unsigned max_blocks) {
