@@ -193,6 +193,8 @@ cudaError_t dispatch_words(const JoinParams& P, int sm_count, cudaStream_t s) {
 
 }  // namespace
 
+uint32_t join_resident_warps(int sm_count) { return (uint32_t)sm_count * HS_JOIN_MIN_BLOCKS * JOIN_WARPS; }
+
 cudaError_t launch_join(const JoinParams& P, int technique, int vmode, int sm_count, cudaStream_t s) {
     if (P.p_hi <= P.p_lo) return cudaSuccess;
     if (technique == TECH_FGSS)

@@ -247,6 +247,8 @@ enum Technique : int { TECH_BITMAP = 1, TECH_FGSS = 2, TECH_DIRECT = 3 };
 // One persistent, work-stealing launch over probes [p_lo, p_hi).
 // vmode: 1 = lane per candidate, 2 = warp per candidate.
 cudaError_t launch_join(const JoinParams& P, int technique, int vmode, int sm_count, cudaStream_t s);
+// Warps of one launch_join (the blocks per SM its kernels are compiled for).
+uint32_t join_resident_warps(int sm_count);
 
 // ---- join_tm.cu ------------------------------------------------------------
 // Token groups: for every token, the entries (set, pos | size << 16) of the sets
