@@ -14,7 +14,7 @@
 namespace hs {
 
 namespace {
-constexpr uint64_t JOIN_POINT_TOKENS = 24ull << 20;  // a host-input join runs a piece every 96 MB landed
+constexpr uint64_t JOIN_POINT_TOKENS = 20ull << 20;  // a host-input join runs a piece every 80 MB landed
 
 cudaEvent_t nth_event(std::vector<cudaEvent_t>& v, size_t k) {
     while (v.size() <= k) {
