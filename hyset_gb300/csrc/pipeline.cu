@@ -15,6 +15,10 @@ namespace hs {
 
 namespace {
 constexpr uint64_t JOIN_POINT_TOKENS = 20ull << 20;  // a host-input join runs a piece every 80 MB landed
+// The small chunks at the end of the copy are checked and emitted in groups of
+// at least 32 MB (or at a join point): the context's stream is behind the copy
+// by then, and each group costs its launches whatever its size.
+constexpr uint64_t GROUP_MIN_TOKENS = 8ull << 20;
 
 cudaEvent_t nth_event(std::vector<cudaEvent_t>& v, size_t k) {
     while (v.size() <= k) {
@@ -470,10 +474,15 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             SP.stats = o->collect_stats ? ctx->s_stats.as<unsigned long long>() : nullptr;
         }
         uint32_t lo = 0;
+        uint64_t grouped_to = 0;  // the tokens that had landed at the last group
         for (uint64_t k = 0; k < n_chunks && lo < n; ++k) {
+            const bool last = k + 1 == n_chunks;
+            const bool join_point = streamed && (last || ends[k] - joined_to >= JOIN_POINT_TOKENS);
+            if (!last && !join_point && ends[k] - grouped_to < GROUP_MIN_TOKENS) continue;  // with the next group
             // sets whose tokens end inside the chunks copied so far
-            const uint32_t hi = k + 1 == n_chunks ? n : std::max(lo, chunk_hi[k]);
+            const uint32_t hi = last ? n : std::max(lo, chunk_hi[k]);
             CK(cudaStreamWaitEvent(s, pipe_event(ctx, k), 0));
+            grouped_to = ends[k];
             if (hi <= lo) continue;
             CollView part = v;
             part.sizes += lo;
@@ -495,7 +504,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
             // at a join point (the last chunk, or JOIN_POINT_TOKENS since the last
             // one): order the records, then join the probes not joined yet, all
             // in stream order while the next chunks are copied
-            if (streamed && (k + 1 == n_chunks || ends[k] - joined_to >= JOIN_POINT_TOKENS)) {
+            if (join_point) {
                 CK(order_records(counts, U, ix.rec.as<uint32_t>(), s, ctx->s_flags.as<uint32_t>(), prev));
                 if (join_launches == 0) CK(cudaEventRecord(ctx->ek0, s));
                 JoinParams Q = SP;
