@@ -121,18 +121,20 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(sim, n_sets, bits, batch):
-    """DRAM bytes per launch of the join kernel from the committed ncu summary,
-    when this run's workload and kernel configuration are the ones captured
-    there (the full 1M-set Jaccard workload, 512-bit signatures, probe batch
-    6); otherwise None."""
-    if sim != "jaccard" or n_sets or bits != 512 or batch != 6:
-        return None
+def ncu_traffic(sim, n_sets, bits):
+    """DRAM bytes per launch of the join kernel from the committed ncu summary
+    and the configuration it was captured in, when this run's workload and
+    kernel instance are the ones captured there (the full 1M-set Jaccard
+    workload, 512-bit signatures; the probe batch is a launch parameter of the
+    same kernel); otherwise (None, None)."""
+    if sim != "jaccard" or n_sets or bits != 512:
+        return None, None
     try:
         with open(os.path.join(ROOT, "profiles", "join_kernel_c3_traffic.json")) as f:
-            return json.load(f).get("dram_bytes_per_launch")
+            m = json.load(f)
+        return m.get("dram_bytes_per_launch"), m.get("kernel")
     except (OSError, ValueError):
-        return None
+        return None, None
 
 
 def algorithmic_bytes(st, count, words, n_probes):
@@ -352,7 +354,7 @@ def run_ours(args, ws, rank, local):
         alg = algorithmic_bytes(st, st_run.count, words, p_hi - p_lo)
         kms = statistics.mean(kern_ms)
         achieved = alg / (kms / 1000.0) / 1e9
-        traffic = ncu_traffic(args.sim, args.sets, st_run.bitmap_bits, st_run.probe_batch) if ws == 1 else None
+        traffic, traffic_capture = ncu_traffic(args.sim, args.sets, st_run.bitmap_bits) if ws == 1 else (None, None)
         cpu = {"value": None}
         if not args.no_cpu:
             n_cpu, join_s, idx_s, wall = cpu_baseline(c, 1, "", args.sim)
@@ -376,8 +378,9 @@ def run_ours(args, ws, rank, local):
                "batch_leg": batch,
                "parity": parity["parity"], "parity_detail": parity,
                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                            "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                            "algorithmic_bytes_per_launch": alg, "kernel": "k_join (probe-major FGSS filter + verify, persistent)"},
+                            "frac": achieved / peak, "traffic": traffic, "traffic_capture": traffic_capture,
+                            "peak_kind": peak_kind, "algorithmic_bytes_per_launch": alg,
+                            "kernel": "k_join (probe-major FGSS filter + verify, persistent)"},
                "cpu_baseline": cpu,
                "e2e": {"value": e2e_value, "unit": "pairs/s", "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": e2e_pairs_bytes + 8, "ms_per_step": 1000.0 * e2e_mean},

@@ -514,7 +514,7 @@ hyset_status hyset_self_join_host(hyset_ctx* ctx, const uint32_t* tokens, uint64
                 // four probe batches per warp the launch ends on its slowest
                 // warps, so their batches are halved (down to 3)
                 while (Q.grab > 3 && (uint64_t)(hi - join_lo) < 4ull * Q.grab * join_resident_warps(ctx->sm_count))
-                    Q.grab = (Q.grab + 1) / 2;
+                    Q.grab = std::max(3u, (Q.grab + 1) / 2);
                 Q.work = ctx->s_work.as<unsigned int>() + 2 * join_launches;  // probe batches, split probes
                 CK(launch_join(Q, TECH_FGSS, tn.vmode, ctx->sm_count, s));
                 ++join_launches;

@@ -293,7 +293,7 @@ constexpr uint32_t TUNE_SAMPLE = 16384;  // a sample fills the GPU for about two
 constexpr float TUNE_MARGIN = 0.92f;  // leave the rule's width only for an estimated gain of 8 % or more
 constexpr float TUNE_VMODE_MARGIN = 0.97f;  // warp verification only for an estimated gain of 3 % or more
 constexpr float TUNE_BATCH_MARGIN = 0.97f;  // a probe batch other than the default only for a gain of 3 % or more
-constexpr uint32_t TUNE_BATCHES[] = {1, 2, 3, 4, 6};  // probe batches the autotuner times
+constexpr uint32_t TUNE_BATCHES[] = {1, 2, 3, 4, 6, 8, 12};  // probe batches the autotuner times
 constexpr float TUNE_BATCH_FULL_MS = 40.0f;  // batches are timed over the whole range up to this estimate
 }  // namespace
 
